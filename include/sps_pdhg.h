@@ -1,0 +1,151 @@
+/*
+ * sps_pdhg.h — C ABI of the GB300 restarted-PDHG LP engine (libsps_gb300.so).
+ *
+ * The reference has no native boundary: its hot path is the Python call
+ *   solve_lp_pdhg(problem, max_iters, tol)          solver/lp/pdhg.py:152-156
+ *   solve_lp_pdhg_gpu(problem, device, max_iters, tol)  solver/lp/pdhg_gpu.py:315-320
+ * reached from Solver.solve(method='pdhg' | 'pdhg_gpu')   solver/solver.py:113-119.
+ * These entry points are what a binding for that call binds (ctypes in
+ * sovereign-solver_gb300/_native.py).  The problem descriptor carries the
+ * reference Problem fields (solver/problem.py:57-64) as plain arrays.
+ *
+ * Conventions
+ *  - Every function returns 0 (SPS_OK) or a negative SPS_ERR_* code and never
+ *    aborts or traps; sps_last_error() gives the message.
+ *  - Host arrays are read during the call only (copied to the device).
+ *  - One handle per thread; calls on one handle are serialised by the caller.
+ *  - No CPU fallback: without a usable sm_103a device sps_create fails with
+ *    SPS_ERR_CUDA.
+ */
+#ifndef SPS_PDHG_H
+#define SPS_PDHG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* return codes */
+#define SPS_OK               0
+#define SPS_ERR_INVALID     -1   /* malformed input (shapes, indices, NaN, lb > ub) */
+#define SPS_ERR_CUDA        -2   /* CUDA runtime error or no usable device */
+#define SPS_ERR_OOM         -3   /* device allocation failed */
+#define SPS_ERR_STATE       -4   /* call out of order (e.g. get_solution before solve) */
+#define SPS_ERR_TIMEOUT     -5   /* host watchdog expired and the device did not stop */
+
+/* solve status (sps_result.status) — solver/lp/simplex_dense.py:49 names */
+#define SPS_STATUS_OPTIMAL          0   /* relative KKT error < tol */
+#define SPS_STATUS_ITERATION_LIMIT  1
+#define SPS_STATUS_TIME_LIMIT       2
+#define SPS_STATUS_NUMERIC_ERROR    3   /* NaN/Inf appeared in the iterates */
+
+/* algorithm */
+#define SPS_MODE_REFERENCE  0  /* the reference's rules: standard form with bound rows and
+                                  slacks, fixed diagonal steps, theta = 1, ergodic average,
+                                  KKT of the average every 50 iterations, restart on halving
+                                  (solver/lp/pdhg.py:62-259) */
+#define SPS_MODE_ADAPTIVE   1  /* box form, Ruiz + Pock-Chambolle scaling, adaptive steps,
+                                  primal weight, KKT-based restarts to average or current */
+
+#define SPS_FP32  0  /* FP32 iterates and SpMV, FP64 checks */
+#define SPS_FP64  1  /* FP64 everywhere */
+
+typedef struct {
+    int32_t n;                      /* variables */
+    int32_t m_ub;                   /* rows of A_ub x <= b_ub */
+    int32_t m_eq;                   /* rows of A_eq x == b_eq */
+    const int32_t *ub_indptr;       /* CSR of A_ub: m_ub+1 offsets */
+    const int32_t *ub_indices;      /*   column of each nonzero */
+    const double  *ub_values;       /*   value of each nonzero */
+    const int32_t *eq_indptr;       /* CSR of A_eq */
+    const int32_t *eq_indices;
+    const double  *eq_values;
+    const double  *c;               /* n, objective of the minimisation */
+    const double  *b_ub;            /* m_ub */
+    const double  *b_eq;            /* m_eq */
+    const double  *lb;              /* n, -INFINITY allowed */
+    const double  *ub;              /* n, +INFINITY allowed */
+} sps_problem_desc;
+
+typedef struct {
+    int32_t mode;             /* SPS_MODE_* (default ADAPTIVE) */
+    int32_t precision;        /* SPS_FP32 / SPS_FP64 (default FP32) */
+    int64_t max_iters;        /* default 100000 (solver/config.py:37) */
+    double  tol;              /* relative KKT tolerance, default 1e-6 (solver/config.py:12) */
+    int32_t check_interval;   /* iterations between KKT checks; 0 = 50 (reference) / 64 (adaptive) */
+    int32_t ruiz_iters;       /* adaptive mode: Ruiz passes before Pock-Chambolle, default 10 */
+    double  time_limit_s;     /* 0 = none; enforced on the device clock and by the host watchdog */
+    int32_t graph_mode;       /* 0 = plain launches, 1 = replayed window graph,
+                                 2 = one graph with a device-driven while loop (default) */
+    int32_t device;           /* CUDA device ordinal */
+    int32_t row_lanes_cta;    /* schedule tuning: rows longer than this use a whole block (default 1024) */
+    int32_t reserved[6];
+} sps_options;
+
+typedef struct {
+    int32_t status;           /* SPS_STATUS_* */
+    int32_t restarts;
+    int64_t iterations;       /* PDHG iterations run (adaptive: step attempts) */
+    int64_t accepted_steps;   /* adaptive mode: accepted attempts */
+    double  objective;        /* c^T x of the returned x (minimisation c), FP64 */
+    double  rel_kkt;          /* max(rel_primal, rel_dual, rel_gap) of the returned point */
+    double  rel_primal;
+    double  rel_dual;
+    double  rel_gap;
+    double  primal_weight;    /* adaptive mode: final omega */
+    double  step_size;        /* adaptive mode: final eta */
+    double  setup_ms;         /* sps_create device work (upload, layout, scaling) */
+    double  solve_ms;         /* device time of sps_solve */
+    int64_t kernel_launches;  /* kernels launched by sps_solve (graph nodes executed count once per run) */
+    int32_t returned_average; /* 1 if the returned point is the ergodic average */
+    int32_t reserved[5];
+} sps_result;
+
+typedef struct sps_handle sps_handle;
+
+/* Fill *opt with defaults. */
+int sps_options_init(sps_options *opt);
+
+/* Upload a problem, build the device layout (row/column-binned CSR and CSC),
+ * scale it, and allocate iterate storage.  Replaces the reference's
+ * _to_standard_form_pdhg + _compute_step_sizes + DeviceEngine.prepare_data
+ * (solver/lp/pdhg.py:62-147, solver/lp/pdhg_gpu.py:123-194). */
+int sps_create(const sps_problem_desc *prob, const sps_options *opt, sps_handle **out);
+
+/* Start the next solve from (x0, y0) in the original space (either may be
+ * NULL = zero) with primal weight omega0 (<= 0 = default).  Adaptive mode only.
+ * New API surface: the reference always starts from zero (solver/lp/pdhg.py:175-176). */
+int sps_set_warm_start(sps_handle *h, const double *x0, const double *y0, double omega0);
+
+/* Run restarted PDHG to tolerance or limit; blocking.  Replaces the iteration
+ * loop of solve_lp_pdhg / solve_lp_pdhg_gpu (solver/lp/pdhg.py:209-244,
+ * solver/lp/pdhg_gpu.py:378-427). */
+int sps_solve(sps_handle *h, sps_result *res);
+
+/* Copy the solution of the last solve into caller buffers (either may be NULL):
+ * x (n) in the original space, clipped to [lb, ub] as solver/lp/pdhg.py:247-253;
+ * y (m_ub + m_eq) duals of the A_ub rows then the A_eq rows. */
+int sps_get_solution(sps_handle *h, double *x, double *y);
+
+/* Message of the last error on this handle (or of the last failed sps_create when h is NULL). */
+const char *sps_last_error(const sps_handle *h);
+
+void sps_destroy(sps_handle *h);
+
+/* Page-lock / release caller host memory so uploads run at full link speed. */
+int sps_pin_host(void *ptr, uint64_t bytes);
+int sps_unpin_host(void *ptr);
+
+/* Library build string (arch, precision support). */
+const char *sps_version(void);
+
+/* Number of visible CUDA devices (0 when none or the driver is unusable).
+ * Backs get_available_device (solver/lp/pdhg_gpu.py:42-67), without its
+ * CuPy/MPS/CPU probing. */
+int sps_device_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPS_PDHG_H */

@@ -3,11 +3,15 @@
 
 Public names mirror the reference package exports (``solver/__init__.py:22-38``)
 for this path: ``Solver``, ``Problem``, ``SolveResult``, ``solve_lp_pdhg``,
-``solve_lp_pdhg_gpu``, ``get_available_device``.
+``solve_lp_pdhg_gpu``, ``get_available_device``; plus ``PDHGEngine`` (a problem
+kept resident on the GPU for repeated / warm-started solves).
 """
 
 from .problem import Problem
 from .result import SolveResult
+from .pdhg import PDHGEngine, get_available_device, solve_lp_pdhg, solve_lp_pdhg_gpu
+from .solver import Solver
 
 __version__ = "0.1.0"
-__all__ = ["Problem", "SolveResult"]
+__all__ = ["Solver", "Problem", "SolveResult", "PDHGEngine", "solve_lp_pdhg",
+           "solve_lp_pdhg_gpu", "get_available_device"]

@@ -1,0 +1,272 @@
+// api.cu — extern "C" entry points of libsps_gb300.so (declared in
+// include/sps_pdhg.h): input validation, the reference standard-form
+// conversion for SPS_MODE_REFERENCE, and handle management.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "engine_impl.cuh"
+
+using namespace sps;
+
+struct sps_handle {
+    EngineBase* eng = nullptr;
+};
+
+namespace {
+
+thread_local std::string g_create_error;
+
+int create_fail(int code, const std::string& msg) {
+    g_create_error = msg;
+    return code;
+}
+
+bool check_csr(const int32_t* ptr, const int32_t* idx, const double* val, int32_t rows, std::string& why,
+               const char* name) {
+    if (rows == 0) return true;
+    if (!ptr) { why = std::string(name) + ": null indptr"; return false; }
+    if (ptr[0] != 0) { why = std::string(name) + ": indptr[0] != 0"; return false; }
+    for (int32_t i = 0; i < rows; ++i)
+        if (ptr[i + 1] < ptr[i]) { why = std::string(name) + ": indptr not monotone"; return false; }
+    if (ptr[rows] > 0 && (!idx || !val)) { why = std::string(name) + ": null indices/values"; return false; }
+    return true;
+}
+
+bool finite_all(const double* v, int64_t len) {
+    for (int64_t i = 0; i < len; ++i)
+        if (!std::isfinite(v[i])) return false;
+    return true;
+}
+
+// Validation shared by both modes (solver/problem.py:103-142 plus the engine's
+// own requirements: finite c and rhs, no lb = +inf / ub = -inf).
+int validate(const sps_problem_desc* d) {
+    if (!d) return create_fail(SPS_ERR_INVALID, "null problem descriptor");
+    if (d->n < 0 || d->m_ub < 0 || d->m_eq < 0) return create_fail(SPS_ERR_INVALID, "negative dimension");
+    std::string why;
+    if (!check_csr(d->ub_indptr, d->ub_indices, d->ub_values, d->m_ub, why, "A_ub") ||
+        !check_csr(d->eq_indptr, d->eq_indices, d->eq_values, d->m_eq, why, "A_eq"))
+        return create_fail(SPS_ERR_INVALID, why);
+    if ((int64_t)(d->m_ub ? d->ub_indptr[d->m_ub] : 0) + (d->m_eq ? d->eq_indptr[d->m_eq] : 0) > INT32_MAX)
+        return create_fail(SPS_ERR_INVALID, "more than 2^31-1 nonzeros");
+    if (d->n > 0 && (!d->c || !d->lb || !d->ub)) return create_fail(SPS_ERR_INVALID, "null c/lb/ub");
+    if ((d->m_ub && !d->b_ub) || (d->m_eq && !d->b_eq)) return create_fail(SPS_ERR_INVALID, "null rhs");
+    if (!finite_all(d->c, d->n)) return create_fail(SPS_ERR_INVALID, "non-finite objective coefficient");
+    if (!finite_all(d->b_ub, d->m_ub) || !finite_all(d->b_eq, d->m_eq))
+        return create_fail(SPS_ERR_INVALID, "non-finite right-hand side");
+    for (int32_t j = 0; j < d->n; ++j) {
+        const double l = d->lb[j], u = d->ub[j];
+        if (std::isnan(l) || std::isnan(u) || l == INFINITY || u == -INFINITY || l > u + 1e-12)
+            return create_fail(SPS_ERR_INVALID, "invalid bounds at variable " + std::to_string(j));
+    }
+    return SPS_OK;
+}
+
+// Box form as given: K = [A_ub; A_eq], rows of A_ub are '<='.
+void build_box(const sps_problem_desc* d, HostProblem& hp) {
+    const int32_t mu = d->m_ub, me = d->m_eq;
+    const int32_t nub = mu ? d->ub_indptr[mu] : 0, neq = me ? d->eq_indptr[me] : 0;
+    hp.n = d->n;
+    hp.m = mu + me;
+    hp.ptr.resize(hp.m + 1);
+    hp.ptr[0] = 0;
+    for (int32_t i = 0; i < mu; ++i) hp.ptr[i + 1] = d->ub_indptr[i + 1];
+    for (int32_t i = 0; i < me; ++i) hp.ptr[mu + i + 1] = nub + d->eq_indptr[i + 1];
+    hp.segs = {{d->ub_indices, d->ub_values, nub}, {d->eq_indices, d->eq_values, neq}};
+    hp.kind.assign(hp.m, 0);
+    for (int32_t i = 0; i < mu; ++i) hp.kind[i] = 1;
+    hp.c = d->c;
+    hp.lb = d->lb;
+    hp.ub = d->ub;
+    hp.rhs.resize(hp.m);
+    for (int32_t i = 0; i < mu; ++i) hp.rhs[i] = d->b_ub[i];
+    for (int32_t i = 0; i < me; ++i) hp.rhs[mu + i] = d->b_eq[i];
+}
+
+// Reference standard form (solver/lp/pdhg.py:62-125): shift by finite lb,
+// one '<=' row per finite ub (column order), a slack per '<=' row, rows with
+// rhs < -1e-6 negated; every row '=', every column in [0, inf).
+void build_standard(const sps_problem_desc* d, HostProblem& hp, StdMap& s) {
+    const int32_t n = d->n, mu = d->m_ub, me = d->m_eq;
+    s.n_orig = n;
+    s.m_ub = mu;
+    s.m_eq = me;
+    s.lb_shift.resize(n);
+    for (int32_t j = 0; j < n; ++j) s.lb_shift[j] = std::isfinite(d->lb[j]) ? d->lb[j] : 0.0;
+    s.ub_cols.clear();
+    for (int32_t j = 0; j < n; ++j)
+        if (std::isfinite(d->ub[j])) s.ub_cols.push_back(j);
+    s.nub = (int32_t)s.ub_cols.size();
+    const int32_t m_le = mu + s.nub, m = m_le + me, ns = n + m_le;
+    const int64_t nz_ub = mu ? d->ub_indptr[mu] : 0, nz_eq = me ? d->eq_indptr[me] : 0;
+    const int64_t nz = nz_ub + nz_eq + 2LL * s.nub + mu;
+    hp.own_idx.resize(nz);
+    hp.own_val.resize(nz);
+    hp.ptr.assign(m + 1, 0);
+    hp.rhs.assign(m, 0.0);
+    int64_t k = 0;
+    auto row_dot_shift = [&](const int32_t* ip, const int32_t* ix, const double* vv, int32_t i) {
+        double acc = 0.0;
+        for (int32_t q = ip[i]; q < ip[i + 1]; ++q) acc += vv[q] * s.lb_shift[ix[q]];
+        return acc;
+    };
+    for (int32_t i = 0; i < mu; ++i) {
+        for (int32_t q = d->ub_indptr[i]; q < d->ub_indptr[i + 1]; ++q) {
+            hp.own_idx[k] = d->ub_indices[q];
+            hp.own_val[k++] = d->ub_values[q];
+        }
+        hp.own_idx[k] = n + i;
+        hp.own_val[k++] = 1.0;
+        hp.ptr[i + 1] = (int32_t)k;
+        hp.rhs[i] = d->b_ub[i] - row_dot_shift(d->ub_indptr, d->ub_indices, d->ub_values, i);
+    }
+    for (int32_t t = 0; t < s.nub; ++t) {
+        const int32_t j = s.ub_cols[t];
+        hp.own_idx[k] = j;
+        hp.own_val[k++] = 1.0;
+        hp.own_idx[k] = n + mu + t;
+        hp.own_val[k++] = 1.0;
+        hp.ptr[mu + t + 1] = (int32_t)k;
+        hp.rhs[mu + t] = d->ub[j] - s.lb_shift[j];
+    }
+    for (int32_t i = 0; i < me; ++i) {
+        for (int32_t q = d->eq_indptr[i]; q < d->eq_indptr[i + 1]; ++q) {
+            hp.own_idx[k] = d->eq_indices[q];
+            hp.own_val[k++] = d->eq_values[q];
+        }
+        hp.ptr[m_le + i + 1] = (int32_t)k;
+        hp.rhs[m_le + i] = d->b_eq[i] - row_dot_shift(d->eq_indptr, d->eq_indices, d->eq_values, i);
+    }
+    s.neg.assign(m, 0);
+    for (int32_t i = 0; i < m; ++i) {
+        if (hp.rhs[i] < -1e-6) {
+            s.neg[i] = 1;
+            hp.rhs[i] = -hp.rhs[i];
+            for (int32_t q = hp.ptr[i]; q < hp.ptr[i + 1]; ++q) hp.own_val[q] = -hp.own_val[q];
+        }
+    }
+    hp.n = ns;
+    hp.m = m;
+    hp.segs = {{hp.own_idx.data(), hp.own_val.data(), k}};
+    hp.kind.assign(m, 0);
+    hp.own_c.assign(ns, 0.0);
+    for (int32_t j = 0; j < n; ++j) hp.own_c[j] = d->c[j];
+    hp.own_lb.assign(ns, 0.0);
+    hp.own_ub.assign(ns, INFINITY);
+    hp.c = hp.own_c.data();
+    hp.lb = hp.own_lb.data();
+    hp.ub = hp.own_ub.data();
+}
+
+}  // namespace
+
+extern "C" {
+
+int sps_options_init(sps_options* o) {
+    if (!o) return SPS_ERR_INVALID;
+    std::memset(o, 0, sizeof(*o));
+    o->mode = SPS_MODE_ADAPTIVE;
+    o->precision = SPS_FP32;
+    o->max_iters = 100000;
+    o->tol = 1e-6;
+    o->check_interval = 0;
+    o->ruiz_iters = 10;
+    o->time_limit_s = 0.0;
+    o->graph_mode = 2;
+    o->device = 0;
+    o->row_lanes_cta = 1024;
+    return SPS_OK;
+}
+
+int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_handle** out) {
+    g_create_error.clear();
+    if (!out) return create_fail(SPS_ERR_INVALID, "null output handle pointer");
+    *out = nullptr;
+    sps_options opt;
+    if (opt_in) opt = *opt_in; else sps_options_init(&opt);
+    if (opt.mode != SPS_MODE_REFERENCE && opt.mode != SPS_MODE_ADAPTIVE)
+        return create_fail(SPS_ERR_INVALID, "unknown mode");
+    if (opt.precision != SPS_FP32 && opt.precision != SPS_FP64)
+        return create_fail(SPS_ERR_INVALID, "unknown precision");
+    if (opt.max_iters < 0 || !(opt.tol >= 0) || opt.check_interval < 0 || opt.time_limit_s < 0)
+        return create_fail(SPS_ERR_INVALID, "invalid options");
+    if (int rc = validate(prob)) return rc;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= opt.device || opt.device < 0) {
+        cudaGetLastError();
+        return create_fail(SPS_ERR_CUDA, "no usable CUDA device");
+    }
+    HostProblem hp;
+    StdMap sm;
+    if (opt.mode == SPS_MODE_REFERENCE) build_standard(prob, hp, sm);
+    else build_box(prob, hp);
+
+    sps_handle* h = new sps_handle();
+    h->eng = opt.precision == SPS_FP32 ? make_engine_f32() : make_engine_f64();
+    EngineBase* e = h->eng;
+    e->n_user = prob->n;
+    e->m_user = prob->m_ub + prob->m_eq;
+    e->c_user.assign(prob->c, prob->c + prob->n);
+    e->lb_user.assign(prob->lb, prob->lb + prob->n);
+    e->ub_user.assign(prob->ub, prob->ub + prob->n);
+    e->smap = sm;
+    const int rc = opt.precision == SPS_FP32 ? setup_f32(e, hp, opt, opt.mode) : setup_f64(e, hp, opt, opt.mode);
+    if (rc != SPS_OK) {
+        g_create_error = e->err;
+        delete e;
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return SPS_OK;
+}
+
+int sps_set_warm_start(sps_handle* h, const double* x0, const double* y0, double omega0) {
+    if (!h) return SPS_ERR_INVALID;
+    return h->eng->warm(x0, y0, omega0);
+}
+
+int sps_solve(sps_handle* h, sps_result* res) {
+    if (!h || !res) return SPS_ERR_INVALID;
+    h->eng->err.clear();
+    return h->eng->solve(res);
+}
+
+int sps_get_solution(sps_handle* h, double* x, double* y) {
+    if (!h) return SPS_ERR_INVALID;
+    return h->eng->get(x, y);
+}
+
+const char* sps_last_error(const sps_handle* h) {
+    return h ? h->eng->err.c_str() : g_create_error.c_str();
+}
+
+void sps_destroy(sps_handle* h) {
+    if (!h) return;
+    delete h->eng;
+    delete h;
+}
+
+int sps_pin_host(void* ptr, uint64_t bytes) {
+    if (!ptr || !bytes) return SPS_ERR_INVALID;
+    return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? SPS_OK : SPS_ERR_CUDA;
+}
+
+int sps_unpin_host(void* ptr) {
+    if (!ptr) return SPS_ERR_INVALID;
+    return cudaHostUnregister(ptr) == cudaSuccess ? SPS_OK : SPS_ERR_CUDA;
+}
+
+const char* sps_version(void) { return "libsps_gb300 0.1 (sm_103a; FP32/FP64 iterates; reference + adaptive PDHG)"; }
+
+int sps_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+}  // extern "C"

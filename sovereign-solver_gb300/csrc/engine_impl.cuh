@@ -1,0 +1,727 @@
+// engine_impl.cuh — host side of one solver handle: device layout build,
+// solve driver (plain launches, a replayed window graph, or one graph with a
+// device-driven while loop), watchdog, and solution extraction.
+#pragma once
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "setup.cuh"
+
+namespace sps {
+
+// Problem handed to the device: rows of kind '<=' or '=', box bounds per column.
+struct HostProblem {
+    int32_t n = 0, m = 0;
+    std::vector<int32_t> ptr;                    // m + 1
+    struct Seg { const int32_t* idx; const double* val; int64_t cnt; };
+    std::vector<Seg> segs;                       // nonzeros, concatenated in row order
+    std::vector<int8_t> kind;                    // m: 1 = '<=' row
+    const double *c = nullptr, *lb = nullptr, *ub = nullptr;
+    std::vector<double> rhs;                     // m
+    std::vector<int32_t> own_idx;                // storage of a built standard form
+    std::vector<double> own_val, own_c, own_lb, own_ub;
+};
+
+// Map between the caller's problem and the reference standard form.
+struct StdMap {
+    int32_t n_orig = 0, m_ub = 0, m_eq = 0, nub = 0;
+    std::vector<int32_t> ub_cols;
+    std::vector<int8_t> neg;
+    std::vector<double> lb_shift;
+};
+
+struct EngineBase {
+    // caller problem (for extraction)
+    int32_t n_user = 0, m_user = 0;
+    std::vector<double> c_user, lb_user, ub_user;
+    StdMap smap;
+    virtual ~EngineBase() {}
+    virtual int solve(sps_result* res) = 0;
+    virtual int warm(const double* x0, const double* y0, double omega0) = 0;
+    virtual int get(double* x, double* y) = 0;
+    std::string err;
+    int fail(int code, const std::string& msg) { err = msg; return code; }
+};
+
+#define SPS_CK(call)                                                                        \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(e_ == cudaErrorMemoryAllocation ? SPS_ERR_OOM : SPS_ERR_CUDA,       \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+inline int lane_class(int64_t len, int cta_threshold) {
+    if (len <= 4) return 0;
+    if (len <= 8) return 1;
+    if (len <= 16) return 2;
+    if (len <= 32) return 3;
+    if (len <= 64) return 4;
+    if (len <= cta_threshold) return 5;
+    return 6;
+}
+constexpr int kClassLanes[7] = {1, 2, 4, 8, 16, 32, 0};
+constexpr int kSms = 152;
+
+template <class V>
+struct Engine : EngineBase {
+    sps_options opt{};
+    int mode = SPS_MODE_ADAPTIVE;
+    int32_t n = 0, m = 0;
+    int64_t nnz = 0;
+    bool trivial = false;
+
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evq = nullptr;
+    char* arena = nullptr;
+    Ctl* d_ctl = nullptr;
+    Ctl* h_ctl = nullptr;               // pinned read-back
+    int32_t* h_abort = nullptr;         // mapped host flag
+    int32_t* d_abort = nullptr;
+    int32_t *d_perm_row = nullptr, *d_perm_col = nullptr;
+    int8_t* d_rkind = nullptr;
+    double *d_xout = nullptr, *d_yout = nullptr, *d_wx = nullptr, *d_wy = nullptr;
+    bool have_warm_x = false, have_warm_y = false;
+    double warm_omega = 0.0;
+    double eta0 = 1.0, omega0 = 1.0;
+    Args<V> args{};
+    cudaGraphExec_t win_exec = nullptr, loop_exec = nullptr;
+    int64_t launches = 0;
+    double setup_ms = 0.0;
+    std::vector<double> x_sol, y_sol;
+    bool solved = false;
+
+    ~Engine() override {
+        if (win_exec) cudaGraphExecDestroy(win_exec);
+        if (loop_exec) cudaGraphExecDestroy(loop_exec);
+        if (arena) cudaFree(arena);
+        if (h_ctl) cudaFreeHost(h_ctl);
+        if (h_abort) cudaFreeHost(h_abort);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (evq) cudaEventDestroy(evq);
+        if (st) cudaStreamDestroy(st);
+    }
+
+    static int grid_for(int64_t work, int per_block = kBlock, int cap = kSms * 16) {
+        int64_t g = (work + per_block - 1) / per_block;
+        return (int)std::max<int64_t>(1, std::min<int64_t>(g, cap));
+    }
+
+    // Bins over a permuted index range.  cls[i] = kind*8 + lane class.
+    static void make_bins(const std::vector<int64_t>& count, const std::vector<int64_t>& nz, BinTable& bt,
+                          int target_nnz_per_block) {
+        bt = BinTable{};
+        int begin = 0, blocks = 0;
+        for (int key = 0; key < 16; ++key) {
+            if (count[key] == 0) continue;
+            Bin b{};
+            b.begin = begin;
+            b.end = begin + (int)count[key];
+            b.kind = key >> 3;
+            b.lanes = kClassLanes[key & 7];
+            const int64_t units = b.lanes ? (count[key] + (kBlock / b.lanes) - 1) / (kBlock / b.lanes) : count[key];
+            int64_t nb = (nz[key] + target_nnz_per_block - 1) / target_nnz_per_block;
+            nb = std::max<int64_t>(1, std::min<int64_t>(nb, units));
+            b.block_begin = blocks;
+            b.nblocks = (int)nb;
+            blocks += (int)nb;
+            begin = b.end;
+            bt.bin[bt.nbins++] = b;
+        }
+        bt.total_blocks = blocks;
+    }
+
+    int setup(const HostProblem& hp, const sps_options& o, int mode_) {
+        opt = o;
+        mode = mode_;
+        n = hp.n;
+        m = hp.m;
+        nnz = hp.ptr[m];
+        SPS_CK(cudaSetDevice(opt.device));
+        SPS_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        SPS_CK(cudaEventCreate(&ev0));
+        SPS_CK(cudaEventCreate(&ev1));
+        SPS_CK(cudaEventCreateWithFlags(&evq, cudaEventDisableTiming));
+        SPS_CK(cudaHostAlloc((void**)&h_ctl, sizeof(Ctl), cudaHostAllocDefault));
+        SPS_CK(cudaHostAlloc((void**)&h_abort, sizeof(int32_t), cudaHostAllocMapped));
+        *h_abort = 0;
+        SPS_CK(cudaHostGetDevicePointer((void**)&d_abort, h_abort, 0));
+        if (m == 0 || n == 0) { trivial = true; return SPS_OK; }
+        SPS_CK(cudaEventRecord(ev0, st));
+
+        const int cta = opt.row_lanes_cta > 64 ? opt.row_lanes_cta : 1024;
+        // ---- row order: stable counting sort by (kind, lane class)
+        std::vector<int64_t> rcount(16, 0), rnz(16, 0);
+        std::vector<uint8_t> rcls(m);
+        for (int i = 0; i < m; ++i) {
+            const int64_t len = hp.ptr[i + 1] - hp.ptr[i];
+            const int key = hp.kind[i] * 8 + lane_class(len, cta);
+            rcls[i] = (uint8_t)key;
+            rcount[key] += 1;
+            rnz[key] += len;
+        }
+        std::vector<int32_t> perm_row(m), roff(17, 0);
+        for (int k = 0; k < 16; ++k) roff[k + 1] = roff[k] + (int32_t)rcount[k];
+        {
+            std::vector<int32_t> pos(roff.begin(), roff.end() - 1);
+            for (int i = 0; i < m; ++i) perm_row[pos[rcls[i]]++] = i;
+        }
+        BinTable rbins;
+        make_bins(rcount, rnz, rbins, 2048);
+
+        // ---- staging upload
+        int32_t *s_ptr, *s_idx, *s_colcount, *s_err;
+        double* s_val;
+        SPS_CK(cudaMalloc(&s_ptr, sizeof(int32_t) * (m + 1)));
+        SPS_CK(cudaMalloc(&s_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(cudaMalloc(&s_val, sizeof(double) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(cudaMalloc(&s_colcount, sizeof(int32_t) * (n + 1)));
+        SPS_CK(cudaMalloc(&s_err, sizeof(int32_t)));
+        SPS_CK(cudaMemcpyAsync(s_ptr, hp.ptr.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
+        {
+            int64_t off = 0;
+            for (const auto& sg : hp.segs) {
+                if (sg.cnt == 0) continue;
+                SPS_CK(cudaMemcpyAsync(s_idx + off, sg.idx, sizeof(int32_t) * sg.cnt, cudaMemcpyHostToDevice, st));
+                SPS_CK(cudaMemcpyAsync(s_val + off, sg.val, sizeof(double) * sg.cnt, cudaMemcpyHostToDevice, st));
+                off += sg.cnt;
+            }
+        }
+        SPS_CK(cudaMemsetAsync(s_colcount, 0, sizeof(int32_t) * (n + 1), st));
+        SPS_CK(cudaMemsetAsync(s_err, 0, sizeof(int32_t), st));
+        if (nnz) k_validate_count<<<grid_for(nnz), kBlock, 0, st>>>(s_idx, s_val, nnz, n, s_colcount, s_err);
+        SPS_CK(cudaGetLastError());
+        std::vector<int32_t> colcount(n);
+        int32_t herr = 0;
+        SPS_CK(cudaMemcpyAsync(colcount.data(), s_colcount, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaMemcpyAsync(&herr, s_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaStreamSynchronize(st));
+        if (herr) {
+            cudaFree(s_ptr); cudaFree(s_idx); cudaFree(s_val); cudaFree(s_colcount); cudaFree(s_err);
+            return fail(SPS_ERR_INVALID, (herr & SE_INDEX) ? "column index out of range [0, n)"
+                                                           : "non-finite constraint matrix value");
+        }
+
+        // ---- column order: stable counting sort by lane class
+        std::vector<int64_t> ccount(16, 0), cnz(16, 0);
+        std::vector<uint8_t> ccls(n);
+        for (int j = 0; j < n; ++j) {
+            const int key = lane_class(colcount[j], cta);
+            ccls[j] = (uint8_t)key;
+            ccount[key] += 1;
+            cnz[key] += colcount[j];
+        }
+        std::vector<int32_t> perm_col(n), inv_col(n), coff(17, 0);
+        for (int k = 0; k < 16; ++k) coff[k + 1] = coff[k] + (int32_t)ccount[k];
+        {
+            std::vector<int32_t> pos(coff.begin(), coff.end() - 1);
+            for (int j = 0; j < n; ++j) { perm_col[pos[ccls[j]]] = j; inv_col[j] = pos[ccls[j]]++; }
+        }
+        BinTable cbins;
+        make_bins(ccount, cnz, cbins, 2048);
+        std::vector<int32_t> nptr(m + 1, 0), cptr(n + 1, 0);
+        for (int r = 0; r < m; ++r) nptr[r + 1] = nptr[r] + (hp.ptr[perm_row[r] + 1] - hp.ptr[perm_row[r]]);
+        for (int j = 0; j < n; ++j) cptr[j + 1] = cptr[j] + colcount[perm_col[j]];
+
+        // ---- persistent arena
+        const int tail = std::min(grid_for(m), kSms * 4);
+        const int apply_blocks = grid_for(std::max(n, m), kBlock, kSms * 8);
+        const size_t part_row_n = (size_t)std::max(rbins.total_blocks, 1) * 8;
+        const size_t part_col_n = (size_t)(cbins.total_blocks + tail) * 10;
+        const size_t part_aux_n = (size_t)std::max(apply_blocks, kSms * 16) * 3;
+        const bool adaptive = mode == SPS_MODE_ADAPTIVE;
+        std::vector<std::pair<void**, size_t>> plan;
+        int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx;
+        V *d_rval, *d_cval, *d_c, *d_b, *d_lo = nullptr, *d_hi = nullptr, *d_tau = nullptr, *d_sigma = nullptr;
+        double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa;
+        V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
+        V *xs, *ys, *xl = nullptr, *yl = nullptr, *AXa = nullptr, *ATYa = nullptr, *xbar = nullptr;
+
+        // uniform bounds: every column [L, U] with L in {0, -inf}, U = +inf
+        bool uniform = true;
+        const double L0 = hp.lb[0], U0 = hp.ub[0];
+        if (!((L0 == 0.0 || std::isinf(L0)) && std::isinf(U0) && U0 > 0)) uniform = false;
+        for (int j = 1; j < n && uniform; ++j)
+            if (!(hp.lb[j] == L0 && hp.ub[j] == U0)) uniform = false;
+
+        auto add = [&](void* p, size_t bytes) { plan.push_back({(void**)p, (bytes + 255) & ~size_t(255)}); };
+        add(&d_rptr, sizeof(int32_t) * (m + 1));
+        add(&d_ridx, sizeof(int32_t) * std::max<int64_t>(nnz, 1));
+        add(&d_rval, sizeof(V) * std::max<int64_t>(nnz, 1));
+        add(&d_cptr, sizeof(int32_t) * (n + 1));
+        add(&d_cidx, sizeof(int32_t) * std::max<int64_t>(nnz, 1));
+        add(&d_cval, sizeof(V) * std::max<int64_t>(nnz, 1));
+        add(&d_perm_row, sizeof(int32_t) * m);
+        add(&d_perm_col, sizeof(int32_t) * n);
+        add(&d_rkind, m);
+        add(&d_c, sizeof(V) * n);
+        add(&d_b, sizeof(V) * m);
+        if (!uniform) { add(&d_lo, sizeof(V) * n); add(&d_hi, sizeof(V) * n); }
+        add(&d_dr, sizeof(double) * m);
+        add(&d_dc, sizeof(double) * n);
+        add(&d_pr, sizeof(double) * part_row_n);
+        add(&d_pc, sizeof(double) * part_col_n);
+        add(&d_pa, sizeof(double) * part_aux_n);
+        add(&X0, sizeof(V) * n); add(&X1, sizeof(V) * n);
+        add(&Y0, sizeof(V) * m); add(&Y1, sizeof(V) * m);
+        add(&xs, sizeof(V) * n); add(&ys, sizeof(V) * m);
+        if (adaptive) {
+            add(&AX0, sizeof(V) * m); add(&AX1, sizeof(V) * m);
+            add(&ATY0, sizeof(V) * n); add(&ATY1, sizeof(V) * n);
+            add(&xl, sizeof(V) * n); add(&yl, sizeof(V) * m);
+            add(&AXa, sizeof(V) * m); add(&ATYa, sizeof(V) * n);
+        } else {
+            add(&xbar, sizeof(V) * n);
+            add(&d_tau, sizeof(V) * n);
+            add(&d_sigma, sizeof(V) * m);
+        }
+        add(&d_ctl, sizeof(Ctl));
+        add(&d_xout, sizeof(double) * n);
+        add(&d_yout, sizeof(double) * m);
+        add(&d_wx, sizeof(double) * n);
+        add(&d_wy, sizeof(double) * m);
+        size_t total = 0;
+        for (auto& p : plan) total += p.second;
+        SPS_CK(cudaMalloc(&arena, total));
+        {
+            size_t off = 0;
+            for (auto& p : plan) { *p.first = arena + off; off += p.second; }
+        }
+
+        // ---- internal CSR and CSC (FP64 values in temporaries)
+        int32_t *t_perm_row, *t_inv_col, *t_fill;
+        double *t_rval, *t_cval, *t_stat;
+        SPS_CK(cudaMalloc(&t_inv_col, sizeof(int32_t) * n));
+        SPS_CK(cudaMalloc(&t_fill, sizeof(int32_t) * n));
+        SPS_CK(cudaMalloc(&t_rval, sizeof(double) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(cudaMalloc(&t_cval, sizeof(double) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(cudaMalloc(&t_stat, sizeof(double) * 2 * (size_t)(n + m)));
+        t_perm_row = d_perm_row;
+        SPS_CK(cudaMemcpyAsync(d_perm_row, perm_row.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
+        SPS_CK(cudaMemcpyAsync(d_perm_col, perm_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+        SPS_CK(cudaMemcpyAsync(t_inv_col, inv_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
+        SPS_CK(cudaMemcpyAsync(d_rptr, nptr.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
+        SPS_CK(cudaMemcpyAsync(d_cptr, cptr.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+        {
+            std::vector<int8_t> kind_int(m);
+            for (int r = 0; r < m; ++r) kind_int[r] = hp.kind[perm_row[r]];
+            SPS_CK(cudaMemcpyAsync(d_rkind, kind_int.data(), m, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaStreamSynchronize(st));
+        }
+        const int warp_grid_m = grid_for((int64_t)m * 32), warp_grid_n = grid_for((int64_t)n * 32);
+        if (nnz) {
+            k_build_csr<<<warp_grid_m, kBlock, 0, st>>>(s_ptr, s_idx, s_val, t_perm_row, t_inv_col, d_rptr, d_ridx,
+                                                        t_rval, m);
+            SPS_CK(cudaMemsetAsync(t_fill, 0, sizeof(int32_t) * n, st));
+            k_scatter_csc<<<warp_grid_m, kBlock, 0, st>>>(d_rptr, d_ridx, t_rval, d_cptr, t_fill, d_cidx, t_cval, m);
+            k_sort_columns<<<grid_for(n), kBlock, 0, st>>>(d_cptr, d_cidx, t_cval, n);
+            SPS_CK(cudaGetLastError());
+        }
+        SPS_CK(cudaStreamSynchronize(st));
+        cudaFree(s_ptr); cudaFree(s_idx); cudaFree(s_val); cudaFree(s_colcount); cudaFree(s_err);
+        // columns too long for the device insertion sort: order on the host
+        for (int j = 0; j < n; ++j) {
+            const int64_t len = cptr[j + 1] - cptr[j];
+            if (len <= kSortMax) continue;
+            std::vector<int32_t> ri(len);
+            std::vector<double> rv(len);
+            SPS_CK(cudaMemcpy(ri.data(), d_cidx + cptr[j], sizeof(int32_t) * len, cudaMemcpyDeviceToHost));
+            SPS_CK(cudaMemcpy(rv.data(), t_cval + cptr[j], sizeof(double) * len, cudaMemcpyDeviceToHost));
+            std::vector<int64_t> ord(len);
+            std::iota(ord.begin(), ord.end(), 0);
+            std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return ri[a] < ri[b]; });
+            std::vector<int32_t> ri2(len);
+            std::vector<double> rv2(len);
+            for (int64_t q = 0; q < len; ++q) { ri2[q] = ri[ord[q]]; rv2[q] = rv[ord[q]]; }
+            SPS_CK(cudaMemcpy(d_cidx + cptr[j], ri2.data(), sizeof(int32_t) * len, cudaMemcpyHostToDevice));
+            SPS_CK(cudaMemcpy(t_cval + cptr[j], rv2.data(), sizeof(double) * len, cudaMemcpyHostToDevice));
+        }
+
+        // ---- scaling (adaptive) or reference diagonal steps
+        double *rmax = t_stat, *rsum = t_stat + m, *cmax = t_stat + 2 * m, *csum = t_stat + 2 * m + n;
+        {
+            std::vector<double> ones(std::max(n, m), 1.0);
+            SPS_CK(cudaMemcpyAsync(d_dr, ones.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(d_dc, ones.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaStreamSynchronize(st));
+        }
+        auto stats = [&]() {
+            k_abs_stats<<<warp_grid_m, kBlock, 0, st>>>(d_rptr, d_ridx, t_rval, d_dr, d_dc, rmax, rsum, m);
+            k_abs_stats<<<warp_grid_n, kBlock, 0, st>>>(d_cptr, d_cidx, t_cval, d_dc, d_dr, cmax, csum, n);
+        };
+        if (adaptive) {
+            const int ruiz = opt.ruiz_iters >= 0 ? opt.ruiz_iters : 10;
+            for (int it = 0; it < ruiz; ++it) {
+                stats();
+                k_rescale<<<grid_for(m), kBlock, 0, st>>>(d_dr, rmax, m);
+                k_rescale<<<grid_for(n), kBlock, 0, st>>>(d_dc, cmax, n);
+            }
+            stats();
+            k_rescale<<<grid_for(m), kBlock, 0, st>>>(d_dr, rsum, m);
+            k_rescale<<<grid_for(n), kBlock, 0, st>>>(d_dc, csum, n);
+        } else {
+            stats();
+            k_diag_steps<V><<<grid_for(std::max(n, m)), kBlock, 0, st>>>(csum, rsum, d_tau, d_sigma, n, m);
+        }
+        k_finish_values<V><<<warp_grid_m, kBlock, 0, st>>>(d_rptr, d_ridx, t_rval, d_dr, d_dc, d_rval, m);
+        k_finish_values<V><<<warp_grid_n, kBlock, 0, st>>>(d_cptr, d_cidx, t_cval, d_dc, d_dr, d_cval, n);
+        SPS_CK(cudaGetLastError());
+
+        // ---- vectors in internal order
+        {
+            std::vector<double> ci(n), li(n), ui(n), bi(m);
+            for (int j = 0; j < n; ++j) { const int o = perm_col[j]; ci[j] = hp.c[o]; li[j] = hp.lb[o]; ui[j] = hp.ub[o]; }
+            for (int r = 0; r < m; ++r) bi[r] = hp.rhs[perm_row[r]];
+            double *t_c, *t_l, *t_u, *t_b;
+            SPS_CK(cudaMalloc(&t_c, sizeof(double) * (3 * (size_t)n + m)));
+            t_l = t_c + n; t_u = t_l + n; t_b = t_u + n;
+            SPS_CK(cudaMemcpyAsync(t_c, ci.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(t_l, li.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(t_u, ui.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(t_b, bi.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+            k_scale_vectors<V><<<grid_for(std::max(n, m)), kBlock, 0, st>>>(t_c, t_l, t_u, t_b, d_dc, d_dr, d_c,
+                                                                           d_lo, d_hi, d_b, n, m);
+            SPS_CK(cudaGetLastError());
+            SPS_CK(cudaStreamSynchronize(st));
+            cudaFree(t_c);
+        }
+        cudaFree(t_inv_col); cudaFree(t_fill); cudaFree(t_rval); cudaFree(t_cval); cudaFree(t_stat);
+
+        // ---- start-up constants: eta0 = 1 / max|K~|, omega0 = ||c~|| / ||b~||
+        {
+            const int g = kSms * 2;
+            double* t_n;
+            SPS_CK(cudaMalloc(&t_n, sizeof(double) * 3 * g));
+            k_norms<V><<<g, kBlock, 0, st>>>(d_rval, nnz, d_c, n, d_b, m, t_n);
+            std::vector<double> hn(3 * g);
+            SPS_CK(cudaMemcpyAsync(hn.data(), t_n, sizeof(double) * 3 * g, cudaMemcpyDeviceToHost, st));
+            SPS_CK(cudaStreamSynchronize(st));
+            cudaFree(t_n);
+            double mx = 0, sc = 0, sb = 0;
+            for (int q = 0; q < g; ++q) { mx = std::max(mx, hn[3 * q]); sc += hn[3 * q + 1]; sb += hn[3 * q + 2]; }
+            eta0 = mx > 0 ? 1.0 / mx : 1.0;
+            omega0 = (sc > 1e-20 && sb > 1e-20) ? std::sqrt(sc) / std::sqrt(sb) : 1.0;
+        }
+
+        // ---- normalisers of the reported error (original data, FP64)
+        double nb2 = 0, nc2 = 0;
+        for (int i = 0; i < m; ++i) nb2 += hp.rhs[i] * hp.rhs[i];
+        for (int j = 0; j < n; ++j) nc2 += hp.c[j] * hp.c[j];
+        Args<V>& a = args;
+        a.n = n; a.m = m;
+        a.csr = Compressed<V>{d_rptr, d_ridx, d_rval};
+        a.csc = Compressed<V>{d_cptr, d_cidx, d_cval};
+        a.rows = rbins; a.cols = cbins;
+        a.col_tail_blocks = tail;
+        a.apply_blocks = apply_blocks;
+        a.c = d_c; a.b = d_b; a.lo = d_lo; a.hi = d_hi;
+        a.uniform_bounds = uniform;
+        a.lo_u = V(L0); a.hi_u = V(U0);
+        a.dr = d_dr; a.dc = d_dc;
+        a.tau = d_tau; a.sigma = d_sigma;
+        if (adaptive) {
+            a.inv_nb = 1.0 / (1.0 + std::sqrt(nb2));
+            a.inv_nc = 1.0 / (1.0 + std::sqrt(nc2));
+        } else {
+            a.inv_nb = 1.0 / std::max(1.0, std::sqrt(nb2));
+            a.inv_nc = 1.0 / std::max(1.0, std::sqrt(nc2));
+        }
+        a.X[0] = X0; a.X[1] = X1; a.Y[0] = Y0; a.Y[1] = Y1;
+        a.AX[0] = AX0; a.AX[1] = AX1; a.ATY[0] = ATY0; a.ATY[1] = ATY1;
+        a.xs = xs; a.ys = ys; a.xl = xl; a.yl = yl; a.AXa = AXa; a.ATYa = ATYa; a.xbar = xbar;
+        a.part_row = d_pr; a.part_col = d_pc; a.part_aux = d_pa;
+        a.ctl = d_ctl;
+        a.abort_flag = d_abort;
+        a.has_cond = 0;
+        a.check_interval = opt.check_interval > 0 ? opt.check_interval : (adaptive ? 64 : 50);
+        SPS_CK(cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st));
+        SPS_CK(cudaEventRecord(ev1, st));
+        SPS_CK(cudaStreamSynchronize(st));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        setup_ms = ms;
+        return SPS_OK;
+    }
+
+    // ---------------------------------------------------------------- solve
+    int nodes_per_window() const { return 2 * args.check_interval + 3; }
+
+    void launch_window(const Args<V>& a) {
+        const int W = a.check_interval;
+        const int gr = a.rows.total_blocks, gc = a.cols.total_blocks;
+        if (mode == SPS_MODE_ADAPTIVE) {
+            for (int w = 0; w < W; ++w) {
+                ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
+                ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+            }
+            ad_row_check<V><<<gr, kBlock, 0, st>>>(a);
+            ad_col_check<V><<<gc, kBlock, 0, st>>>(a);
+            ad_apply<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
+        } else {
+            for (int w = 0; w < W; ++w) {
+                rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
+                rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
+            }
+            rf_row_check<V><<<gr, kBlock, 0, st>>>(a, 0);
+            rf_col_check<V><<<gc, kBlock, 0, st>>>(a, 0);
+            rf_apply<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
+        }
+    }
+
+    int build_window_graph() {
+        cudaGraph_t g;
+        SPS_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        Args<V> a = args;
+        a.has_cond = 0;
+        launch_window(a);
+        SPS_CK(cudaStreamEndCapture(st, &g));
+        cudaError_t e = cudaGraphInstantiate(&win_exec, g, 0);
+        cudaGraphDestroy(g);
+        SPS_CK(e);
+        return SPS_OK;
+    }
+
+    int build_loop_graph() {
+        cudaGraph_t g;
+        SPS_CK(cudaGraphCreate(&g, 0));
+        cudaGraphConditionalHandle h;
+        cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+        if (e != cudaSuccess) { cudaGraphDestroy(g); SPS_CK(e); }
+        cudaGraphNodeParams p{};
+        p.type = cudaGraphNodeTypeConditional;
+        p.conditional.handle = h;
+        p.conditional.type = cudaGraphCondTypeWhile;
+        p.conditional.size = 1;
+        cudaGraphNode_t node;
+        e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &p);
+        if (e != cudaSuccess) { cudaGraphDestroy(g); SPS_CK(e); }
+        cudaGraph_t body = p.conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) { cudaGraphDestroy(g); SPS_CK(e); }
+        Args<V> a = args;
+        a.cond = h;
+        a.has_cond = 1;
+        launch_window(a);
+        e = cudaStreamEndCapture(st, &body);
+        if (e != cudaSuccess) { cudaGraphDestroy(g); SPS_CK(e); }
+        e = cudaGraphInstantiate(&loop_exec, g, 0);
+        cudaGraphDestroy(g);
+        SPS_CK(e);
+        return SPS_OK;
+    }
+
+    // Wait for the stream with bounded polling; raises the abort flag once the
+    // time limit (plus grace) has passed and gives up after a hard limit.
+    int wait_stream(std::chrono::steady_clock::time_point t0) {
+        SPS_CK(cudaEventRecord(evq, st));
+        const double tl = opt.time_limit_s;
+        for (;;) {
+            cudaError_t q = cudaEventQuery(evq);
+            if (q == cudaSuccess) return SPS_OK;
+            if (q != cudaErrorNotReady) SPS_CK(q);
+            const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (tl > 0 && el > tl + 2.0) *(volatile int32_t*)h_abort = 1;
+            if (tl > 0 && el > tl + 120.0) return fail(SPS_ERR_TIMEOUT, "device did not stop after the time limit");
+            std::this_thread::sleep_for(std::chrono::microseconds(el < 0.01 ? 5 : 100));
+        }
+    }
+
+    int run_loop(std::chrono::steady_clock::time_point t0) {
+        const int64_t W = args.check_interval;
+        const int64_t max_windows = opt.max_iters / W + 3;
+        args.max_windows = max_windows;
+        int gm = opt.graph_mode;
+        if (gm == 2) {
+            if (!loop_exec && build_loop_graph() != SPS_OK) { cudaGetLastError(); gm = 1; err.clear(); }
+            if (gm == 2) {
+                SPS_CK(cudaGraphLaunch(loop_exec, st));
+                int rc = wait_stream(t0);
+                if (rc) return rc;
+                SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+                SPS_CK(cudaStreamSynchronize(st));
+                launches += (int64_t)h_ctl->windows * nodes_per_window();
+                return SPS_OK;
+            }
+        }
+        if (gm == 1 && !win_exec && build_window_graph() != SPS_OK) { cudaGetLastError(); gm = 0; err.clear(); }
+        int64_t batch = 1, run = 0;
+        for (;;) {
+            for (int64_t b = 0; b < batch; ++b) {
+                if (gm == 1) SPS_CK(cudaGraphLaunch(win_exec, st));
+                else launch_window(args);
+            }
+            run += batch;
+            launches += batch * nodes_per_window();
+            SPS_CK(cudaGetLastError());
+            SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+            int rc = wait_stream(t0);
+            if (rc) return rc;
+            if (h_ctl->done || h_ctl->iters >= opt.max_iters || run >= max_windows) break;
+            batch = std::min<int64_t>(batch * 2, 16);
+        }
+        return SPS_OK;
+    }
+
+    int solve(sps_result* res) override {
+        SPS_CK(cudaSetDevice(opt.device));
+        std::memset(res, 0, sizeof(*res));
+        if (trivial) return solve_trivial(res);
+        const auto t0 = std::chrono::steady_clock::now();
+        const bool adaptive = mode == SPS_MODE_ADAPTIVE;
+        Ctl c0{};
+        c0.status = SPS_STATUS_ITERATION_LIMIT;
+        c0.init_phase = 1;
+        c0.max_iters = opt.max_iters;
+        c0.tol = opt.tol;
+        c0.eta = eta0;
+        c0.omega = (adaptive && warm_omega > 0) ? warm_omega : omega0;
+        c0.kkt_last = INFINITY;
+        *h_ctl = c0;
+        *(volatile int32_t*)h_abort = 0;
+        launches = 0;
+        const uint64_t tl_ns = opt.time_limit_s > 0 ? (uint64_t)(opt.time_limit_s * 1e9) : 0;
+        SPS_CK(cudaEventRecord(ev0, st));
+        SPS_CK(cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+        const int gr = args.rows.total_blocks, gc = args.cols.total_blocks;
+        if (adaptive) {
+            k_ad_start<V><<<args.apply_blocks, kBlock, 0, st>>>(args, have_warm_x ? d_wx : nullptr,
+                                                               have_warm_y ? d_wy : nullptr, d_perm_col,
+                                                               d_perm_row, d_rkind, tl_ns);
+            spmv_rows<V><<<gr, kBlock, 0, st>>>(args, args.X[0], args.AX[0]);
+            spmv_cols<V><<<gc, kBlock, 0, st>>>(args, args.Y[0], args.ATY[0]);
+            ad_row_check<V><<<gr, kBlock, 0, st>>>(args);
+            ad_col_check<V><<<gc, kBlock, 0, st>>>(args);
+            ad_apply<V><<<args.apply_blocks, kBlock, 0, st>>>(args);
+            launches += 6;
+        } else {
+            k_rf_start<V><<<args.apply_blocks, kBlock, 0, st>>>(args, tl_ns);
+            rf_row_check<V><<<gr, kBlock, 0, st>>>(args, 1);
+            rf_col_check<V><<<gc, kBlock, 0, st>>>(args, 1);
+            launches += 3;
+        }
+        SPS_CK(cudaGetLastError());
+        int rc = run_loop(t0);
+        if (rc) return rc;
+        SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaStreamSynchronize(st));
+        int status = h_ctl->status;
+        if (!h_ctl->done) status = SPS_STATUS_ITERATION_LIMIT;
+        if (!adaptive && status != SPS_STATUS_OPTIMAL) {
+            // report the error of the returned (current) point
+            rf_row_check<V><<<gr, kBlock, 0, st>>>(args, 1);
+            rf_col_check<V><<<gc, kBlock, 0, st>>>(args, 1);
+            launches += 2;
+        }
+        const int cur = adaptive ? h_ctl->cur : 0;
+        k_extract<V><<<args.apply_blocks, kBlock, 0, st>>>(args.X[cur], args.Y[cur], args.dc, args.dr, d_perm_col,
+                                                           d_perm_row, d_xout, d_yout, n, m);
+        launches += 1;
+        SPS_CK(cudaGetLastError());
+        SPS_CK(cudaEventRecord(ev1, st));
+        std::vector<double> xo(n), yo(m);
+        SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaMemcpyAsync(xo.data(), d_xout, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaMemcpyAsync(yo.data(), d_yout, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaStreamSynchronize(st));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ev0, ev1);
+        to_user(xo, yo);
+        res->status = status;
+        res->restarts = h_ctl->restarts;
+        res->iterations = h_ctl->iters;
+        res->accepted_steps = adaptive ? h_ctl->accepted_total : h_ctl->iters;
+        res->rel_kkt = h_ctl->rel_kkt;
+        res->rel_primal = h_ctl->rel_p;
+        res->rel_dual = h_ctl->rel_d;
+        res->rel_gap = h_ctl->rel_gap;
+        res->primal_weight = h_ctl->omega;
+        res->step_size = h_ctl->eta;
+        res->setup_ms = setup_ms;
+        res->solve_ms = ms;
+        res->kernel_launches = launches;
+        res->returned_average = h_ctl->choice;
+        double obj = 0;
+        for (int j = 0; j < n_user; ++j) obj += c_user[j] * x_sol[j];
+        res->objective = obj;
+        solved = true;
+        return SPS_OK;
+    }
+
+    // Problems with no rows or no columns: nothing runs on the device.
+    int solve_trivial(sps_result* res) {
+        x_sol.assign(n_user, 0.0);
+        y_sol.assign(m_user, 0.0);
+        res->status = SPS_STATUS_OPTIMAL;
+        if (mode == SPS_MODE_ADAPTIVE) {
+            for (int j = 0; j < n_user; ++j) {
+                const double c = c_user[j];
+                double v = c > 0 ? lb_user[j] : (c < 0 ? ub_user[j] : std::min(std::max(0.0, lb_user[j]), ub_user[j]));
+                if (!std::isfinite(v)) { res->status = SPS_STATUS_NUMERIC_ERROR; v = std::min(std::max(0.0, lb_user[j]), ub_user[j]); }
+                x_sol[j] = v;
+            }
+        }
+        double obj = 0;
+        for (int j = 0; j < n_user; ++j) obj += c_user[j] * x_sol[j];
+        res->objective = obj;
+        res->setup_ms = setup_ms;
+        solved = true;
+        return SPS_OK;
+    }
+
+    // Device-problem solution -> caller's space.
+    void to_user(const std::vector<double>& xo, const std::vector<double>& yo) {
+        x_sol.assign(n_user, 0.0);
+        y_sol.assign(m_user, 0.0);
+        if (mode == SPS_MODE_ADAPTIVE) {
+            for (int j = 0; j < n_user; ++j) x_sol[j] = xo[j];
+            for (int i = 0; i < m_user; ++i) y_sol[i] = yo[i];
+        } else {
+            const StdMap& s = smap;
+            for (int j = 0; j < n_user; ++j) x_sol[j] = xo[j] + s.lb_shift[j];
+            const int m_le = s.m_ub + s.nub;
+            for (int i = 0; i < s.m_ub; ++i) y_sol[i] = s.neg[i] ? -yo[i] : yo[i];
+            for (int i = 0; i < s.m_eq; ++i) y_sol[s.m_ub + i] = s.neg[m_le + i] ? -yo[m_le + i] : yo[m_le + i];
+        }
+        for (int j = 0; j < n_user; ++j) {
+            const double lo = std::isfinite(lb_user[j]) ? lb_user[j] : -1e30;
+            const double hi = std::isfinite(ub_user[j]) ? ub_user[j] : 1e30;
+            x_sol[j] = std::min(std::max(x_sol[j], lo), hi);
+        }
+    }
+
+    int warm(const double* x0, const double* y0, double omega0_) override {
+        if (mode != SPS_MODE_ADAPTIVE) return fail(SPS_ERR_STATE, "warm start needs the adaptive mode");
+        warm_omega = omega0_;
+        have_warm_x = x0 != nullptr;
+        have_warm_y = y0 != nullptr;
+        if (trivial) return SPS_OK;
+        SPS_CK(cudaSetDevice(opt.device));
+        if (x0) SPS_CK(cudaMemcpyAsync(d_wx, x0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+        if (y0) SPS_CK(cudaMemcpyAsync(d_wy, y0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+        SPS_CK(cudaStreamSynchronize(st));
+        return SPS_OK;
+    }
+
+    int get(double* x, double* y) override {
+        if (!solved) return fail(SPS_ERR_STATE, "no solution: call sps_solve first");
+        if (x) std::memcpy(x, x_sol.data(), sizeof(double) * n_user);
+        if (y) std::memcpy(y, y_sol.data(), sizeof(double) * m_user);
+        return SPS_OK;
+    }
+};
+
+EngineBase* make_engine_f32();
+EngineBase* make_engine_f64();
+int setup_f32(EngineBase* e, const HostProblem& hp, const sps_options& o, int mode);
+int setup_f64(EngineBase* e, const HostProblem& hp, const sps_options& o, int mode);
+
+}  // namespace sps

@@ -1,0 +1,670 @@
+// kernels.cuh — PDHG iteration, check and apply kernels (templated on V).
+//
+// Adaptive mode, one step attempt = two kernels:
+//   ad_row_step  (CSR pass)  K x'  fused with the dual update and projection,
+//                            partials of ||y'-y||^2 and (y'-y)^T K (x'-x);
+//                            its last block takes the step-size decision.
+//   ad_col_step  (CSC pass)  K^T y' (only if the attempt was accepted) fused
+//                            with the weighted-average update and the NEXT
+//                            primal candidate x'' = proj(x - tau (c - K^T y)).
+// Every `check_interval` attempts:
+//   ad_row_check / ad_col_check  FP64 KKT of the average and of the current
+//                            point (both gathers share one matrix read); the
+//                            last block decides termination / restart / weight.
+//   ad_apply                 restart copies, new candidate, loop condition.
+//
+// Reference mode (solver/lp/pdhg.py:209-244), one iteration = two kernels:
+//   rf_col_step  (CSC pass)  A^T y fused with x' = max(0, x - tau (c - A^T y)),
+//                            x_bar = 2x' - x and the x sum.
+//   rf_row_step  (CSR pass)  A x_bar fused with y += sigma (b - A x_bar) and the y sum.
+// Every 50 iterations: rf_row_check / rf_col_check (KKT of the average in
+// FP64, decision in the last block), rf_apply.
+#pragma once
+
+#include "engine.cuh"
+#include "../../include/sps_pdhg.h"
+
+namespace sps {
+
+template <class V>
+struct Args {
+    int32_t n, m;
+    Compressed<V> csr, csc;
+    BinTable rows, cols;
+    int32_t col_tail_blocks;   // extra blocks of ad_col_step that sweep the rows
+    int32_t apply_blocks;
+    const V* c; const V* b; const V* lo; const V* hi;
+    V lo_u, hi_u;
+    int32_t uniform_bounds;
+    const double* dr; const double* dc;
+    const V* tau; const V* sigma;
+    double inv_nb, inv_nc;     // normalisers of the reported relative error
+    V* X[2]; V* Y[2]; V* AX[2]; V* ATY[2];
+    V* xs; V* ys; V* xl; V* yl; V* AXa; V* ATYa; V* xbar;
+    double* part_row; double* part_col; double* part_aux;
+    Ctl* ctl;
+    const volatile int32_t* abort_flag;
+    cudaGraphConditionalHandle cond;
+    int32_t has_cond;
+    int32_t check_interval;
+    int64_t max_windows;
+};
+
+enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4 };
+
+// --- precision helpers -------------------------------------------------------
+__device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double rn_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float rn_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double rn_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float rn_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double rn_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float rn_div(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double rn_div(double a, double b) { return __ddiv_rn(a, b); }
+
+template <class V>
+__device__ __forceinline__ V lo_at(const Args<V>& a, int j) { return a.uniform_bounds ? a.lo_u : a.lo[j]; }
+template <class V>
+__device__ __forceinline__ V hi_at(const Args<V>& a, int j) { return a.uniform_bounds ? a.hi_u : a.hi[j]; }
+template <class V>
+__device__ __forceinline__ V clampv(V x, V lo, V hi) { return fmin(fmax(x, lo), hi); }
+
+// Loop condition of the device-driven while graph: set by one thread only.
+template <class V>
+__device__ __forceinline__ void set_loop_condition(const Args<V>& a, Ctl* ctl) {
+    ctl->windows += 1;
+    const bool keep = !ctl->done && ctl->iters < ctl->max_iters && ctl->windows < a.max_windows;
+    if (a.has_cond) cudaGraphSetConditional(a.cond, keep ? 1u : 0u);
+}
+
+// Shared stop conditions checked at every KKT check: device deadline and host abort.
+__device__ __forceinline__ bool stop_requested(const Ctl* ctl, const volatile int32_t* abort_flag) {
+    if (abort_flag && *abort_flag) return true;
+    return ctl->deadline_ns && global_ns() > ctl->deadline_ns;
+}
+
+// ============================================================================
+// Adaptive mode
+// ============================================================================
+
+template <class V>
+struct GatherOne {
+    const V* x;
+    __device__ __forceinline__ V operator()(int, int j) const { return __ldg(x + j); }
+};
+
+template <class V>
+struct AdRowStepEpi {
+    const V *b, *axo, *yo;
+    V *axn, *yn;
+    V sigma;
+    double dy2 = 0.0, inter = 0.0;
+    __device__ __forceinline__ void operator()(int r, int kind, const V (&acc)[1]) {
+        const V ax = acc[0];
+        const V ao = axo[r];
+        axn[r] = ax;
+        const V yv = yo[r];
+        V y2 = yv + sigma * (b[r] - (ax + ax - ao));
+        if (kind) y2 = fmin(y2, V(0));
+        yn[r] = y2;
+        const double dy = double(y2) - double(yv);
+        dy2 += dy * dy;
+        inter += dy * (double(ax) - double(ao));
+    }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) ad_row_step(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    if (ctl->done || ctl->iters >= ctl->max_iters) return;
+    __shared__ double sm[kWarps * 4];
+    __shared__ V red[kWarps];
+    __shared__ bool last;
+    const int cur = ctl->cur;
+    AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], V(ctl->eta * ctl->omega)};
+    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e, red);
+    double v[2] = {e.dy2, e.inter};
+    if (!publish_partials<2>(v, a.part_row, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
+    double t[2];
+    gather_partials<2>(t, a.part_row, gridDim.x, sm);
+    if (threadIdx.x != 0) return;
+    ctl->ticket[T_ROW_STEP] = 0;
+    const double w = ctl->omega, eta = ctl->eta;
+    const double dy2 = t[0], inter = fabs(t[1]), dx2 = ctl->dx2;
+    const double move = w * dx2 + dy2 / w;
+    const int64_t k = ctl->iters + 1;
+    if (!isfinite(move) || !isfinite(inter)) {
+        ctl->done = 1;
+        ctl->status = SPS_STATUS_NUMERIC_ERROR;
+        ctl->iters = k;
+        return;
+    }
+    const double lim = inter > 0.0 ? move / (2.0 * inter) : INFINITY;
+    const double kk = double(k + 1);
+    const double next = fmin((1.0 - pow(kk, -0.3)) * lim, (1.0 + pow(kk, -0.6)) * eta);
+    const bool acc = (eta <= lim) || move == 0.0;
+    ctl->iters = k;
+    ctl->window += 1;
+    ctl->accepted = acc;
+    if (acc) {
+        ctl->cur = 1 - cur;
+        ctl->eta_used = eta;
+        ctl->w_sum += eta;
+        ctl->accepted_total += 1;
+    }
+    ctl->eta = next;
+    ctl->apply = 8;      // step pending for ad_col_step
+}
+
+template <class V>
+struct AdColStepEpi {
+    const Args<V>* a;
+    const V *xc, *cc;
+    V *aty, *xn, *xs;
+    V tau, wgt;
+    double dx2 = 0.0;
+    __device__ __forceinline__ void column(int j, V atyj, bool accepted) {
+        const V xj = xc[j];
+        if (accepted) { aty[j] = atyj; xs[j] += wgt * xj; }
+        const V x2 = clampv(xj - tau * (cc[j] - atyj), lo_at(*a, j), hi_at(*a, j));
+        xn[j] = x2;
+        const double d = double(x2) - double(xj);
+        dx2 += d * d;
+    }
+    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1]) { column(j, acc[0], true); }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) ad_col_step(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    if (ctl->apply != 8) return;            // no step attempt pending
+    __shared__ double sm[kWarps * 2];
+    __shared__ V red[kWarps];
+    __shared__ bool last;
+    const int cur = ctl->cur;
+    const bool acc = ctl->accepted;
+    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.X[1 - cur], a.xs,
+                      V(ctl->eta / ctl->omega), V(ctl->eta_used)};
+    const int colblocks = a.cols.total_blocks;
+    if ((int)blockIdx.x < colblocks) {
+        if (acc) {
+            visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[cur]}, e, red);
+        } else {
+            for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock)
+                e.column(j, a.ATY[cur][j], false);
+        }
+    } else if (acc) {
+        const V wgt = V(ctl->eta_used);
+        const V* yc = a.Y[cur];
+        for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
+            a.ys[i] += wgt * yc[i];
+    }
+    double v[1] = {e.dx2};
+    if (!publish_partials<1>(v, a.part_col, &ctl->ticket[T_COL_STEP], sm, &last)) return;
+    double t[1];
+    gather_partials<1>(t, a.part_col, gridDim.x, sm);
+    if (threadIdx.x != 0) return;
+    ctl->ticket[T_COL_STEP] = 0;
+    ctl->dx2 = t[0];
+    ctl->apply = 0;
+}
+
+// ---- checks -----------------------------------------------------------------
+// Point 0 = weighted average (x_sum / w_sum), point 1 = current iterate.
+
+template <class V>
+struct GatherTwo {
+    const V *s, *x;
+    double inv_w;
+    __device__ __forceinline__ double operator()(int q, int j) const {
+        return q == 0 ? double(__ldg(s + j)) * inv_w : double(__ldg(x + j));
+    }
+};
+
+template <class V>
+struct AdRowCheckEpi {
+    const Args<V>* a;
+    const V *ys, *yc, *yl;
+    V* axa;
+    double inv_w;
+    double p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // per point q: res_scaled^2, res_orig^2, b^T y, ||y - y_last||^2
+    __device__ __forceinline__ void operator()(int r, int kind, const double (&acc)[2]) {
+        const double br = double(a->b[r]), dr = a->dr[r];
+        axa[r] = V(acc[0]);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            double res = acc[q] - br;
+            if (kind) res = fmax(res, 0.0);
+            p[4 * q + 0] += res * res;
+            const double ro = res / dr;
+            p[4 * q + 1] += ro * ro;
+            const double yv = q == 0 ? double(ys[r]) * inv_w : double(yc[r]);
+            p[4 * q + 2] += br * yv;
+            const double d = yv - double(yl[r]);
+            p[4 * q + 3] += d * d;
+        }
+    }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) ad_row_check(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    if (ctl->done) return;
+    __shared__ double sm[kWarps * 8];
+    __shared__ double red[kWarps * 2];
+    const int cur = ctl->cur;
+    const double inv_w = ctl->w_sum > 0.0 ? 1.0 / ctl->w_sum : 0.0;
+    // with no average yet, point 0 aliases the current iterate
+    const bool has_avg = ctl->w_sum > 0.0;
+    GatherTwo<V> g{has_avg ? a.xs : a.X[cur], a.X[cur], has_avg ? inv_w : 1.0};
+    AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], a.Y[cur], a.yl, a.AXa, has_avg ? inv_w : 1.0};
+    visit_bins<2, double>(a.rows, blockIdx.x, a.csr, g, e, red);
+    block_sum<8>(e.p, sm);
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 8; ++q) a.part_row[(size_t)blockIdx.x * 8 + q] = e.p[q];
+}
+
+template <class V>
+struct AdColCheckEpi {
+    const Args<V>* a;
+    const V *xs, *xc, *xl;
+    V* atya;
+    double inv_w;
+    double p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // per point: dres_s^2, dres_o^2, c^T x, bound terms, ||x - x_last||^2
+    __device__ __forceinline__ void operator()(int j, int, const double (&acc)[2]) {
+        const double cj = double(a->c[j]), dc = a->dc[j];
+        const double lo = double(lo_at(*a, j)), hi = double(hi_at(*a, j));
+        const bool hl = isfinite(lo), hh = isfinite(hi);
+        atya[j] = V(acc[0]);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const double rc = cj - acc[q];
+            const double lam = (hl && hh) ? rc : hl ? fmax(rc, 0.0) : hh ? fmin(rc, 0.0) : 0.0;
+            const double dres = rc - lam;
+            p[5 * q + 0] += dres * dres;
+            const double dor = dres / dc;
+            p[5 * q + 1] += dor * dor;
+            const double xv = q == 0 ? double(xs[j]) * inv_w : double(xc[j]);
+            p[5 * q + 2] += cj * xv;
+            p[5 * q + 3] += (hl ? lo * fmax(lam, 0.0) : 0.0) + (hh ? hi * fmin(lam, 0.0) : 0.0);
+            const double d = xv - double(xl[j]);
+            p[5 * q + 4] += d * d;
+        }
+    }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) ad_col_check(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    if (ctl->done) return;
+    __shared__ double sm[kWarps * 10];
+    __shared__ double red[kWarps * 2];
+    __shared__ bool last;
+    const int cur = ctl->cur;
+    const bool has_avg = ctl->w_sum > 0.0;
+    const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
+    GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], a.Y[cur], inv_w};
+    AdColCheckEpi<V> e{&a, has_avg ? a.xs : a.X[cur], a.X[cur], a.xl, a.ATYa, inv_w};
+    visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e, red);
+    if (!publish_partials<10>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
+    double tc[10], tr[8];
+    gather_partials<10>(tc, a.part_col, gridDim.x, sm);
+    gather_partials<8>(tr, a.part_row, a.rows.total_blocks, sm);
+    if (threadIdx.x != 0) return;
+    ctl->ticket[T_COL_CHECK] = 0;
+
+    const double w = ctl->omega;
+    double rel[2], kw[2], rp[2], rd[2], gp[2], po[2], dob[2];
+    for (int q = 0; q < 2; ++q) {
+        po[q] = tc[5 * q + 2];
+        dob[q] = tr[4 * q + 2] + tc[5 * q + 3];
+        rp[q] = sqrt(tr[4 * q + 1]) * a.inv_nb;
+        rd[q] = sqrt(tc[5 * q + 1]) * a.inv_nc;
+        gp[q] = fabs(po[q] - dob[q]) / (1.0 + fabs(po[q]) + fabs(dob[q]));
+        rel[q] = fmax(rp[q], fmax(rd[q], gp[q]));
+        const double g = po[q] - dob[q];
+        kw[q] = sqrt(w * w * tr[4 * q + 0] + tc[5 * q + 0] / (w * w) + g * g);
+        if (!isfinite(rel[q])) rel[q] = INFINITY;
+        if (!isfinite(kw[q])) kw[q] = INFINITY;
+    }
+    ctl->last_avg_kkt = rel[0];
+    ctl->last_cur_kkt = rel[1];
+    int apply = 0;
+    if (ctl->init_phase) {
+        ctl->init_phase = 0;
+        ctl->kkt_last = kw[1];
+        ctl->kkt_prev_cand = kw[1];
+        const int q = 1;
+        ctl->rel_kkt = rel[q]; ctl->rel_p = rp[q]; ctl->rel_d = rd[q]; ctl->rel_gap = gp[q];
+        ctl->pobj = po[q]; ctl->dobj = dob[q];
+        ctl->apply = AP_CANDIDATE;
+        return;
+    }
+    const int best = (has_avg && rel[0] < rel[1]) ? 0 : 1;
+    const bool bad = !isfinite(rel[1]) && !(has_avg && isfinite(rel[0]));
+    bool finish = false;
+    if (bad) {
+        ctl->status = SPS_STATUS_NUMERIC_ERROR; finish = true;
+    } else if (rel[best] < ctl->tol) {
+        ctl->status = SPS_STATUS_OPTIMAL; finish = true;
+    } else if (ctl->iters >= ctl->max_iters) {
+        ctl->status = SPS_STATUS_ITERATION_LIMIT; finish = true;
+    } else if (stop_requested(ctl, a.abort_flag)) {
+        ctl->status = SPS_STATUS_TIME_LIMIT; finish = true;
+    }
+    if (finish) {
+        ctl->done = 1;
+        ctl->choice = best == 0 ? 1 : 0;
+        ctl->rel_kkt = rel[best]; ctl->rel_p = rp[best]; ctl->rel_d = rd[best]; ctl->rel_gap = gp[best];
+        ctl->pobj = po[best]; ctl->dobj = dob[best];
+        ctl->apply = best == 0 ? AP_LOAD_AVG : 0;
+        return;
+    }
+    // restart decision on the weighted KKT (scaled space)
+    const int cand = (has_avg && kw[0] < kw[1]) ? 0 : 1;
+    const double kc = kw[cand];
+    const bool restart = kc <= 0.2 * ctl->kkt_last ||
+                         (kc <= 0.8 * ctl->kkt_last && kc > ctl->kkt_prev_cand) ||
+                         double(ctl->window) >= 0.36 * double(ctl->iters);
+    ctl->kkt_prev_cand = kc;
+    if (restart) {
+        const double dx = sqrt(tc[5 * cand + 4]), dy = sqrt(tr[4 * cand + 3]);
+        if (dx > 1e-10 && dy > 1e-10) {
+            const double nw = exp(0.5 * log(dy / dx) + 0.5 * log(w));
+            if (isfinite(nw) && nw > 0.0) ctl->omega = nw;
+        }
+        ctl->kkt_last = kc;
+        ctl->kkt_prev_cand = kc;
+        ctl->restarts += 1;
+        ctl->window = 0;
+        ctl->last_restart_iter = ctl->iters;
+        apply = AP_RESTART | AP_CANDIDATE | (cand == 0 ? AP_LOAD_AVG : 0);
+    }
+    ctl->apply = apply;
+}
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    const int ap = ctl->apply;
+    __shared__ double sm[kWarps];
+    __shared__ bool last;
+    if (ap != 0 && ap != 8) {
+        const int cur = ctl->cur;
+        const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !ctl->done;
+        const double inv_w = ctl->w_sum > 0.0 ? 1.0 / ctl->w_sum : 0.0;
+        const V tau = V(ctl->eta / ctl->omega);
+        double dx2 = 0.0;
+        const int stride = gridDim.x * kBlock;
+        for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += stride) {
+            V xv;
+            if (load) {
+                xv = V(double(a.xs[j]) * inv_w);
+                a.X[cur][j] = xv;
+                a.ATY[cur][j] = a.ATYa[j];
+            } else {
+                xv = a.X[cur][j];
+            }
+            if (rst) { a.xl[j] = xv; a.xs[j] = V(0); }
+            if (cand) {
+                const V x2 = clampv(xv - tau * (a.c[j] - a.ATY[cur][j]), lo_at(a, j), hi_at(a, j));
+                a.X[1 - cur][j] = x2;
+                const double d = double(x2) - double(xv);
+                dx2 += d * d;
+            }
+        }
+        for (int i = blockIdx.x * kBlock + threadIdx.x; i < a.m; i += stride) {
+            V yv;
+            if (load) {
+                yv = V(double(a.ys[i]) * inv_w);
+                a.Y[cur][i] = yv;
+                a.AX[cur][i] = a.AXa[i];
+            } else {
+                yv = a.Y[cur][i];
+            }
+            if (rst) { a.yl[i] = yv; a.ys[i] = V(0); }
+        }
+        double v[1] = {dx2};
+        if (publish_partials<1>(v, a.part_aux, &ctl->ticket[T_APPLY], sm, &last)) {
+            double t[1];
+            gather_partials<1>(t, a.part_aux, gridDim.x, sm);
+            if (threadIdx.x == 0) {
+                ctl->ticket[T_APPLY] = 0;
+                if (cand) ctl->dx2 = t[0];
+                if (rst) ctl->w_sum = 0.0;
+                ctl->apply = 0;
+                set_loop_condition(a, ctl);
+            }
+        }
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_loop_condition(a, ctl);
+}
+
+// Plain SpMV passes used at start-up: out = K x (rows) or out = K^T y (columns).
+template <class V>
+struct StoreEpi {
+    V* out;
+    __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1]) { out[r] = acc[0]; }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) spmv_rows(Args<V> a, const V* x, V* out) {
+    __shared__ V red[kWarps];
+    StoreEpi<V> e{out};
+    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{x}, e, red);
+}
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) spmv_cols(Args<V> a, const V* y, V* out) {
+    __shared__ V red[kWarps];
+    StoreEpi<V> e{out};
+    visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{y}, e, red);
+}
+
+// ============================================================================
+// Reference mode (standard form: every row '=', x >= 0; tau, sigma vectors)
+// Elementwise arithmetic is rounded op by op (no FMA contraction) in the
+// reference's own order of operations.
+// ============================================================================
+
+template <class V>
+struct RfColStepEpi {
+    const V *tau, *c;
+    V *x, *xbar, *xs;
+    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1]) {
+        const V xv = x[j];
+        V x2 = rn_sub(xv, rn_mul(tau[j], rn_sub(c[j], acc[0])));
+        x2 = fmax(x2, V(0));
+        xbar[j] = rn_sub(rn_mul(V(2), x2), xv);
+        x[j] = x2;
+        xs[j] = rn_add(xs[j], x2);
+    }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) rf_col_step(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    if (ctl->done || ctl->iters >= ctl->max_iters) return;
+    __shared__ V red[kWarps];
+    RfColStepEpi<V> e{a.tau, a.c, a.X[0], a.xbar, a.xs};
+    visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[0]}, e, red);
+}
+
+template <class V>
+struct RfRowStepEpi {
+    const V *sigma, *b;
+    V *y, *ys;
+    __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1]) {
+        const V y2 = rn_add(y[r], rn_mul(sigma[r], rn_sub(b[r], acc[0])));
+        y[r] = y2;
+        ys[r] = rn_add(ys[r], y2);
+    }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) rf_row_step(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    if (ctl->done || ctl->iters >= ctl->max_iters) return;
+    __shared__ V red[kWarps];
+    __shared__ bool last;
+    RfRowStepEpi<V> e{a.sigma, a.b, a.Y[0], a.ys};
+    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.xbar}, e, red);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(&ctl->ticket[T_ROW_STEP], 1u) == gridDim.x - 1;
+        if (last) {
+            ctl->ticket[T_ROW_STEP] = 0;
+            ctl->iters += 1;
+            ctl->window += 1;
+        }
+    }
+}
+
+// Gather of the point being checked: the average x_sum / window (reference
+// division), or the current iterate.
+template <class V>
+struct RfGather {
+    const V* v;
+    V win;
+    bool avg;
+    __device__ __forceinline__ double operator()(int, int j) const {
+        return avg ? double(rn_div(__ldg(v + j), win)) : double(__ldg(v + j));
+    }
+};
+
+template <class V>
+struct RfRowCheckEpi {
+    const V *b, *yv;
+    V win;
+    bool avg;
+    double p[2] = {0, 0};     // ||A x - b||^2, b^T y
+    __device__ __forceinline__ void operator()(int r, int, const double (&acc)[1]) {
+        const double res = acc[0] - double(b[r]);
+        p[0] += res * res;
+        const double y = avg ? double(rn_div(yv[r], win)) : double(yv[r]);
+        p[1] += double(b[r]) * y;
+    }
+};
+
+// mode: 0 = scheduled check of the average (only when window % interval == 0),
+//       1 = evaluate the current iterate (start-up error / final report).
+template <class V>
+__global__ void __launch_bounds__(kBlock) rf_row_check(Args<V> a, int mode) {
+    Ctl* ctl = a.ctl;
+    if (mode == 0 && (ctl->done || ctl->window == 0 || ctl->window % a.check_interval != 0)) return;
+    __shared__ double sm[kWarps * 2];
+    __shared__ double red[kWarps];
+    const bool avg = mode == 0;
+    const V win = V(ctl->window);
+    RfGather<V> g{avg ? a.xs : a.X[0], win, avg};
+    RfRowCheckEpi<V> e{a.b, avg ? a.ys : a.Y[0], win, avg};
+    visit_bins<1, double>(a.rows, blockIdx.x, a.csr, g, e, red);
+    block_sum<2>(e.p, sm);
+    if (threadIdx.x == 0) {
+        a.part_row[(size_t)blockIdx.x * 2 + 0] = e.p[0];
+        a.part_row[(size_t)blockIdx.x * 2 + 1] = e.p[1];
+    }
+}
+
+template <class V>
+struct RfColCheckEpi {
+    const V *c, *xv;
+    V win;
+    bool avg;
+    double p[2] = {0, 0};     // ||min(c - A^T y, 0)||^2, c^T x
+    __device__ __forceinline__ void operator()(int j, int, const double (&acc)[1]) {
+        const double rc = double(c[j]) - acc[0];
+        const double neg = fmin(rc, 0.0);
+        p[0] += neg * neg;
+        const double x = avg ? double(rn_div(xv[j], win)) : double(xv[j]);
+        p[1] += double(c[j]) * x;
+    }
+};
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) rf_col_check(Args<V> a, int mode) {
+    Ctl* ctl = a.ctl;
+    if (mode == 0 && (ctl->done || ctl->window == 0 || ctl->window % a.check_interval != 0)) return;
+    __shared__ double sm[kWarps * 2];
+    __shared__ double red[kWarps];
+    __shared__ bool last;
+    const bool avg = mode == 0;
+    const V win = V(ctl->window);
+    RfGather<V> g{avg ? a.ys : a.Y[0], win, avg};
+    RfColCheckEpi<V> e{a.c, avg ? a.xs : a.X[0], win, avg};
+    visit_bins<1, double>(a.cols, blockIdx.x, a.csc, g, e, red);
+    if (!publish_partials<2>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
+    double tc[2], tr[2];
+    gather_partials<2>(tc, a.part_col, gridDim.x, sm);
+    gather_partials<2>(tr, a.part_row, a.rows.total_blocks, sm);
+    if (threadIdx.x != 0) return;
+    ctl->ticket[T_COL_CHECK] = 0;
+    const double rp = sqrt(tr[0]) * a.inv_nb;
+    const double rd = sqrt(tc[0]) * a.inv_nc;
+    const double po = tc[1], dob = tr[1];
+    const double gap = fabs(po - dob) / (1.0 + fabs(po) + fabs(dob));
+    double err = fmax(rp, fmax(rd, gap));
+    if (isnan(err)) err = INFINITY;
+    ctl->rel_p = rp; ctl->rel_d = rd; ctl->rel_gap = gap; ctl->pobj = po; ctl->dobj = dob;
+    ctl->rel_kkt = err;
+    if (mode == 1) {
+        if (ctl->init_phase) { ctl->kkt_last = err; ctl->init_phase = 0; }
+        return;
+    }
+    ctl->last_avg_kkt = err;
+    int apply = 0;
+    if (err < ctl->tol) {
+        ctl->done = 1;
+        ctl->status = SPS_STATUS_OPTIMAL;
+        ctl->choice = 1;
+        apply = AP_LOAD_AVG;
+    } else if (err < 0.5 * ctl->kkt_last) {
+        ctl->kkt_last = err;
+        ctl->restarts += 1;
+        apply = AP_LOAD_AVG | AP_RESTART;
+    } else if (!isfinite(err)) {
+        ctl->done = 1;
+        ctl->status = SPS_STATUS_NUMERIC_ERROR;
+    } else if (stop_requested(ctl, a.abort_flag)) {
+        ctl->done = 1;
+        ctl->status = SPS_STATUS_TIME_LIMIT;
+    }
+    ctl->apply = apply;
+}
+
+template <class V>
+__global__ void __launch_bounds__(kBlock) rf_apply(Args<V> a) {
+    Ctl* ctl = a.ctl;
+    const int ap = ctl->apply;
+    __shared__ bool last;
+    if (ap & AP_LOAD_AVG) {
+        const V win = V(ctl->window);
+        const bool rst = ap & AP_RESTART;
+        const int stride = gridDim.x * kBlock;
+        for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += stride) {
+            a.X[0][j] = rn_div(a.xs[j], win);
+            if (rst) a.xs[j] = V(0);
+        }
+        for (int i = blockIdx.x * kBlock + threadIdx.x; i < a.m; i += stride) {
+            a.Y[0][i] = rn_div(a.ys[i], win);
+            if (rst) a.ys[i] = V(0);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            last = atomicAdd(&ctl->ticket[T_APPLY], 1u) == gridDim.x - 1;
+            if (last) {
+                ctl->ticket[T_APPLY] = 0;
+                if (rst) ctl->window = 0;
+                ctl->apply = 0;
+                set_loop_condition(a, ctl);
+            }
+        }
+        return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_loop_condition(a, ctl);
+}
+
+}  // namespace sps

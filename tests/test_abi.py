@@ -1,0 +1,115 @@
+"""C ABI: the library loads, exports every declared entry point, and its
+host-side validation reports malformed input without a GPU."""
+
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+import sovereign_solver_gb300 as sps
+from sovereign_solver_gb300 import _native as N, pdhg
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "sps_pdhg.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(sps_[a-z_]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = N.load()
+    names = declared_functions()
+    assert len(names) >= 10
+    for nm in names:
+        assert hasattr(lib, nm), nm
+
+
+def test_struct_layout_matches_header(tmp_path):
+    """ctypes mirrors agree with a C compiler's view of include/sps_pdhg.h."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    checks = []
+    for cname, py in (("sps_problem_desc", N.ProblemDesc), ("sps_options", N.Options),
+                      ("sps_result", N.Result)):
+        checks.append(f'printf("%s %zu\\n", "{cname}", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            checks.append(f'printf("%s.%s %zu\\n", "{cname}", "{fname}", offsetof({cname}, {fname}));')
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "sps_pdhg.h"\nint main(void){'
+                   + "".join(checks) + "return 0;}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", str(exe)], check=True)
+    got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.splitlines())
+    for cname, py in (("sps_problem_desc", N.ProblemDesc), ("sps_options", N.Options),
+                      ("sps_result", N.Result)):
+        assert int(got[cname]) == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
+
+
+def test_options_defaults():
+    o = pdhg.make_options()
+    assert o.mode == 1 and o.precision == 0 and o.max_iters == 100000 and o.tol == 1e-6
+    assert o.graph_mode == 2 and o.ruiz_iters == 10
+    with pytest.raises(ValueError):
+        pdhg.make_options(mode="simplex")
+    with pytest.raises(ValueError):
+        pdhg.make_options(precision="bf16")
+
+
+def _lp(**kw):
+    p = sps.Problem(c=np.array([1.0, 2.0]), A_ub=sp.csr_matrix(np.array([[-1.0, -1.0]])),
+                    b_ub=np.array([-2.0]), A_eq=sp.csr_matrix((0, 2)), b_eq=np.zeros(0),
+                    lb=np.zeros(2), ub=np.full(2, np.inf), integer_mask=np.zeros(2, bool))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+@pytest.mark.parametrize("bad,msg", [
+    (dict(c=np.array([np.nan, 1.0])), "objective"),
+    (dict(b_ub=np.array([np.inf])), "right-hand side"),
+    (dict(lb=np.array([1.0, 0.0]), ub=np.array([0.0, 1.0])), "bounds"),
+    (dict(lb=np.array([np.inf, 0.0])), "bounds"),
+])
+def test_invalid_input_raises_valueerror_before_device_use(bad, msg):
+    with pytest.raises(ValueError, match=msg):
+        pdhg.solve_lp_pdhg(_lp(**bad))
+
+
+def test_bad_column_index_is_rejected():
+    p = _lp()
+    A = p.A_ub.copy()
+    A.indices = A.indices.copy()
+    A.indices[0] = 7                       # out of range; caught on the device or with no device
+    p.A_ub = A
+    with pytest.raises((ValueError, RuntimeError)):
+        pdhg.solve_lp_pdhg(p)
+
+
+def test_unknown_device_and_method():
+    with pytest.raises(ValueError):
+        sps.solve_lp_pdhg_gpu(_lp(), device="mps")
+    with pytest.raises(ValueError):
+        sps.Solver().set_problem(_lp()).solve(method="simplex")
+    with pytest.raises(RuntimeError):
+        sps.Solver().solve(method="pdhg")
+
+
+def test_get_available_device_values():
+    assert sps.get_available_device() in ("cuda", "cpu")
+
+
+@pytest.mark.skipif(pdhg.get_available_device() == "cuda", reason="checks the no-GPU error path")
+def test_no_gpu_fails_loudly():
+    with pytest.raises(RuntimeError, match="CUDA"):
+        pdhg.solve_lp_pdhg(_lp())
