@@ -1,0 +1,381 @@
+"""Benchmark: restarted PDHG to 1e-4 relative KKT on one GB300.
+
+Default workload: the synthetic transportation LP with 1000 sources x 2000
+sinks (2M variables, 3000 rows, 4M nonzeros), solved from a cold start to a
+relative KKT error of 1e-4 (FP32 iterates and SpMV, FP64 checks).  One step =
+one complete solve.  ``value`` = solves/s with the problem resident in HBM
+(``PDHGEngine.solve`` on the uploaded problem); ``e2e`` = the same through the
+public C-ABI call from pinned host buffers (upload + layout + solve + solution
+read-back inside the timed region).
+
+``--impl reference`` times the reference algorithm (the oracle's C + OpenMP
+restatement of ``solver/lp/pdhg.py``, all host threads) on the same workload.
+
+Multi-GPU: replicas (each rank solves its own seed of the workload; no
+collective), value = total solves / slowest rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sec & iters to 1e-4 rel KKT; solves/s batched; warm vs cold PDHG; SpMV % HBM"
+TOL = 1e-4
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------- workloads
+def make_workload(config: int, seed: int):
+    import sovereign_solver_gb300.workloads as wl
+    if config == 0:
+        p, info = wl.planted_lp(seed=seed)
+        return p, info, {"workload": "planted LP m=200 n=500 5% density u=2 (equality rows)", "seed": seed}
+    if config == 1:
+        p, info = wl.transportation_lp(1000, 2000, seed=seed)
+        return p, info, {"workload": "transportation LP 1000 sources x 2000 sinks (n=2M, m=3000, nnz=4M)",
+                         "seed": seed}
+    if config == 2:
+        p, info = wl.powerlaw_lp(seed=seed)
+        return p, info, {"workload": f"power-law LP m=1M n=2M Zipf(1.5) rows, nnz={p.A_eq.nnz}", "seed": seed}
+    raise SystemExit(f"unknown config {config}")
+
+
+def problem_bytes(p) -> int:
+    """Host bytes one upload moves: CSR arrays of A_ub and A_eq plus c, b, lb, ub."""
+    tot = 0
+    for M in (p.A_ub, p.A_eq):
+        tot += M.indptr.size * 4 + M.indices.size * 4 + M.data.size * 8
+    return tot + 8 * (3 * p.n_vars + p.n_ineq + p.n_eq)
+
+
+def iteration_bytes(p) -> dict:
+    """Algorithmic HBM bytes per launch of the two fused iteration kernels (FP32).
+
+    row pass  (K x' + dual update):   8 nnz + 4(m+1) + 4n + 20m
+    col pass  (K^T y' + primal update + averages):
+              8 nnz + 4(n+1) + 4m + 24n (+8n with per-column bounds) + 12m
+    Vectors gathered through the SpMV are counted once (L2-resident gather).
+    """
+    n, m = p.n_vars, p.n_ineq + p.n_eq
+    nnz = p.A_ub.nnz + p.A_eq.nnz
+    lb, ub = np.asarray(p.lb), np.asarray(p.ub)
+    uniform = (np.all(lb == lb[0]) and np.all(ub == ub[0]) and (lb[0] == 0 or np.isinf(lb[0]))
+               and np.isinf(ub[0]) and ub[0] > 0)
+    row = 8 * nnz + 4 * (m + 1) + 4 * n + 20 * m
+    col = 8 * nnz + 4 * (n + 1) + 4 * m + 24 * n + (0 if uniform else 8 * n) + 12 * m
+    spmv_row = 8 * nnz + 4 * (m + 1) + 4 * n + 4 * m
+    spmv_col = 8 * nnz + 4 * (n + 1) + 4 * m + 4 * n
+    return {"row": row, "col": col, "spmv_row": spmv_row, "spmv_col": spmv_col, "nnz": nnz}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# --------------------------------------------------------------------------- CPU reference timing
+def reference_sample(p, budget_s: float):
+    """Time the reference algorithm (C + OpenMP restatement) on a bounded number
+    of iterations; returns dict with seconds per iteration and the sample."""
+    from oracle import pdhg_ref, pdhg_ref_c
+    t0 = time.perf_counter()
+    std = pdhg_ref.to_standard_form(p)
+    t_std = time.perf_counter() - t0
+    # probe with a few iterations, then size the sample to the budget
+    t0 = time.perf_counter()
+    pdhg_ref_c.solve_std(std, 5, 0.0)
+    probe = (time.perf_counter() - t0) / 5
+    iters = int(max(10, min(100000, budget_s / max(probe, 1e-6))))
+    t0 = time.perf_counter()
+    pdhg_ref_c.solve_std(std, iters, 0.0)
+    dt = time.perf_counter() - t0
+    return {"s_per_iter": dt / iters, "iters": iters, "seconds": dt, "std_form_s": t_std,
+            "threads": pdhg_ref_c.threads()}
+
+
+def load_reference_iterations(config: int):
+    path = os.path.join(ROOT, "tests", "golden", "reference_iterations.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(str(config))
+    except OSError:
+        return None
+
+
+# --------------------------------------------------------------------------- arms
+def run_ours(args, rank, world):
+    import ctypes as C
+    import sovereign_solver_gb300 as sps
+    from sovereign_solver_gb300 import _native as N, pdhg
+
+    p, info, cfg = make_workload(args.config, seed=args.seed + rank)
+    hbm, peak_kind = peaks()
+    eng = sps.PDHGEngine(p, tol=args.tol, max_iters=args.max_iters, device=args.device)
+    for _ in range(args.warmup):
+        r = eng.solve_raw()
+    barrier(world)
+    ms, iters, res = [], [], None
+    t_wall = time.perf_counter()
+    with ClockSampler(args.device) as clk:
+        for _ in range(args.steps):
+            r = eng.solve_raw()
+            ms.append(r.solve_ms)
+            iters.append(r.iterations)
+            res = r
+    wall = time.perf_counter() - t_wall
+    x, y = eng.solution()
+    launches = int(res.kernel_launches) * args.steps
+    kt = np.zeros(3)
+    N.check(eng.lib.sps_time_iteration_kernels(eng.h, 20, N.f64p(kt)), eng.h)
+    eng.close()
+
+    # end to end: public C-ABI call from pinned host buffers
+    d = pdhg._Desc(p)
+    lib = N.load()
+    pinned, seen = [], set()
+    for a in d.arrays():          # one registration per buffer (builders may share arrays)
+        if a.size and a.ctypes.data not in seen and lib.sps_pin_host(a.ctypes.data, a.nbytes) == 0:
+            pinned.append(a)
+            seen.add(a.ctypes.data)
+    opts = pdhg.make_options(tol=args.tol, max_iters=args.max_iters, device=args.device)
+    xo, yo = np.empty(d.n), np.empty(d.m_ub + d.m_eq)
+    for a in (xo, yo):
+        if lib.sps_pin_host(a.ctypes.data, a.nbytes) == 0:
+            pinned.append(a)
+    e2e_s = []
+    e2e_steps = max(1, min(args.steps, args.e2e_steps))
+    for it in range(e2e_steps + 1):
+        t0 = time.perf_counter()
+        h = C.c_void_p()
+        N.check(lib.sps_create(C.byref(d.desc), C.byref(opts), C.byref(h)), None)
+        rr = N.Result()
+        N.check(lib.sps_solve(h, C.byref(rr)), h)
+        N.check(lib.sps_get_solution(h, N.f64p(xo), N.f64p(yo)), h)
+        lib.sps_destroy(h)
+        if it > 0:                      # first call pays one-time lazy CUDA init
+            e2e_s.append(time.perf_counter() - t0)
+    for a in pinned:
+        lib.sps_unpin_host(a.ctypes.data)
+
+    per_rank = {"ms": sum(ms), "e2e_s": sum(e2e_s), "e2e_steps": len(e2e_s)}
+    gathered = gather(world, per_rank)
+    if rank != 0:
+        return None
+    t_max = max(g["ms"] for g in gathered) / 1e3
+    value = world * args.steps / t_max
+    e2e_t = max(g["e2e_s"] / g["e2e_steps"] for g in gathered)
+    ib = iteration_bytes(p)
+    dom = "col" if kt[1] >= kt[0] else "row"
+    dom_ms = kt[1] if dom == "col" else kt[0]
+    achieved = ib[dom] / (dom_ms / 1e3) / 1e9
+    obj_err = None
+    if "obj_star" in info:
+        obj_err = abs(float(res.objective) - info["obj_star"]) / (1 + abs(info["obj_star"]))
+    status = N.STATUS.get(res.status, str(res.status))
+    line = {
+        "metric": METRIC,
+        "value": value, "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic",
+        "config": {**cfg, "tol_rel_kkt": args.tol, "mode": "adaptive", "precision": "fp32 iterates, fp64 checks",
+                   "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)"},
+        "iters_to_tol": int(np.median(iters)),
+        "sec_to_tol": t_max / args.steps,
+        "status": status, "rel_kkt": float(res.rel_kkt), "obj_error_vs_planted": obj_err,
+        "restarts": int(res.restarts), "setup_ms": float(res.setup_ms),
+        "host_wall_s_timed": wall,
+        "gpu_launches": launches,
+        "e2e": {"value": world / e2e_t, "unit": "solves/s", "sec_per_solve": e2e_t,
+                "h2d_bytes_per_step": problem_bytes(p), "d2h_bytes_per_step": 8 * (len(x) + len(y))},
+        "kernel_ms": {"row_pass": kt[0], "col_pass": kt[1], "accept_rate": kt[2]},
+        "roofline": {"bound": "hbm", "kernel": f"ad_{dom}_step (fused {'CSC' if dom == 'col' else 'CSR'} SpMV + update)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "algorithmic_bytes": ib[dom], "traffic": None,
+                     "other_pass_gbs": (ib["row" if dom == "col" else "col"] /
+                                        ((kt[0] if dom == "col" else kt[1]) / 1e3) / 1e9)},
+        "clocks": clk.summary(),
+    }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(p, args)
+    print(json.dumps(line), flush=True)
+    return line
+
+
+def cpu_baseline(p, args):
+    s = reference_sample(p, args.cpu_budget)
+    ref_iters = load_reference_iterations(args.config)
+    out = {"unit": "solves/s", "cores": s["threads"], "kind": "port",
+           "s_per_iter": s["s_per_iter"],
+           "sample": (f"{s['iters']} iterations of the reference algorithm (C+OpenMP restatement of "
+                      f"solver/lp/pdhg.py) on the standard form of the same LP, {s['seconds']:.1f} s; "
+                      f"standard-form build {s['std_form_s']:.1f} s not included")}
+    if ref_iters:
+        n_it = ref_iters["iterations"]
+        out["value"] = 1.0 / (s["s_per_iter"] * n_it)
+        out["extrapolated_to_iters"] = n_it
+        out["reference_status_at_that_count"] = ref_iters["status"]
+    else:
+        out["value"] = None
+    return out
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    p, info, cfg = make_workload(args.config, seed=args.seed)
+    for _ in range(args.warmup):
+        reference_sample(p, min(2.0, args.cpu_budget))
+    vals, spi = [], []
+    for _ in range(args.steps):
+        s = reference_sample(p, args.cpu_budget)
+        spi.append(s["s_per_iter"])
+    ref_iters = load_reference_iterations(args.config)
+    n_it = ref_iters["iterations"] if ref_iters else None
+    s_per_iter = statistics.median(spi)
+    value = 1.0 / (s_per_iter * n_it) if n_it else None
+    line = {
+        "metric": METRIC, "impl": "reference", "value": value, "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": s_per_iter * n_it * 1e3 if n_it else None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
+        "data": "synthetic", "config": {**cfg, "tol_rel_kkt": args.tol},
+        "cpu_baseline": {"value": value, "unit": "solves/s", "cores": s["threads"], "kind": "port",
+                         "sample": (f"per step {s['iters']} iterations of the reference algorithm (C+OpenMP "
+                                    f"restatement of solver/lp/pdhg.py), extrapolated to the "
+                                    f"{n_it} iterations the reference needs on this LP "
+                                    f"({ref_iters['status'] if ref_iters else 'unknown'})")},
+        "s_per_iter": s_per_iter,
+        "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return line
+
+
+# --------------------------------------------------------------------------- distributed plumbing
+def init_dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, world
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def gather(world, obj):
+    if world == 1:
+        return [obj]
+    import torch.distributed as dist
+    out = [None] * world
+    dist.all_gather_object(out, obj)
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--tol", type=float, default=TOL)
+    ap.add_argument("--max-iters", type=int, default=100000)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    rank, world = init_dist()
+    args.device = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -79,7 +79,7 @@ typedef struct {
     int32_t graph_mode;       /* 0 = plain launches, 1 = replayed window graph,
                                  2 = one graph with a device-driven while loop (default) */
     int32_t device;           /* CUDA device ordinal */
-    int32_t row_lanes_cta;    /* schedule tuning: rows longer than this use a whole block (default 1024) */
+    int32_t max_blocks;       /* schedule tuning: blocks per matrix-pass launch, 0 = 16 per SM */
     int32_t reserved[6];
 } sps_options;
 
@@ -127,6 +127,15 @@ int sps_solve(sps_handle *h, sps_result *res);
  * x (n) in the original space, clipped to [lb, ub] as solver/lp/pdhg.py:247-253;
  * y (m_ub + m_eq) duals of the A_ub rows then the A_eq rows. */
 int sps_get_solution(sps_handle *h, double *x, double *y);
+
+/* Benchmark support (no reference counterpart): after a sps_solve, launch
+ * `reps` iterations' kernels one by one on the handle's stream and time each
+ * launch with CUDA events.  out[0] = mean ms of the row-pass kernel (CSR SpMV
+ * fused with the dual update), out[1] = mean ms of the column-pass kernel (CSC
+ * SpMV fused with the primal update), out[2] = fraction of step attempts whose
+ * column pass ran the SpMV (accepted steps; 1 in the reference mode).  The
+ * solution returned by sps_get_solution is not affected. */
+int sps_time_iteration_kernels(sps_handle *h, int32_t reps, double *out);
 
 /* Message of the last error on this handle (or of the last failed sps_create when h is NULL). */
 const char *sps_last_error(const sps_handle *h);

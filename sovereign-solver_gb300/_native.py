@@ -39,7 +39,7 @@ class Options(C.Structure):
     _fields_ = [
         ("mode", C.c_int32), ("precision", C.c_int32), ("max_iters", C.c_int64), ("tol", C.c_double),
         ("check_interval", C.c_int32), ("ruiz_iters", C.c_int32), ("time_limit_s", C.c_double),
-        ("graph_mode", C.c_int32), ("device", C.c_int32), ("row_lanes_cta", C.c_int32),
+        ("graph_mode", C.c_int32), ("device", C.c_int32), ("max_blocks", C.c_int32),
         ("reserved", C.c_int32 * 6),
     ]
 
@@ -86,6 +86,7 @@ def load() -> C.CDLL:
         "sps_unpin_host": (C.c_int, [C.c_void_p]),
         "sps_version": (C.c_char_p, []),
         "sps_device_count": (C.c_int, []),
+        "sps_time_iteration_kernels": (C.c_int, [H, C.c_int32, _f64p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

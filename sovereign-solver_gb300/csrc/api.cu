@@ -175,7 +175,7 @@ int sps_options_init(sps_options* o) {
     o->time_limit_s = 0.0;
     o->graph_mode = 2;
     o->device = 0;
-    o->row_lanes_cta = 1024;
+    o->max_blocks = 0;
     return SPS_OK;
 }
 
@@ -233,6 +233,11 @@ int sps_solve(sps_handle* h, sps_result* res) {
     return h->eng->solve(res);
 }
 
+int sps_time_iteration_kernels(sps_handle* h, int32_t reps, double* out) {
+    if (!h || !out) return SPS_ERR_INVALID;
+    return h->eng->time_kernels(reps, out);
+}
+
 int sps_get_solution(sps_handle* h, double* x, double* y) {
     if (!h) return SPS_ERR_INVALID;
     return h->eng->get(x, y);
@@ -250,12 +255,16 @@ void sps_destroy(sps_handle* h) {
 
 int sps_pin_host(void* ptr, uint64_t bytes) {
     if (!ptr || !bytes) return SPS_ERR_INVALID;
-    return cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess ? SPS_OK : SPS_ERR_CUDA;
+    if (cudaHostRegister(ptr, bytes, cudaHostRegisterDefault) == cudaSuccess) return SPS_OK;
+    cudaGetLastError();   // not sticky: clear it so later calls do not report it
+    return SPS_ERR_CUDA;
 }
 
 int sps_unpin_host(void* ptr) {
     if (!ptr) return SPS_ERR_INVALID;
-    return cudaHostUnregister(ptr) == cudaSuccess ? SPS_OK : SPS_ERR_CUDA;
+    if (cudaHostUnregister(ptr) == cudaSuccess) return SPS_OK;
+    cudaGetLastError();
+    return SPS_ERR_CUDA;
 }
 
 const char* sps_version(void) { return "libsps_gb300 0.1 (sm_103a; FP32/FP64 iterates; reference + adaptive PDHG)"; }

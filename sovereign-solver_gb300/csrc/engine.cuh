@@ -1,12 +1,21 @@
 // engine.cuh — device data layout and shared device helpers of the PDHG engine.
 //
-// Layout in HBM (all indices internal):
-//   rows are renumbered so that each row bin (row type x length class) is one
-//   contiguous range; columns are renumbered by column length class.  The
-//   matrix is stored twice, as CSR (row pass: K x) and CSC (column pass: K^T y),
-//   each as int32 offsets, int32 indices and V values (V = float or double).
-//   Vectors are V arrays in internal order; scale factors and every reduction
-//   are FP64.
+// Matrix layout in HBM (both orientations: CSR for K x, CSC for K^T y).
+// Rows (or columns) are renumbered so that every bin — one row kind ('<=' or
+// '=') and one schedule — is a contiguous index range.  Three schedules:
+//
+//   SLICED   rows with <= 32 nonzeros, sorted by length (descending) inside the
+//            bin and stored as SELL-32 slices: the k-th entry of the t-th row of
+//            slice s sits at soff[s] + 32 k + t.  One thread per row; a warp's 32
+//            loads of step k are one 128-byte line; no offset -> index chain.
+//            Short rows are zero-padded to the slice's longest row.
+//   WARP     rows with 33..512 nonzeros, CSR; one warp per row.
+//   SEGMENT  longer rows, CSR, cut into 512-nonzero segments; one warp per
+//            segment; the last warp to finish a row (per-row ticket) adds the
+//            segment partials in segment order and runs the row's epilogue.
+//
+// Index arrays are int32, values V (float or double); every reduction is FP64
+// at block level.  Scale factors are FP64.
 #pragma once
 
 #include <cstdint>
@@ -16,15 +25,22 @@ namespace sps {
 
 constexpr int kBlock = 256;          // threads per block of every pass kernel
 constexpr int kWarps = kBlock / 32;
-constexpr int kMaxBins = 16;
+constexpr int kMaxBins = 8;
+constexpr int kSliceMax = 32;        // rows up to this length are SLICED
+constexpr int kSegment = 512;        // WARP rows up to this length; SEGMENT size above it
+
+enum BinMode { BM_SLICED = 0, BM_WARP = 1, BM_SEGMENT = 2 };
 
 // One contiguous range of internal rows (or columns) with one schedule.
 struct Bin {
-    int32_t begin, end;      // [begin, end)
-    int32_t lanes;           // 1,2,4,8,16,32 lanes per row, or 0 = whole block per row
+    int32_t begin, end;      // internal rows [begin, end)
+    int32_t mode;            // BinMode
     int32_t kind;            // row pass: 1 = '<=' rows, 0 = '=' rows; column pass: 0
-    int32_t block_begin;     // first block of this bin in the launch
+    int32_t block_begin;     // first block of this bin in a launch
     int32_t nblocks;
+    int32_t units;           // slices (SLICED), rows (WARP) or segments (SEGMENT)
+    int32_t aux;             // SLICED: first global slice; SEGMENT: first global segment
+    int32_t aux2;            // SEGMENT: first per-row ticket index
 };
 
 struct BinTable {
@@ -34,10 +50,15 @@ struct BinTable {
 };
 
 template <class V>
-struct Compressed {          // CSR (ptr over rows) or CSC (ptr over columns)
-    const int32_t* ptr;
+struct Layout {
+    const int32_t* ptr;      // CSR offsets of WARP / SEGMENT rows (m + 1 entries)
     const int32_t* idx;
     const V* val;
+    const int32_t* soff;     // slice offsets (slices + 1)
+    const int32_t* seg_row;  // internal row of each segment
+    const int32_t* seg_k;    // segment number inside its row
+    double* seg_part;        // per-segment partial sums (2 doubles of room each)
+    uint32_t* seg_ticket;    // per-row tickets of SEGMENT rows (left at 0 after every pass)
 };
 
 // Control block, one per handle, in device memory.  Written only by single
@@ -47,7 +68,7 @@ struct Ctl {
     int32_t status;          // SPS_STATUS_* once done
     int32_t cur;             // adaptive: index of the accepted state buffers
     int32_t accepted;        // adaptive: last attempt accepted
-    int32_t apply;           // pending action for the apply kernel (bit 0: load average, bit 1: reset window)
+    int32_t apply;           // pending action for the apply kernel (ApplyBits), 8 = step pending
     int32_t restarts;
     int32_t choice;          // returned point: 0 current, 1 average
     int32_t init_phase;      // 1 while the check kernels only record the starting error
@@ -144,120 +165,157 @@ __device__ __forceinline__ uint64_t global_ns() {
     return t;
 }
 
+
 // ---------------------------------------------------------------------------
-// Binned traversal.  The launch's blocks are split among bins; each bin's
-// rows are visited with `lanes` lanes per row (lane-strided, coalesced index
-// and value streams) or with the whole block per row.  For every row the
-// functor gets the NV dot products of the row with NV gathered vectors:
-//   g(q, j) -> value of vector q at column j (as Acc)
-//   e(r, kind, acc[NV]) is called once per row by exactly one thread.
+// Binned traversal.  For every row the epilogue functor provides
+//   e.pre(r)                  loads the row's own operands (issued before the
+//                             row's dot product, so they overlap its gathers)
+//   e(r, kind, acc[NV], pre)  consumes them; called once per row by one thread
+// and the gather functor g(q, j) returns vector q at column j (as Acc).
+// All control flow below is warp-uniform, so full-mask shuffles are safe.
 
-template <int NV, class Acc>
-struct Dots { Acc v[NV]; };
+constexpr int kUnroll = 8;
+constexpr int kPassMinBlocks = 5;    // resident blocks per SM the iteration kernels are built for
 
-template <int G, int NV, class Acc, class V, class Gather, class Epi>
-__device__ __forceinline__ void visit_lanes(const Bin& b, int bib, const Compressed<V>& M,
-                                            const Gather& g, Epi& e) {
-    constexpr int per_warp = 32 / G;
-    const int warp = threadIdx.x >> 5, wl = threadIdx.x & 31, lane = wl & (G - 1);
-    const int stride = b.nblocks * kWarps * per_warp;
-    for (int base = b.begin + (bib * kWarps + warp) * per_warp; base < b.end; base += stride) {
-        const int r = base + wl / G;
-        const bool valid = r < b.end;
-        const int s = valid ? __ldg(M.ptr + r) : 0;
-        const int t = valid ? __ldg(M.ptr + r + 1) : 0;
-        Acc acc[NV];
-#pragma unroll
-        for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
-        int k = s + lane;
-        for (; k + 3 * G < t; k += 4 * G) {
-            int j[4];
-            Acc a[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) { j[u] = __ldg(M.idx + k + u * G); a[u] = Acc(__ldg(M.val + k + u * G)); }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-#pragma unroll
-                for (int q = 0; q < NV; ++q) acc[q] += a[u] * g(q, j[u]);
-        }
-        for (; k < t; k += G) {
-            const int j = __ldg(M.idx + k);
-            const Acc a = Acc(__ldg(M.val + k));
-#pragma unroll
-            for (int q = 0; q < NV; ++q) acc[q] += a * g(q, j);
-        }
-#pragma unroll
-        for (int q = 0; q < NV; ++q) acc[q] = group_sum<G>(acc[q]);
-        if (valid && lane == 0) e(r, b.kind, acc);
-    }
-}
-
+// SLICED: lane t of the warp owns row begin + 32*slice + t.  Two slices per
+// step (the second may be past the bin) so their loads are in flight together.
 template <int NV, class Acc, class V, class Gather, class Epi>
-__device__ __forceinline__ void visit_block(const Bin& b, int bib, const Compressed<V>& M,
-                                            const Gather& g, Epi& e, Acc* red /* kWarps*NV */) {
-    for (int r = b.begin + bib; r < b.end; r += b.nblocks) {
-        const int s = __ldg(M.ptr + r), t = __ldg(M.ptr + r + 1);
-        Acc acc[NV];
+__device__ __forceinline__ void visit_slice_pair(const Bin& b, int s0, int s1, const Layout<V>& L,
+                                                 const Gather& g, Epi& e) {
+    const int lane = threadIdx.x & 31;
+    const bool has1 = s1 < b.units;
+    int off[2], len[2], r[2];
+    typename Epi::Pre pre[2];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
-        int k = s + threadIdx.x;
-        for (; k + 3 * kBlock < t; k += 4 * kBlock) {
-            int j[4];
-            Acc a[4];
+    for (int h = 0; h < 2; ++h) {
+        const int s = h ? (has1 ? s1 : s0) : s0;
+        const int gs = b.aux + s;
+        off[h] = __ldg(L.soff + gs);
+        len[h] = (h && !has1) ? 0 : ((__ldg(L.soff + gs + 1) - off[h]) >> 5);
+        r[h] = b.begin + s * 32 + lane;
+        if (r[h] < b.end && (h == 0 || has1)) pre[h] = e.pre(r[h]);
+    }
+    Acc acc[2][NV];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) { j[u] = __ldg(M.idx + k + u * kBlock); a[u] = Acc(__ldg(M.val + k + u * kBlock)); }
+    for (int h = 0; h < 2; ++h)
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+        for (int q = 0; q < NV; ++q) acc[h][q] = Acc(0);
+    const int lmax = max(len[0], len[1]);
+    for (int k = 0; k < lmax; k += 4) {
+        int j[2][4];
+        Acc a[2][4];
 #pragma unroll
-                for (int q = 0; q < NV; ++q) acc[q] += a[u] * g(q, j[u]);
-        }
-        for (; k < t; k += kBlock) {
-            const int j = __ldg(M.idx + k);
-            const Acc a = Acc(__ldg(M.val + k));
+        for (int h = 0; h < 2; ++h)
 #pragma unroll
-            for (int q = 0; q < NV; ++q) acc[q] += a * g(q, j);
-        }
-#pragma unroll
-        for (int q = 0; q < NV; ++q) acc[q] = group_sum<32>(acc[q]);
-        const int w = threadIdx.x >> 5;
-        if ((threadIdx.x & 31) == 0) {
-#pragma unroll
-            for (int q = 0; q < NV; ++q) red[w * NV + q] = acc[q];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-#pragma unroll
-            for (int q = 0; q < NV; ++q) {
-                Acc s2 = Acc(0);
-                for (int u = 0; u < kWarps; ++u) s2 += red[u * NV + q];
-                acc[q] = s2;
+            for (int u = 0; u < 4; ++u) {
+                const bool ok = k + u < len[h];
+                const int p = off[h] + lane + 32 * (k + u);
+                j[h][u] = ok ? __ldg(L.idx + p) : 0;
+                a[h][u] = ok ? Acc(__ldg(L.val + p)) : Acc(0);
             }
-            e(r, b.kind, acc);
-        }
-        __syncthreads();
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+#pragma unroll
+                for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
     }
+    if (r[0] < b.end) e(r[0], b.kind, acc[0], pre[0]);
+    if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
 }
 
-// Dispatch: find this block's bin and run its schedule.  Returns false if the
-// block has no bin (launch grids can be padded).
+// Dot products of nonzeros [s, t) with the warp (lane-strided, predicated).
+template <int NV, class Acc, class V, class Gather>
+__device__ __forceinline__ void warp_dot(int s, int t, const Layout<V>& L, const Gather& g, Acc (&acc)[NV]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
+    for (int k = s + lane; k < t; k += 32 * kUnroll) {
+        int j[kUnroll];
+        Acc a[kUnroll];
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) {
+            const int kk = k + 32 * u;
+            const bool ok = kk < t;
+            j[u] = ok ? __ldg(L.idx + kk) : 0;
+            a[u] = ok ? Acc(__ldg(L.val + kk)) : Acc(0);
+        }
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) acc[q] += a[u] * g(q, j[u]);
+    }
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = group_sum<32>(acc[q]);
+}
+
 template <int NV, class Acc, class V, class Gather, class Epi>
-__device__ __forceinline__ void visit_bins(const BinTable& bt, int block, const Compressed<V>& M,
-                                           const Gather& g, Epi& e, Acc* red) {
+__device__ __forceinline__ void visit_warp_row(const Bin& b, int unit, const Layout<V>& L, const Gather& g,
+                                               Epi& e) {
+    const int r = b.begin + unit;
+    const bool lead = (threadIdx.x & 31) == 0;
+    typename Epi::Pre pre;
+    if (lead) pre = e.pre(r);
+    Acc acc[NV];
+    warp_dot<NV, Acc>(__ldg(L.ptr + r), __ldg(L.ptr + r + 1), L, g, acc);
+    if (lead) e(r, b.kind, acc, pre);
+}
+
+template <int NV, class Acc, class V, class Gather, class Epi>
+__device__ __forceinline__ void visit_segment(const Bin& b, int unit, const Layout<V>& L, const Gather& g,
+                                              Epi& e) {
+    const int gseg = b.aux + unit;
+    const int r = __ldg(L.seg_row + gseg), kseg = __ldg(L.seg_k + gseg);
+    const int rs = __ldg(L.ptr + r), re = __ldg(L.ptr + r + 1);
+    const int s = rs + kseg * kSegment;
+    const int t = min(re, s + kSegment);
+    Acc acc[NV];
+    warp_dot<NV, Acc>(s, t, L, g, acc);
+    if ((threadIdx.x & 31) != 0) return;
+    Acc* part = reinterpret_cast<Acc*>(L.seg_part);
+#pragma unroll
+    for (int q = 0; q < NV; ++q) part[(size_t)gseg * NV + q] = acc[q];
+    __threadfence();
+    const int nseg = (re - rs + kSegment - 1) / kSegment;
+    uint32_t* tk = L.seg_ticket + b.aux2 + (r - b.begin);
+    if (atomicAdd(tk, 1u) != (uint32_t)(nseg - 1)) return;
+    __threadfence();
+    *tk = 0u;
+    typename Epi::Pre pre = e.pre(r);
+    const int first = gseg - kseg;
+    Acc tot[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) tot[q] = Acc(0);
+    for (int sg = 0; sg < nseg; ++sg)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) tot[q] += __ldcg(part + (size_t)(first + sg) * NV + q);
+    e(r, b.kind, tot, pre);
+}
+
+// Dispatch: find this block's bin; each warp walks the bin's units with a
+// grid stride.
+template <int NV, class Acc, class V, class Gather, class Epi>
+__device__ __forceinline__ void visit_bins(const BinTable& bt, int block, const Layout<V>& L,
+                                           const Gather& g, Epi& e) {
     int bi = -1;
-    for (int i = 0; i < bt.nbins; ++i)
-        if (block >= bt.bin[i].block_begin && block < bt.bin[i].block_begin + bt.bin[i].nblocks) bi = i;
+#pragma unroll
+    for (int i = 0; i < kMaxBins; ++i)
+        if (i < bt.nbins && block >= bt.bin[i].block_begin && block < bt.bin[i].block_begin + bt.bin[i].nblocks)
+            bi = i;
     if (bi < 0) return;
     const Bin& b = bt.bin[bi];
-    const int bib = block - b.block_begin;
-    switch (b.lanes) {
-        case 1:  visit_lanes<1, NV, Acc>(b, bib, M, g, e); break;
-        case 2:  visit_lanes<2, NV, Acc>(b, bib, M, g, e); break;
-        case 4:  visit_lanes<4, NV, Acc>(b, bib, M, g, e); break;
-        case 8:  visit_lanes<8, NV, Acc>(b, bib, M, g, e); break;
-        case 16: visit_lanes<16, NV, Acc>(b, bib, M, g, e); break;
-        case 32: visit_lanes<32, NV, Acc>(b, bib, M, g, e); break;
-        default: visit_block<NV, Acc>(b, bib, M, g, e, red); break;
+    const int stride = b.nblocks * kWarps;
+    const int w0 = (block - b.block_begin) * kWarps + (threadIdx.x >> 5);
+    if (b.mode == BM_SLICED) {
+        for (int u = w0; u < b.units; u += 2 * stride) visit_slice_pair<NV, Acc>(b, u, u + stride, L, g, e);
+    } else if (b.mode == BM_WARP) {
+        for (int u = w0; u < b.units; u += stride) visit_warp_row<NV, Acc>(b, u, L, g, e);
+    } else {
+        for (int u = w0; u < b.units; u += stride) visit_segment<NV, Acc>(b, u, L, g, e);
     }
 }
+
+// Epilogue helper with nothing to prefetch.
+struct NoPre {};
 
 }  // namespace sps

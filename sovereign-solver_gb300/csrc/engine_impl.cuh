@@ -47,6 +47,7 @@ struct EngineBase {
     virtual int solve(sps_result* res) = 0;
     virtual int warm(const double* x0, const double* y0, double omega0) = 0;
     virtual int get(double* x, double* y) = 0;
+    virtual int time_kernels(int reps, double* out) = 0;
     std::string err;
     int fail(int code, const std::string& msg) { err = msg; return code; }
 };
@@ -59,16 +60,6 @@ struct EngineBase {
                         std::string(#call) + ": " + cudaGetErrorString(e_));                \
     } while (0)
 
-inline int lane_class(int64_t len, int cta_threshold) {
-    if (len <= 4) return 0;
-    if (len <= 8) return 1;
-    if (len <= 16) return 2;
-    if (len <= 32) return 3;
-    if (len <= 64) return 4;
-    if (len <= cta_threshold) return 5;
-    return 6;
-}
-constexpr int kClassLanes[7] = {1, 2, 4, 8, 16, 32, 0};
 constexpr int kSms = 152;
 
 template <class V>
@@ -98,6 +89,8 @@ struct Engine : EngineBase {
     double setup_ms = 0.0;
     std::vector<double> x_sol, y_sol;
     bool solved = false;
+    BinTable layout_rows{}, layout_cols{};
+    int64_t padded_nnz_rows = 0, padded_nnz_cols = 0;
 
     ~Engine() override {
         if (win_exec) cudaGraphExecDestroy(win_exec);
@@ -116,28 +109,124 @@ struct Engine : EngineBase {
         return (int)std::max<int64_t>(1, std::min<int64_t>(g, cap));
     }
 
-    // Bins over a permuted index range.  cls[i] = kind*8 + lane class.
-    static void make_bins(const std::vector<int64_t>& count, const std::vector<int64_t>& nz, BinTable& bt,
-                          int target_nnz_per_block) {
-        bt = BinTable{};
-        int begin = 0, blocks = 0;
-        for (int key = 0; key < 16; ++key) {
-            if (count[key] == 0) continue;
-            Bin b{};
-            b.begin = begin;
-            b.end = begin + (int)count[key];
-            b.kind = key >> 3;
-            b.lanes = kClassLanes[key & 7];
-            const int64_t units = b.lanes ? (count[key] + (kBlock / b.lanes) - 1) / (kBlock / b.lanes) : count[key];
-            int64_t nb = (nz[key] + target_nnz_per_block - 1) / target_nnz_per_block;
-            nb = std::max<int64_t>(1, std::min<int64_t>(nb, units));
-            b.block_begin = blocks;
-            b.nblocks = (int)nb;
-            blocks += (int)nb;
-            begin = b.end;
-            bt.bin[bt.nbins++] = b;
+    // Host plan of one orientation's layout (rows of the CSR or columns of the CSC).
+    struct Plan {
+        std::vector<int32_t> perm;      // internal -> original
+        BinTable bt{};
+        std::vector<int32_t> fptr;      // final CSR offsets (R + 1); SLICED rows hold their bin's start
+        std::vector<int32_t> soff;      // slice offsets, one sentinel after each SLICED bin
+        std::vector<int32_t> seg_row, seg_k;
+        int64_t total = 0;              // final index/value array length (with slice padding)
+        int32_t ntickets = 0;
+    };
+
+    static int mode_of(int64_t len) {
+        return len <= kSliceMax ? BM_SLICED : (len <= kSegment ? BM_WARP : BM_SEGMENT);
+    }
+
+    // Order: per kind, SLICED rows by decreasing length, then WARP rows, then
+    // SEGMENT rows (stable counting sort); one bin per (kind, schedule).
+    static void make_plan(const std::vector<int64_t>& lens, const std::vector<int8_t>* kinds, Plan& P,
+                          int block_cap) {
+        const int R = (int)lens.size();
+        constexpr int NB = kSliceMax + 3;
+        auto kind_of = [&](int i) { return kinds ? (int)(*kinds)[i] : 0; };
+        auto bucket = [&](int i) {
+            const int md = mode_of(lens[i]);
+            const int sub = md == BM_SLICED ? (int)(kSliceMax - lens[i]) : (md == BM_WARP ? kSliceMax + 1 : kSliceMax + 2);
+            return kind_of(i) * NB + sub;
+        };
+        std::vector<int64_t> cnt(2 * NB + 1, 0);
+        for (int i = 0; i < R; ++i) cnt[bucket(i) + 1]++;
+        for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] += cnt[b];
+        P.perm.assign(R, 0);
+        {
+            std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+            for (int i = 0; i < R; ++i) P.perm[pos[bucket(i)]++] = i;
         }
-        bt.total_blocks = blocks;
+        P.fptr.assign(R + 1, 0);
+        P.bt = BinTable{};
+        int64_t off = 0;
+        for (int r = 0; r < R;) {
+            const int kd = kind_of(P.perm[r]), md = mode_of(lens[P.perm[r]]);
+            int e = r;
+            while (e < R && kind_of(P.perm[e]) == kd && mode_of(lens[P.perm[e]]) == md) ++e;
+            Bin b{};
+            b.begin = r;
+            b.end = e;
+            b.mode = md;
+            b.kind = kd;
+            if (md == BM_SLICED) {
+                b.aux = (int32_t)P.soff.size();
+                for (int q = r; q < e; ++q) P.fptr[q] = (int32_t)off;
+                for (int s = r; s < e; s += 32) {
+                    P.soff.push_back((int32_t)off);
+                    off += 32 * lens[P.perm[s]];          // the slice's first row is its longest
+                }
+                b.units = (int32_t)P.soff.size() - b.aux;
+                P.soff.push_back((int32_t)off);           // sentinel: end of the bin's last slice
+            } else if (md == BM_WARP) {
+                for (int q = r; q < e; ++q) { P.fptr[q] = (int32_t)off; off += lens[P.perm[q]]; }
+                b.units = e - r;
+            } else {
+                b.aux = (int32_t)P.seg_row.size();
+                b.aux2 = P.ntickets;
+                for (int q = r; q < e; ++q) {
+                    P.fptr[q] = (int32_t)off;
+                    const int64_t ns = (lens[P.perm[q]] + kSegment - 1) / kSegment;
+                    for (int64_t k = 0; k < ns; ++k) { P.seg_row.push_back(q); P.seg_k.push_back((int32_t)k); }
+                    off += lens[P.perm[q]];
+                }
+                b.units = (int32_t)P.seg_row.size() - b.aux;
+                P.ntickets += e - r;
+            }
+            P.bt.bin[P.bt.nbins++] = b;
+            r = e;
+        }
+        P.fptr[R] = (int32_t)std::min<int64_t>(off, INT32_MAX);
+        P.total = off;
+        int64_t want = 0;
+        for (int i = 0; i < P.bt.nbins; ++i) want += (P.bt.bin[i].units + kWarps - 1) / kWarps;
+        const double scale = want > block_cap ? double(block_cap) / double(want) : 1.0;
+        int blocks = 0;
+        for (int i = 0; i < P.bt.nbins; ++i) {
+            Bin& b = P.bt.bin[i];
+            const int64_t need = (b.units + kWarps - 1) / kWarps;
+            b.nblocks = (int)std::max<int64_t>(1, (int64_t)std::ceil(need * scale));
+            b.block_begin = blocks;
+            blocks += b.nblocks;
+        }
+        P.bt.total_blocks = blocks;
+    }
+
+    // Final device layout of one orientation from the internal CSR temporaries.
+    int build_layout(const Plan& P, int R, const int32_t* tptr, const int32_t* tidx, const V* tval,
+                     Layout<V>& L, int32_t* d_fptr, int32_t* d_soff, int32_t* d_segrow, int32_t* d_segk,
+                     int32_t* d_idx, V* d_val) {
+        SPS_CK(cudaMemcpyAsync(d_fptr, P.fptr.data(), sizeof(int32_t) * (R + 1), cudaMemcpyHostToDevice, st));
+        if (!P.soff.empty())
+            SPS_CK(cudaMemcpyAsync(d_soff, P.soff.data(), sizeof(int32_t) * P.soff.size(), cudaMemcpyHostToDevice, st));
+        if (!P.seg_row.empty()) {
+            SPS_CK(cudaMemcpyAsync(d_segrow, P.seg_row.data(), sizeof(int32_t) * P.seg_row.size(), cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(d_segk, P.seg_k.data(), sizeof(int32_t) * P.seg_k.size(), cudaMemcpyHostToDevice, st));
+        }
+        for (int i = 0; i < P.bt.nbins; ++i) {
+            const Bin& b = P.bt.bin[i];
+            if (b.mode == BM_SLICED)
+                k_fill_sliced<V><<<grid_for((int64_t)b.units * 32), kBlock, 0, st>>>(
+                    tptr, tidx, tval, d_soff, b.begin, b.end, b.aux, b.units, d_idx, d_val);
+            else
+                k_fill_rows<V><<<grid_for((int64_t)(b.end - b.begin) * 32), kBlock, 0, st>>>(
+                    tptr, tidx, tval, d_fptr, b.begin, b.end, d_idx, d_val);
+        }
+        SPS_CK(cudaGetLastError());
+        L.ptr = d_fptr;
+        L.idx = d_idx;
+        L.val = d_val;
+        L.soff = d_soff;
+        L.seg_row = d_segrow;
+        L.seg_k = d_segk;
+        return SPS_OK;
     }
 
     int setup(const HostProblem& hp, const sps_options& o, int mode_) {
@@ -147,6 +236,7 @@ struct Engine : EngineBase {
         m = hp.m;
         nnz = hp.ptr[m];
         SPS_CK(cudaSetDevice(opt.device));
+        cudaGetLastError();   // a stale non-sticky error from an unrelated call must not fail this setup
         SPS_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
         SPS_CK(cudaEventCreate(&ev0));
         SPS_CK(cudaEventCreate(&ev1));
@@ -157,28 +247,16 @@ struct Engine : EngineBase {
         SPS_CK(cudaHostGetDevicePointer((void**)&d_abort, h_abort, 0));
         if (m == 0 || n == 0) { trivial = true; return SPS_OK; }
         SPS_CK(cudaEventRecord(ev0, st));
+        const int block_cap = opt.max_blocks > 0 ? opt.max_blocks : kSms * kPassMinBlocks;   // one resident wave
 
-        const int cta = opt.row_lanes_cta > 64 ? opt.row_lanes_cta : 1024;
-        // ---- row order: stable counting sort by (kind, lane class)
-        std::vector<int64_t> rcount(16, 0), rnz(16, 0);
-        std::vector<uint8_t> rcls(m);
-        for (int i = 0; i < m; ++i) {
-            const int64_t len = hp.ptr[i + 1] - hp.ptr[i];
-            const int key = hp.kind[i] * 8 + lane_class(len, cta);
-            rcls[i] = (uint8_t)key;
-            rcount[key] += 1;
-            rnz[key] += len;
-        }
-        std::vector<int32_t> perm_row(m), roff(17, 0);
-        for (int k = 0; k < 16; ++k) roff[k + 1] = roff[k] + (int32_t)rcount[k];
-        {
-            std::vector<int32_t> pos(roff.begin(), roff.end() - 1);
-            for (int i = 0; i < m; ++i) perm_row[pos[rcls[i]]++] = i;
-        }
-        BinTable rbins;
-        make_bins(rcount, rnz, rbins, 2048);
+        // ---- row plan (host): schedule bins by row kind and length
+        std::vector<int64_t> rlen(m);
+        for (int i = 0; i < m; ++i) rlen[i] = hp.ptr[i + 1] - hp.ptr[i];
+        Plan rp;
+        make_plan(rlen, &hp.kind, rp, block_cap);
+        const std::vector<int32_t>& perm_row = rp.perm;
 
-        // ---- staging upload
+        // ---- staging upload and validation
         int32_t *s_ptr, *s_idx, *s_colcount, *s_err;
         double* s_val;
         SPS_CK(cudaMalloc(&s_ptr, sizeof(int32_t) * (m + 1)));
@@ -211,38 +289,36 @@ struct Engine : EngineBase {
                                                            : "non-finite constraint matrix value");
         }
 
-        // ---- column order: stable counting sort by lane class
-        std::vector<int64_t> ccount(16, 0), cnz(16, 0);
-        std::vector<uint8_t> ccls(n);
-        for (int j = 0; j < n; ++j) {
-            const int key = lane_class(colcount[j], cta);
-            ccls[j] = (uint8_t)key;
-            ccount[key] += 1;
-            cnz[key] += colcount[j];
+        // ---- column plan
+        std::vector<int64_t> clen(n);
+        for (int j = 0; j < n; ++j) clen[j] = colcount[j];
+        Plan cp;
+        make_plan(clen, nullptr, cp, block_cap);
+        const std::vector<int32_t>& perm_col = cp.perm;
+        if (rp.total > INT32_MAX || cp.total > INT32_MAX) {
+            cudaFree(s_ptr); cudaFree(s_idx); cudaFree(s_val); cudaFree(s_colcount); cudaFree(s_err);
+            return fail(SPS_ERR_INVALID, "padded matrix layout exceeds 2^31-1 entries");
         }
-        std::vector<int32_t> perm_col(n), inv_col(n), coff(17, 0);
-        for (int k = 0; k < 16; ++k) coff[k + 1] = coff[k] + (int32_t)ccount[k];
-        {
-            std::vector<int32_t> pos(coff.begin(), coff.end() - 1);
-            for (int j = 0; j < n; ++j) { perm_col[pos[ccls[j]]] = j; inv_col[j] = pos[ccls[j]]++; }
-        }
-        BinTable cbins;
-        make_bins(ccount, cnz, cbins, 2048);
+        std::vector<int32_t> inv_col(n);
+        for (int j = 0; j < n; ++j) inv_col[perm_col[j]] = j;
         std::vector<int32_t> nptr(m + 1, 0), cptr(n + 1, 0);
-        for (int r = 0; r < m; ++r) nptr[r + 1] = nptr[r] + (hp.ptr[perm_row[r] + 1] - hp.ptr[perm_row[r]]);
+        for (int r = 0; r < m; ++r) nptr[r + 1] = nptr[r] + (int32_t)rlen[perm_row[r]];
         for (int j = 0; j < n; ++j) cptr[j + 1] = cptr[j] + colcount[perm_col[j]];
 
         // ---- persistent arena
         const int tail = std::min(grid_for(m), kSms * 4);
         const int apply_blocks = grid_for(std::max(n, m), kBlock, kSms * 8);
-        const size_t part_row_n = (size_t)std::max(rbins.total_blocks, 1) * 8;
-        const size_t part_col_n = (size_t)(cbins.total_blocks + tail) * 10;
+        const size_t part_row_n = (size_t)std::max(rp.bt.total_blocks, 1) * 8;
+        const size_t part_col_n = (size_t)(cp.bt.total_blocks + tail) * 10;
         const size_t part_aux_n = (size_t)std::max(apply_blocks, kSms * 16) * 3;
+        const size_t nseg = std::max<size_t>(std::max(rp.seg_row.size(), cp.seg_row.size()), 1);
+        const size_t ntk = (size_t)std::max(std::max(rp.ntickets, cp.ntickets), 1);
         const bool adaptive = mode == SPS_MODE_ADAPTIVE;
         std::vector<std::pair<void**, size_t>> plan;
-        int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx;
+        int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx, *d_rsoff, *d_csoff, *d_rseg, *d_rsegk, *d_cseg, *d_csegk;
         V *d_rval, *d_cval, *d_c, *d_b, *d_lo = nullptr, *d_hi = nullptr, *d_tau = nullptr, *d_sigma = nullptr;
-        double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa;
+        double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa, *d_segpart;
+        uint32_t* d_tickets;
         V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
         V *xs, *ys, *xl = nullptr, *yl = nullptr, *AXa = nullptr, *ATYa = nullptr, *xbar = nullptr;
 
@@ -253,13 +329,21 @@ struct Engine : EngineBase {
         for (int j = 1; j < n && uniform; ++j)
             if (!(hp.lb[j] == L0 && hp.ub[j] == U0)) uniform = false;
 
-        auto add = [&](void* p, size_t bytes) { plan.push_back({(void**)p, (bytes + 255) & ~size_t(255)}); };
+        auto add = [&](void* p, size_t bytes) { plan.push_back({(void**)p, (std::max<size_t>(bytes, 4) + 255) & ~size_t(255)}); };
         add(&d_rptr, sizeof(int32_t) * (m + 1));
-        add(&d_ridx, sizeof(int32_t) * std::max<int64_t>(nnz, 1));
-        add(&d_rval, sizeof(V) * std::max<int64_t>(nnz, 1));
+        add(&d_ridx, sizeof(int32_t) * std::max<int64_t>(rp.total, 1));
+        add(&d_rval, sizeof(V) * std::max<int64_t>(rp.total, 1));
+        add(&d_rsoff, sizeof(int32_t) * (rp.soff.size() + 1));
+        add(&d_rseg, sizeof(int32_t) * (rp.seg_row.size() + 1));
+        add(&d_rsegk, sizeof(int32_t) * (rp.seg_row.size() + 1));
         add(&d_cptr, sizeof(int32_t) * (n + 1));
-        add(&d_cidx, sizeof(int32_t) * std::max<int64_t>(nnz, 1));
-        add(&d_cval, sizeof(V) * std::max<int64_t>(nnz, 1));
+        add(&d_cidx, sizeof(int32_t) * std::max<int64_t>(cp.total, 1));
+        add(&d_cval, sizeof(V) * std::max<int64_t>(cp.total, 1));
+        add(&d_csoff, sizeof(int32_t) * (cp.soff.size() + 1));
+        add(&d_cseg, sizeof(int32_t) * (cp.seg_row.size() + 1));
+        add(&d_csegk, sizeof(int32_t) * (cp.seg_row.size() + 1));
+        add(&d_segpart, sizeof(double) * 2 * nseg);
+        add(&d_tickets, sizeof(uint32_t) * ntk);
         add(&d_perm_row, sizeof(int32_t) * m);
         add(&d_perm_col, sizeof(int32_t) * n);
         add(&d_rkind, m);
@@ -296,21 +380,25 @@ struct Engine : EngineBase {
             size_t off = 0;
             for (auto& p : plan) { *p.first = arena + off; off += p.second; }
         }
+        SPS_CK(cudaMemsetAsync(d_tickets, 0, sizeof(uint32_t) * ntk, st));
 
-        // ---- internal CSR and CSC (FP64 values in temporaries)
-        int32_t *t_perm_row, *t_inv_col, *t_fill;
+        // ---- internal CSR and CSC temporaries (FP64 values)
+        int32_t *t_inv_col, *t_fill, *t_ptr, *t_idx, *t_cptr, *t_cidx;
         double *t_rval, *t_cval, *t_stat;
         SPS_CK(cudaMalloc(&t_inv_col, sizeof(int32_t) * n));
         SPS_CK(cudaMalloc(&t_fill, sizeof(int32_t) * n));
+        SPS_CK(cudaMalloc(&t_ptr, sizeof(int32_t) * (m + 1)));
+        SPS_CK(cudaMalloc(&t_cptr, sizeof(int32_t) * (n + 1)));
+        SPS_CK(cudaMalloc(&t_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(cudaMalloc(&t_cidx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
         SPS_CK(cudaMalloc(&t_rval, sizeof(double) * std::max<int64_t>(nnz, 1)));
         SPS_CK(cudaMalloc(&t_cval, sizeof(double) * std::max<int64_t>(nnz, 1)));
         SPS_CK(cudaMalloc(&t_stat, sizeof(double) * 2 * (size_t)(n + m)));
-        t_perm_row = d_perm_row;
         SPS_CK(cudaMemcpyAsync(d_perm_row, perm_row.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
         SPS_CK(cudaMemcpyAsync(d_perm_col, perm_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
         SPS_CK(cudaMemcpyAsync(t_inv_col, inv_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
-        SPS_CK(cudaMemcpyAsync(d_rptr, nptr.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
-        SPS_CK(cudaMemcpyAsync(d_cptr, cptr.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
+        SPS_CK(cudaMemcpyAsync(t_ptr, nptr.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
+        SPS_CK(cudaMemcpyAsync(t_cptr, cptr.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, st));
         {
             std::vector<int8_t> kind_int(m);
             for (int r = 0; r < m; ++r) kind_int[r] = hp.kind[perm_row[r]];
@@ -319,11 +407,11 @@ struct Engine : EngineBase {
         }
         const int warp_grid_m = grid_for((int64_t)m * 32), warp_grid_n = grid_for((int64_t)n * 32);
         if (nnz) {
-            k_build_csr<<<warp_grid_m, kBlock, 0, st>>>(s_ptr, s_idx, s_val, t_perm_row, t_inv_col, d_rptr, d_ridx,
+            k_build_csr<<<warp_grid_m, kBlock, 0, st>>>(s_ptr, s_idx, s_val, d_perm_row, t_inv_col, t_ptr, t_idx,
                                                         t_rval, m);
             SPS_CK(cudaMemsetAsync(t_fill, 0, sizeof(int32_t) * n, st));
-            k_scatter_csc<<<warp_grid_m, kBlock, 0, st>>>(d_rptr, d_ridx, t_rval, d_cptr, t_fill, d_cidx, t_cval, m);
-            k_sort_columns<<<grid_for(n), kBlock, 0, st>>>(d_cptr, d_cidx, t_cval, n);
+            k_scatter_csc<<<warp_grid_m, kBlock, 0, st>>>(t_ptr, t_idx, t_rval, t_cptr, t_fill, t_cidx, t_cval, m);
+            k_sort_columns<<<grid_for(n), kBlock, 0, st>>>(t_cptr, t_cidx, t_cval, n);
             SPS_CK(cudaGetLastError());
         }
         SPS_CK(cudaStreamSynchronize(st));
@@ -334,7 +422,7 @@ struct Engine : EngineBase {
             if (len <= kSortMax) continue;
             std::vector<int32_t> ri(len);
             std::vector<double> rv(len);
-            SPS_CK(cudaMemcpy(ri.data(), d_cidx + cptr[j], sizeof(int32_t) * len, cudaMemcpyDeviceToHost));
+            SPS_CK(cudaMemcpy(ri.data(), t_cidx + cptr[j], sizeof(int32_t) * len, cudaMemcpyDeviceToHost));
             SPS_CK(cudaMemcpy(rv.data(), t_cval + cptr[j], sizeof(double) * len, cudaMemcpyDeviceToHost));
             std::vector<int64_t> ord(len);
             std::iota(ord.begin(), ord.end(), 0);
@@ -342,11 +430,11 @@ struct Engine : EngineBase {
             std::vector<int32_t> ri2(len);
             std::vector<double> rv2(len);
             for (int64_t q = 0; q < len; ++q) { ri2[q] = ri[ord[q]]; rv2[q] = rv[ord[q]]; }
-            SPS_CK(cudaMemcpy(d_cidx + cptr[j], ri2.data(), sizeof(int32_t) * len, cudaMemcpyHostToDevice));
+            SPS_CK(cudaMemcpy(t_cidx + cptr[j], ri2.data(), sizeof(int32_t) * len, cudaMemcpyHostToDevice));
             SPS_CK(cudaMemcpy(t_cval + cptr[j], rv2.data(), sizeof(double) * len, cudaMemcpyHostToDevice));
         }
 
-        // ---- scaling (adaptive) or reference diagonal steps
+        // ---- scaling (adaptive) or reference diagonal steps, on the FP64 temporaries
         double *rmax = t_stat, *rsum = t_stat + m, *cmax = t_stat + 2 * m, *csum = t_stat + 2 * m + n;
         {
             std::vector<double> ones(std::max(n, m), 1.0);
@@ -355,8 +443,8 @@ struct Engine : EngineBase {
             SPS_CK(cudaStreamSynchronize(st));
         }
         auto stats = [&]() {
-            k_abs_stats<<<warp_grid_m, kBlock, 0, st>>>(d_rptr, d_ridx, t_rval, d_dr, d_dc, rmax, rsum, m);
-            k_abs_stats<<<warp_grid_n, kBlock, 0, st>>>(d_cptr, d_cidx, t_cval, d_dc, d_dr, cmax, csum, n);
+            k_abs_stats<<<warp_grid_m, kBlock, 0, st>>>(t_ptr, t_idx, t_rval, d_dr, d_dc, rmax, rsum, m);
+            k_abs_stats<<<warp_grid_n, kBlock, 0, st>>>(t_cptr, t_cidx, t_cval, d_dc, d_dr, cmax, csum, n);
         };
         if (adaptive) {
             const int ruiz = opt.ruiz_iters >= 0 ? opt.ruiz_iters : 10;
@@ -372,9 +460,22 @@ struct Engine : EngineBase {
             stats();
             k_diag_steps<V><<<grid_for(std::max(n, m)), kBlock, 0, st>>>(csum, rsum, d_tau, d_sigma, n, m);
         }
-        k_finish_values<V><<<warp_grid_m, kBlock, 0, st>>>(d_rptr, d_ridx, t_rval, d_dr, d_dc, d_rval, m);
-        k_finish_values<V><<<warp_grid_n, kBlock, 0, st>>>(d_cptr, d_cidx, t_cval, d_dc, d_dr, d_cval, n);
+        // scaled values in the iterate precision
+        SPS_CK(cudaStreamSynchronize(st));
+        cudaFree(t_stat);
+        V *t_rvV, *t_cvV;
+        SPS_CK(cudaMalloc(&t_rvV, sizeof(V) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(cudaMalloc(&t_cvV, sizeof(V) * std::max<int64_t>(nnz, 1)));
+        k_finish_values<V><<<warp_grid_m, kBlock, 0, st>>>(t_ptr, t_idx, t_rval, d_dr, d_dc, t_rvV, m);
+        k_finish_values<V><<<warp_grid_n, kBlock, 0, st>>>(t_cptr, t_cidx, t_cval, d_dc, d_dr, t_cvV, n);
         SPS_CK(cudaGetLastError());
+
+        // ---- final binned layouts
+        Layout<V> Lr{}, Lc{};
+        if (int rc = build_layout(rp, m, t_ptr, t_idx, t_rvV, Lr, d_rptr, d_rsoff, d_rseg, d_rsegk, d_ridx, d_rval)) return rc;
+        if (int rc = build_layout(cp, n, t_cptr, t_cidx, t_cvV, Lc, d_cptr, d_csoff, d_cseg, d_csegk, d_cidx, d_cval)) return rc;
+        Lr.seg_part = Lc.seg_part = d_segpart;
+        Lr.seg_ticket = Lc.seg_ticket = d_tickets;
 
         // ---- vectors in internal order
         {
@@ -394,14 +495,15 @@ struct Engine : EngineBase {
             SPS_CK(cudaStreamSynchronize(st));
             cudaFree(t_c);
         }
-        cudaFree(t_inv_col); cudaFree(t_fill); cudaFree(t_rval); cudaFree(t_cval); cudaFree(t_stat);
+        cudaFree(t_inv_col); cudaFree(t_fill); cudaFree(t_ptr); cudaFree(t_cptr); cudaFree(t_idx);
+        cudaFree(t_cidx); cudaFree(t_rval); cudaFree(t_cval); cudaFree(t_rvV); cudaFree(t_cvV);
 
         // ---- start-up constants: eta0 = 1 / max|K~|, omega0 = ||c~|| / ||b~||
         {
             const int g = kSms * 2;
             double* t_n;
             SPS_CK(cudaMalloc(&t_n, sizeof(double) * 3 * g));
-            k_norms<V><<<g, kBlock, 0, st>>>(d_rval, nnz, d_c, n, d_b, m, t_n);
+            k_norms<V><<<g, kBlock, 0, st>>>(d_rval, rp.total, d_c, n, d_b, m, t_n);
             std::vector<double> hn(3 * g);
             SPS_CK(cudaMemcpyAsync(hn.data(), t_n, sizeof(double) * 3 * g, cudaMemcpyDeviceToHost, st));
             SPS_CK(cudaStreamSynchronize(st));
@@ -418,9 +520,9 @@ struct Engine : EngineBase {
         for (int j = 0; j < n; ++j) nc2 += hp.c[j] * hp.c[j];
         Args<V>& a = args;
         a.n = n; a.m = m;
-        a.csr = Compressed<V>{d_rptr, d_ridx, d_rval};
-        a.csc = Compressed<V>{d_cptr, d_cidx, d_cval};
-        a.rows = rbins; a.cols = cbins;
+        a.csr = Lr;
+        a.csc = Lc;
+        a.rows = rp.bt; a.cols = cp.bt;
         a.col_tail_blocks = tail;
         a.apply_blocks = apply_blocks;
         a.c = d_c; a.b = d_b; a.lo = d_lo; a.hi = d_hi;
@@ -443,6 +545,10 @@ struct Engine : EngineBase {
         a.abort_flag = d_abort;
         a.has_cond = 0;
         a.check_interval = opt.check_interval > 0 ? opt.check_interval : (adaptive ? 64 : 50);
+        layout_rows = rp.bt;
+        layout_cols = cp.bt;
+        padded_nnz_rows = rp.total;
+        padded_nnz_cols = cp.total;
         SPS_CK(cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st));
         SPS_CK(cudaEventRecord(ev1, st));
         SPS_CK(cudaStreamSynchronize(st));
@@ -708,6 +814,58 @@ struct Engine : EngineBase {
         if (x0) SPS_CK(cudaMemcpyAsync(d_wx, x0, sizeof(double) * n, cudaMemcpyHostToDevice, st));
         if (y0) SPS_CK(cudaMemcpyAsync(d_wy, y0, sizeof(double) * m, cudaMemcpyHostToDevice, st));
         SPS_CK(cudaStreamSynchronize(st));
+        return SPS_OK;
+    }
+
+    // Per-launch timing of the two iteration kernels on the resident state.
+    // The control block is saved, opened for `reps` more iterations, and restored.
+    int time_kernels(int reps, double* out) override {
+        if (!solved) return fail(SPS_ERR_STATE, "call sps_solve before timing kernels");
+        if (reps <= 0) return fail(SPS_ERR_INVALID, "reps must be positive");
+        if (trivial) { out[0] = out[1] = 0.0; out[2] = 1.0; return SPS_OK; }
+        SPS_CK(cudaSetDevice(opt.device));
+        Ctl saved;
+        SPS_CK(cudaMemcpy(&saved, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+        Ctl t = saved;
+        t.done = 0;
+        t.apply = 0;
+        t.max_iters = INT64_MAX / 2;
+        SPS_CK(cudaMemcpy(d_ctl, &t, sizeof(Ctl), cudaMemcpyHostToDevice));
+        std::vector<cudaEvent_t> ev(2 * reps + 1);
+        for (auto& e : ev) SPS_CK(cudaEventCreate(&e));
+        const int gr = args.rows.total_blocks, gc = args.cols.total_blocks;
+        Args<V> a = args;
+        a.has_cond = 0;
+        SPS_CK(cudaEventRecord(ev[0], st));
+        for (int r = 0; r < reps; ++r) {
+            if (mode == SPS_MODE_ADAPTIVE) {
+                ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
+                SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
+                ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+            } else {
+                rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
+                SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
+                rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
+            }
+            SPS_CK(cudaEventRecord(ev[2 * r + 2], st));
+        }
+        SPS_CK(cudaGetLastError());
+        SPS_CK(cudaStreamSynchronize(st));
+        double row = 0, col = 0;
+        for (int r = 0; r < reps; ++r) {
+            float a1 = 0, a2 = 0;
+            cudaEventElapsedTime(&a1, ev[2 * r], ev[2 * r + 1]);
+            cudaEventElapsedTime(&a2, ev[2 * r + 1], ev[2 * r + 2]);
+            row += a1;
+            col += a2;
+        }
+        Ctl after;
+        SPS_CK(cudaMemcpy(&after, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+        for (auto& e : ev) cudaEventDestroy(e);
+        SPS_CK(cudaMemcpy(d_ctl, &saved, sizeof(Ctl), cudaMemcpyHostToDevice));
+        out[0] = row / reps;
+        out[1] = col / reps;
+        out[2] = mode == SPS_MODE_ADAPTIVE ? double(after.accepted_total - saved.accepted_total) / reps : 1.0;
         return SPS_OK;
     }
 

@@ -29,7 +29,7 @@ namespace sps {
 template <class V>
 struct Args {
     int32_t n, m;
-    Compressed<V> csr, csc;
+    Layout<V> csr, csc;
     BinTable rows, cols;
     int32_t col_tail_blocks;   // extra blocks of ad_col_step that sweep the rows
     int32_t apply_blocks;
@@ -50,7 +50,12 @@ struct Args {
     int64_t max_windows;
 };
 
-enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4 };
+enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4, AP_STEP_PENDING = 8 };
+
+// iteration kernels: register budget for kPassMinBlocks resident blocks per SM;
+// check kernels (FP64 accumulators, once per window) get the default budget
+#define SPS_PASS_KERNEL __global__ void __launch_bounds__(kBlock, kPassMinBlocks)
+#define SPS_CHECK_KERNEL __global__ void __launch_bounds__(kBlock)
 
 // --- precision helpers -------------------------------------------------------
 __device__ __forceinline__ float rn_add(float a, float b) { return __fadd_rn(a, b); }
@@ -83,52 +88,53 @@ __device__ __forceinline__ bool stop_requested(const Ctl* ctl, const volatile in
     return ctl->deadline_ns && global_ns() > ctl->deadline_ns;
 }
 
-// ============================================================================
-// Adaptive mode
-// ============================================================================
-
 template <class V>
 struct GatherOne {
     const V* x;
     __device__ __forceinline__ V operator()(int, int j) const { return __ldg(x + j); }
 };
 
+// ============================================================================
+// Adaptive mode
+// ============================================================================
+
 template <class V>
 struct AdRowStepEpi {
     const V *b, *axo, *yo;
     V *axn, *yn;
     V sigma;
-    double dy2 = 0.0, inter = 0.0;
-    __device__ __forceinline__ void operator()(int r, int kind, const V (&acc)[1]) {
+    V dy2 = V(0), inter = V(0);          // per-thread partials; FP64 from the block sum on
+    struct Pre { V ao, yv, br; };
+    __device__ __forceinline__ Pre pre(int r) const { return Pre{axo[r], yo[r], b[r]}; }
+    __device__ __forceinline__ void operator()(int r, int kind, const V (&acc)[1], const Pre& p) {
         const V ax = acc[0];
-        const V ao = axo[r];
         axn[r] = ax;
-        const V yv = yo[r];
-        V y2 = yv + sigma * (b[r] - (ax + ax - ao));
+        V y2 = p.yv + sigma * (p.br - (ax + ax - p.ao));
         if (kind) y2 = fmin(y2, V(0));
         yn[r] = y2;
-        const double dy = double(y2) - double(yv);
+        const V dy = y2 - p.yv;
         dy2 += dy * dy;
-        inter += dy * (double(ax) - double(ao));
+        inter += dy * (ax - p.ao);
     }
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) ad_row_step(Args<V> a) {
+SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
     __shared__ double sm[kWarps * 4];
-    __shared__ V red[kWarps];
     __shared__ bool last;
     const int cur = ctl->cur;
     AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], V(ctl->eta * ctl->omega)};
-    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e, red);
-    double v[2] = {e.dy2, e.inter};
+    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e);
+    double v[2] = {double(e.dy2), double(e.inter)};
     if (!publish_partials<2>(v, a.part_row, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
     double t[2];
     gather_partials<2>(t, a.part_row, gridDim.x, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_ROW_STEP] = 0;
+    // adaptive step (PDLP): limit = ||dz||_w^2 / (2 |dy^T K dx|); accept if eta <= limit;
+    // next eta = min((1 - (k+1)^-0.3) limit, (1 + (k+1)^-0.6) eta)
     const double w = ctl->omega, eta = ctl->eta;
     const double dy2 = t[0], inter = fabs(t[1]), dx2 = ctl->dx2;
     const double move = w * dx2 + dy2 / w;
@@ -140,8 +146,8 @@ __global__ void __launch_bounds__(kBlock) ad_row_step(Args<V> a) {
         return;
     }
     const double lim = inter > 0.0 ? move / (2.0 * inter) : INFINITY;
-    const double kk = double(k + 1);
-    const double next = fmin((1.0 - pow(kk, -0.3)) * lim, (1.0 + pow(kk, -0.6)) * eta);
+    const float kk = float(k + 1);
+    const double next = fmin((1.0 - double(powf(kk, -0.3f))) * lim, (1.0 + double(powf(kk, -0.6f))) * eta);
     const bool acc = (eta <= lim) || move == 0.0;
     ctl->iters = k;
     ctl->window += 1;
@@ -153,45 +159,54 @@ __global__ void __launch_bounds__(kBlock) ad_row_step(Args<V> a) {
         ctl->accepted_total += 1;
     }
     ctl->eta = next;
-    ctl->apply = 8;      // step pending for ad_col_step
+    ctl->apply = AP_STEP_PENDING;
 }
 
 template <class V>
 struct AdColStepEpi {
     const Args<V>* a;
-    const V *xc, *cc;
+    const V *xc, *cc, *atyo;
     V *aty, *xn, *xs;
     V tau, wgt;
-    double dx2 = 0.0;
-    __device__ __forceinline__ void column(int j, V atyj, bool accepted) {
-        const V xj = xc[j];
-        if (accepted) { aty[j] = atyj; xs[j] += wgt * xj; }
-        const V x2 = clampv(xj - tau * (cc[j] - atyj), lo_at(*a, j), hi_at(*a, j));
+    bool accepted;
+    V dx2 = V(0);
+    struct Pre { V xj, cj, lo, hi, s; };
+    __device__ __forceinline__ Pre pre(int j) const {
+        Pre p;
+        p.xj = xc[j];
+        p.cj = cc[j];
+        p.lo = lo_at(*a, j);
+        p.hi = hi_at(*a, j);
+        p.s = accepted ? xs[j] : V(0);
+        return p;
+    }
+    __device__ __forceinline__ void finish(int j, V atyj, const Pre& p) {
+        if (accepted) { aty[j] = atyj; xs[j] = p.s + wgt * p.xj; }
+        const V x2 = clampv(p.xj - tau * (p.cj - atyj), p.lo, p.hi);
         xn[j] = x2;
-        const double d = double(x2) - double(xj);
+        const V d = x2 - p.xj;
         dx2 += d * d;
     }
-    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1]) { column(j, acc[0], true); }
+    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) { finish(j, acc[0], p); }
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) ad_col_step(Args<V> a) {
+SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     Ctl* ctl = a.ctl;
-    if (ctl->apply != 8) return;            // no step attempt pending
+    if (ctl->apply != AP_STEP_PENDING) return;
     __shared__ double sm[kWarps * 2];
-    __shared__ V red[kWarps];
     __shared__ bool last;
     const int cur = ctl->cur;
     const bool acc = ctl->accepted;
-    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.X[1 - cur], a.xs,
-                      V(ctl->eta / ctl->omega), V(ctl->eta_used)};
+    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.ATY[cur], a.X[1 - cur], a.xs,
+                      V(ctl->eta / ctl->omega), V(ctl->eta_used), acc};
     const int colblocks = a.cols.total_blocks;
     if ((int)blockIdx.x < colblocks) {
         if (acc) {
-            visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[cur]}, e, red);
+            visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[cur]}, e);
         } else {
             for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock)
-                e.column(j, a.ATY[cur][j], false);
+                e.finish(j, e.atyo[j], e.pre(j));
         }
     } else if (acc) {
         const V wgt = V(ctl->eta_used);
@@ -199,7 +214,7 @@ __global__ void __launch_bounds__(kBlock) ad_col_step(Args<V> a) {
         for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
             a.ys[i] += wgt * yc[i];
     }
-    double v[1] = {e.dx2};
+    double v[1] = {double(e.dx2)};
     if (!publish_partials<1>(v, a.part_col, &ctl->ticket[T_COL_STEP], sm, &last)) return;
     double t[1];
     gather_partials<1>(t, a.part_col, gridDim.x, sm);
@@ -228,7 +243,9 @@ struct AdRowCheckEpi {
     V* axa;
     double inv_w;
     double p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // per point q: res_scaled^2, res_orig^2, b^T y, ||y - y_last||^2
-    __device__ __forceinline__ void operator()(int r, int kind, const double (&acc)[2]) {
+    using Pre = NoPre;
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int r, int kind, const double (&acc)[2], const Pre&) {
         const double br = double(a->b[r]), dr = a->dr[r];
         axa[r] = V(acc[0]);
 #pragma unroll
@@ -247,18 +264,17 @@ struct AdRowCheckEpi {
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) ad_row_check(Args<V> a) {
+SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done) return;
     __shared__ double sm[kWarps * 8];
-    __shared__ double red[kWarps * 2];
     const int cur = ctl->cur;
-    const double inv_w = ctl->w_sum > 0.0 ? 1.0 / ctl->w_sum : 0.0;
     // with no average yet, point 0 aliases the current iterate
     const bool has_avg = ctl->w_sum > 0.0;
-    GatherTwo<V> g{has_avg ? a.xs : a.X[cur], a.X[cur], has_avg ? inv_w : 1.0};
-    AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], a.Y[cur], a.yl, a.AXa, has_avg ? inv_w : 1.0};
-    visit_bins<2, double>(a.rows, blockIdx.x, a.csr, g, e, red);
+    const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
+    GatherTwo<V> g{has_avg ? a.xs : a.X[cur], a.X[cur], inv_w};
+    AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], a.Y[cur], a.yl, a.AXa, inv_w};
+    visit_bins<2, double>(a.rows, blockIdx.x, a.csr, g, e);
     block_sum<8>(e.p, sm);
     if (threadIdx.x == 0)
         for (int q = 0; q < 8; ++q) a.part_row[(size_t)blockIdx.x * 8 + q] = e.p[q];
@@ -271,7 +287,9 @@ struct AdColCheckEpi {
     V* atya;
     double inv_w;
     double p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // per point: dres_s^2, dres_o^2, c^T x, bound terms, ||x - x_last||^2
-    __device__ __forceinline__ void operator()(int j, int, const double (&acc)[2]) {
+    using Pre = NoPre;
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int j, int, const double (&acc)[2], const Pre&) {
         const double cj = double(a->c[j]), dc = a->dc[j];
         const double lo = double(lo_at(*a, j)), hi = double(hi_at(*a, j));
         const bool hl = isfinite(lo), hh = isfinite(hi);
@@ -294,18 +312,17 @@ struct AdColCheckEpi {
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) ad_col_check(Args<V> a) {
+SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done) return;
     __shared__ double sm[kWarps * 10];
-    __shared__ double red[kWarps * 2];
     __shared__ bool last;
     const int cur = ctl->cur;
     const bool has_avg = ctl->w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
     GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], a.Y[cur], inv_w};
     AdColCheckEpi<V> e{&a, has_avg ? a.xs : a.X[cur], a.X[cur], a.xl, a.ATYa, inv_w};
-    visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e, red);
+    visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e);
     if (!publish_partials<10>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
     double tc[10], tr[8];
     gather_partials<10>(tc, a.part_col, gridDim.x, sm);
@@ -389,12 +406,12 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
     const int ap = ctl->apply;
     __shared__ double sm[kWarps];
     __shared__ bool last;
-    if (ap != 0 && ap != 8) {
+    if (ap != 0 && ap != AP_STEP_PENDING) {
         const int cur = ctl->cur;
         const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !ctl->done;
         const double inv_w = ctl->w_sum > 0.0 ? 1.0 / ctl->w_sum : 0.0;
         const V tau = V(ctl->eta / ctl->omega);
-        double dx2 = 0.0;
+        V dx2 = V(0);
         const int stride = gridDim.x * kBlock;
         for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += stride) {
             V xv;
@@ -409,7 +426,7 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
             if (cand) {
                 const V x2 = clampv(xv - tau * (a.c[j] - a.ATY[cur][j]), lo_at(a, j), hi_at(a, j));
                 a.X[1 - cur][j] = x2;
-                const double d = double(x2) - double(xv);
+                const V d = x2 - xv;
                 dx2 += d * d;
             }
         }
@@ -424,7 +441,7 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
             }
             if (rst) { a.yl[i] = yv; a.ys[i] = V(0); }
         }
-        double v[1] = {dx2};
+        double v[1] = {double(dx2)};
         if (publish_partials<1>(v, a.part_aux, &ctl->ticket[T_APPLY], sm, &last)) {
             double t[1];
             gather_partials<1>(t, a.part_aux, gridDim.x, sm);
@@ -445,21 +462,21 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
 template <class V>
 struct StoreEpi {
     V* out;
-    __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1]) { out[r] = acc[0]; }
+    using Pre = NoPre;
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1], const Pre&) { out[r] = acc[0]; }
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) spmv_rows(Args<V> a, const V* x, V* out) {
-    __shared__ V red[kWarps];
+SPS_CHECK_KERNEL spmv_rows(Args<V> a, const V* x, V* out) {
     StoreEpi<V> e{out};
-    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{x}, e, red);
+    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{x}, e);
 }
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) spmv_cols(Args<V> a, const V* y, V* out) {
-    __shared__ V red[kWarps];
+SPS_CHECK_KERNEL spmv_cols(Args<V> a, const V* y, V* out) {
     StoreEpi<V> e{out};
-    visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{y}, e, red);
+    visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{y}, e);
 }
 
 // ============================================================================
@@ -472,44 +489,45 @@ template <class V>
 struct RfColStepEpi {
     const V *tau, *c;
     V *x, *xbar, *xs;
-    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1]) {
-        const V xv = x[j];
-        V x2 = rn_sub(xv, rn_mul(tau[j], rn_sub(c[j], acc[0])));
+    struct Pre { V xv, t, cj, s; };
+    __device__ __forceinline__ Pre pre(int j) const { return Pre{x[j], tau[j], c[j], xs[j]}; }
+    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) {
+        V x2 = rn_sub(p.xv, rn_mul(p.t, rn_sub(p.cj, acc[0])));
         x2 = fmax(x2, V(0));
-        xbar[j] = rn_sub(rn_mul(V(2), x2), xv);
+        xbar[j] = rn_sub(rn_mul(V(2), x2), p.xv);
         x[j] = x2;
-        xs[j] = rn_add(xs[j], x2);
+        xs[j] = rn_add(p.s, x2);
     }
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) rf_col_step(Args<V> a) {
+SPS_PASS_KERNEL rf_col_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
-    __shared__ V red[kWarps];
     RfColStepEpi<V> e{a.tau, a.c, a.X[0], a.xbar, a.xs};
-    visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[0]}, e, red);
+    visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[0]}, e);
 }
 
 template <class V>
 struct RfRowStepEpi {
     const V *sigma, *b;
     V *y, *ys;
-    __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1]) {
-        const V y2 = rn_add(y[r], rn_mul(sigma[r], rn_sub(b[r], acc[0])));
+    struct Pre { V yv, s, br, acc_s; };
+    __device__ __forceinline__ Pre pre(int r) const { return Pre{y[r], sigma[r], b[r], ys[r]}; }
+    __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1], const Pre& p) {
+        const V y2 = rn_add(p.yv, rn_mul(p.s, rn_sub(p.br, acc[0])));
         y[r] = y2;
-        ys[r] = rn_add(ys[r], y2);
+        ys[r] = rn_add(p.acc_s, y2);
     }
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) rf_row_step(Args<V> a) {
+SPS_PASS_KERNEL rf_row_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
-    __shared__ V red[kWarps];
     __shared__ bool last;
     RfRowStepEpi<V> e{a.sigma, a.b, a.Y[0], a.ys};
-    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.xbar}, e, red);
+    visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.xbar}, e);
     __syncthreads();
     if (threadIdx.x == 0) {
         __threadfence();
@@ -540,7 +558,9 @@ struct RfRowCheckEpi {
     V win;
     bool avg;
     double p[2] = {0, 0};     // ||A x - b||^2, b^T y
-    __device__ __forceinline__ void operator()(int r, int, const double (&acc)[1]) {
+    using Pre = NoPre;
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int r, int, const double (&acc)[1], const Pre&) {
         const double res = acc[0] - double(b[r]);
         p[0] += res * res;
         const double y = avg ? double(rn_div(yv[r], win)) : double(yv[r]);
@@ -551,16 +571,15 @@ struct RfRowCheckEpi {
 // mode: 0 = scheduled check of the average (only when window % interval == 0),
 //       1 = evaluate the current iterate (start-up error / final report).
 template <class V>
-__global__ void __launch_bounds__(kBlock) rf_row_check(Args<V> a, int mode) {
+SPS_CHECK_KERNEL rf_row_check(Args<V> a, int mode) {
     Ctl* ctl = a.ctl;
     if (mode == 0 && (ctl->done || ctl->window == 0 || ctl->window % a.check_interval != 0)) return;
     __shared__ double sm[kWarps * 2];
-    __shared__ double red[kWarps];
     const bool avg = mode == 0;
     const V win = V(ctl->window);
     RfGather<V> g{avg ? a.xs : a.X[0], win, avg};
     RfRowCheckEpi<V> e{a.b, avg ? a.ys : a.Y[0], win, avg};
-    visit_bins<1, double>(a.rows, blockIdx.x, a.csr, g, e, red);
+    visit_bins<1, double>(a.rows, blockIdx.x, a.csr, g, e);
     block_sum<2>(e.p, sm);
     if (threadIdx.x == 0) {
         a.part_row[(size_t)blockIdx.x * 2 + 0] = e.p[0];
@@ -574,7 +593,9 @@ struct RfColCheckEpi {
     V win;
     bool avg;
     double p[2] = {0, 0};     // ||min(c - A^T y, 0)||^2, c^T x
-    __device__ __forceinline__ void operator()(int j, int, const double (&acc)[1]) {
+    using Pre = NoPre;
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int j, int, const double (&acc)[1], const Pre&) {
         const double rc = double(c[j]) - acc[0];
         const double neg = fmin(rc, 0.0);
         p[0] += neg * neg;
@@ -584,17 +605,16 @@ struct RfColCheckEpi {
 };
 
 template <class V>
-__global__ void __launch_bounds__(kBlock) rf_col_check(Args<V> a, int mode) {
+SPS_CHECK_KERNEL rf_col_check(Args<V> a, int mode) {
     Ctl* ctl = a.ctl;
     if (mode == 0 && (ctl->done || ctl->window == 0 || ctl->window % a.check_interval != 0)) return;
     __shared__ double sm[kWarps * 2];
-    __shared__ double red[kWarps];
     __shared__ bool last;
     const bool avg = mode == 0;
     const V win = V(ctl->window);
     RfGather<V> g{avg ? a.ys : a.Y[0], win, avg};
     RfColCheckEpi<V> e{a.c, avg ? a.xs : a.X[0], win, avg};
-    visit_bins<1, double>(a.cols, blockIdx.x, a.csc, g, e, red);
+    visit_bins<1, double>(a.cols, blockIdx.x, a.csc, g, e);
     if (!publish_partials<2>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
     double tc[2], tr[2];
     gather_partials<2>(tc, a.part_col, gridDim.x, sm);

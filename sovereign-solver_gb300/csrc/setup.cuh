@@ -119,6 +119,43 @@ __global__ void k_finish_values(const int32_t* __restrict__ ptr, const int32_t* 
     }
 }
 
+// Final layout, SLICED bin: slot (slice, lane) of rows [begin, end) copies its
+// row's entries to soff[slice] + 32 k + lane, zero-padding to the slice length.
+template <class V>
+__global__ void k_fill_sliced(const int32_t* __restrict__ tptr, const int32_t* __restrict__ tidx,
+                              const V* __restrict__ tval, const int32_t* __restrict__ soff, int32_t begin,
+                              int32_t end, int32_t first_slice, int32_t nslices, int32_t* __restrict__ oidx,
+                              V* __restrict__ oval) {
+    const int64_t slots = (int64_t)nslices * 32;
+    for (int64_t sl = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; sl < slots; sl += (int64_t)gridDim.x * blockDim.x) {
+        const int s = (int)(sl >> 5), lane = (int)(sl & 31);
+        const int r = begin + (int)sl;
+        const int rs = r < end ? tptr[r] : 0;
+        const int len = r < end ? tptr[r + 1] - rs : 0;
+        const int off = soff[first_slice + s];
+        const int L = (soff[first_slice + s + 1] - off) >> 5;
+        for (int k = 0; k < L; ++k) {
+            oidx[off + 32 * k + lane] = k < len ? tidx[rs + k] : 0;
+            oval[off + 32 * k + lane] = k < len ? tval[rs + k] : V(0);
+        }
+    }
+}
+
+// Final layout, WARP / SEGMENT bins: rows [begin, end) copied to their final offsets.
+template <class V>
+__global__ void k_fill_rows(const int32_t* __restrict__ tptr, const int32_t* __restrict__ tidx,
+                            const V* __restrict__ tval, const int32_t* __restrict__ fptr, int32_t begin,
+                            int32_t end, int32_t* __restrict__ oidx, V* __restrict__ oval) {
+    const int lane = threadIdx.x & 31;
+    for (int r = begin + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); r < end; r += (gridDim.x * blockDim.x) >> 5) {
+        const int s = tptr[r], t = tptr[r + 1], d = fptr[r];
+        for (int k = s + lane; k < t; k += 32) {
+            oidx[d + k - s] = tidx[k];
+            oval[d + k - s] = tval[k];
+        }
+    }
+}
+
 // Scaled vectors from FP64 inputs already in internal order:
 //   c~ = c*dc, l~ = l/dc, u~ = u/dc (columns);  b~ = b*dr (rows).
 template <class V>

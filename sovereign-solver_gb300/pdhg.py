@@ -90,7 +90,7 @@ class _Desc:
 
 def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, tol=PDHG_TOL,
                  check_interval=0, ruiz_iters=10, time_limit=0.0, graph_mode=2, device=0,
-                 row_lanes_cta=1024) -> N.Options:
+                 max_blocks=0) -> N.Options:
     if mode not in N.MODES:
         raise ValueError(f"Unknown mode {mode!r}. Choose 'adaptive' or 'reference'.")
     if precision not in N.PRECISIONS:
@@ -101,7 +101,7 @@ def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, to
     o.max_iters, o.tol = int(max_iters), float(tol)
     o.check_interval, o.ruiz_iters = int(check_interval), int(ruiz_iters)
     o.time_limit_s, o.graph_mode, o.device = float(time_limit), int(graph_mode), int(device)
-    o.row_lanes_cta = int(row_lanes_cta)
+    o.max_blocks = int(max_blocks)
     return o
 
 
