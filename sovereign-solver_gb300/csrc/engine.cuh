@@ -59,7 +59,11 @@ struct Layout {
     const int32_t* seg_k;    // segment number inside its row
     double* seg_part;        // per-segment partial sums (2 doubles of room each)
     uint32_t* seg_ticket;    // per-row tickets of SEGMENT rows (left at 0 after every pass)
+    double* seg_rowpart;     // per SEGMENT row: its epilogue's reduction partials (room for 10)
+    int32_t nsegrows;        // SEGMENT rows of this orientation
 };
+
+constexpr int kMaxEpiPartials = 10;
 
 // Control block, one per handle, in device memory.  Written only by single
 // threads of "last blocks" or by block 0 thread 0, read by every kernel.
@@ -289,7 +293,32 @@ __device__ __forceinline__ void visit_segment(const Bin& b, int unit, const Layo
     for (int sg = 0; sg < nseg; ++sg)
 #pragma unroll
         for (int q = 0; q < NV; ++q) tot[q] += __ldcg(part + (size_t)(first + sg) * NV + q);
-    e(r, b.kind, tot, pre);
+    if constexpr (Epi::NP == 0) {
+        e(r, b.kind, tot, pre);
+    } else {
+        // Which warp finishes a row last varies between runs: the row's share of
+        // the kernel's reductions goes to its own slot, summed in row order by
+        // the kernel's last block, so every run adds the same numbers in the same order.
+        Epi one = e;
+        one.zero();
+        one(r, b.kind, tot, pre);
+        one.export_to(L.seg_rowpart + (size_t)(b.aux2 + (r - b.begin)) * Epi::NP);
+    }
+}
+
+// In a kernel's last block: add the SEGMENT rows' epilogue partials, in row order.
+template <int NP, class V>
+__device__ __forceinline__ void add_segment_rows(double (&tot)[NP], const Layout<V>& L, double* smem) {
+    double s[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) s[p] = 0.0;
+    for (int k = threadIdx.x; k < L.nsegrows; k += kBlock)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) s[p] += __ldcg(L.seg_rowpart + (size_t)k * NP + p);
+    block_sum<NP>(s, smem);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) tot[p] += s[p];
 }
 
 // Dispatch: find this block's bin; each warp walks the bin's units with a

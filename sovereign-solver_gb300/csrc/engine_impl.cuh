@@ -317,7 +317,7 @@ struct Engine : EngineBase {
         std::vector<std::pair<void**, size_t>> plan;
         int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx, *d_rsoff, *d_csoff, *d_rseg, *d_rsegk, *d_cseg, *d_csegk;
         V *d_rval, *d_cval, *d_c, *d_b, *d_lo = nullptr, *d_hi = nullptr, *d_tau = nullptr, *d_sigma = nullptr;
-        double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa, *d_segpart;
+        double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa, *d_segpart, *d_rowpart_r, *d_rowpart_c;
         uint32_t* d_tickets;
         V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
         V *xs, *ys, *xl = nullptr, *yl = nullptr, *AXa = nullptr, *ATYa = nullptr, *xbar = nullptr;
@@ -344,6 +344,8 @@ struct Engine : EngineBase {
         add(&d_csegk, sizeof(int32_t) * (cp.seg_row.size() + 1));
         add(&d_segpart, sizeof(double) * 2 * nseg);
         add(&d_tickets, sizeof(uint32_t) * ntk);
+        add(&d_rowpart_r, sizeof(double) * kMaxEpiPartials * std::max(rp.ntickets, 1));
+        add(&d_rowpart_c, sizeof(double) * kMaxEpiPartials * std::max(cp.ntickets, 1));
         add(&d_perm_row, sizeof(int32_t) * m);
         add(&d_perm_col, sizeof(int32_t) * n);
         add(&d_rkind, m);
@@ -476,6 +478,10 @@ struct Engine : EngineBase {
         if (int rc = build_layout(cp, n, t_cptr, t_cidx, t_cvV, Lc, d_cptr, d_csoff, d_cseg, d_csegk, d_cidx, d_cval)) return rc;
         Lr.seg_part = Lc.seg_part = d_segpart;
         Lr.seg_ticket = Lc.seg_ticket = d_tickets;
+        Lr.seg_rowpart = d_rowpart_r;
+        Lc.seg_rowpart = d_rowpart_c;
+        Lr.nsegrows = rp.ntickets;
+        Lc.nsegrows = cp.ntickets;
 
         // ---- vectors in internal order
         {

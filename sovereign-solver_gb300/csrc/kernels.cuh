@@ -105,6 +105,9 @@ struct AdRowStepEpi {
     V sigma;
     V dy2 = V(0), inter = V(0);          // per-thread partials; FP64 from the block sum on
     struct Pre { V ao, yv, br; };
+    static constexpr int NP = 2;
+    __device__ __forceinline__ void zero() { dy2 = inter = V(0); }
+    __device__ __forceinline__ void export_to(double* d) const { d[0] = double(dy2); d[1] = double(inter); }
     __device__ __forceinline__ Pre pre(int r) const { return Pre{axo[r], yo[r], b[r]}; }
     __device__ __forceinline__ void operator()(int r, int kind, const V (&acc)[1], const Pre& p) {
         const V ax = acc[0];
@@ -131,6 +134,7 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     if (!publish_partials<2>(v, a.part_row, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
     double t[2];
     gather_partials<2>(t, a.part_row, gridDim.x, sm);
+    add_segment_rows<2>(t, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_ROW_STEP] = 0;
     // adaptive step (PDLP): limit = ||dz||_w^2 / (2 |dy^T K dx|); accept if eta <= limit;
@@ -171,6 +175,9 @@ struct AdColStepEpi {
     bool accepted;
     V dx2 = V(0);
     struct Pre { V xj, cj, lo, hi, s; };
+    static constexpr int NP = 1;
+    __device__ __forceinline__ void zero() { dx2 = V(0); }
+    __device__ __forceinline__ void export_to(double* d) const { d[0] = double(dx2); }
     __device__ __forceinline__ Pre pre(int j) const {
         Pre p;
         p.xj = xc[j];
@@ -218,6 +225,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     if (!publish_partials<1>(v, a.part_col, &ctl->ticket[T_COL_STEP], sm, &last)) return;
     double t[1];
     gather_partials<1>(t, a.part_col, gridDim.x, sm);
+    add_segment_rows<1>(t, a.csc, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_STEP] = 0;
     ctl->dx2 = t[0];
@@ -244,6 +252,9 @@ struct AdRowCheckEpi {
     double inv_w;
     double p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // per point q: res_scaled^2, res_orig^2, b^T y, ||y - y_last||^2
     using Pre = NoPre;
+    static constexpr int NP = 8;
+    __device__ __forceinline__ void zero() { for (int q = 0; q < NP; ++q) p[q] = 0.0; }
+    __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int r, int kind, const double (&acc)[2], const Pre&) {
         const double br = double(a->b[r]), dr = a->dr[r];
@@ -288,6 +299,9 @@ struct AdColCheckEpi {
     double inv_w;
     double p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // per point: dres_s^2, dres_o^2, c^T x, bound terms, ||x - x_last||^2
     using Pre = NoPre;
+    static constexpr int NP = 10;
+    __device__ __forceinline__ void zero() { for (int q = 0; q < NP; ++q) p[q] = 0.0; }
+    __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int j, int, const double (&acc)[2], const Pre&) {
         const double cj = double(a->c[j]), dc = a->dc[j];
@@ -327,6 +341,8 @@ SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     double tc[10], tr[8];
     gather_partials<10>(tc, a.part_col, gridDim.x, sm);
     gather_partials<8>(tr, a.part_row, a.rows.total_blocks, sm);
+    add_segment_rows<10>(tc, a.csc, sm);
+    add_segment_rows<8>(tr, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_CHECK] = 0;
 
@@ -463,6 +479,7 @@ template <class V>
 struct StoreEpi {
     V* out;
     using Pre = NoPre;
+    static constexpr int NP = 0;
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1], const Pre&) { out[r] = acc[0]; }
 };
@@ -490,6 +507,7 @@ struct RfColStepEpi {
     const V *tau, *c;
     V *x, *xbar, *xs;
     struct Pre { V xv, t, cj, s; };
+    static constexpr int NP = 0;
     __device__ __forceinline__ Pre pre(int j) const { return Pre{x[j], tau[j], c[j], xs[j]}; }
     __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) {
         V x2 = rn_sub(p.xv, rn_mul(p.t, rn_sub(p.cj, acc[0])));
@@ -513,6 +531,7 @@ struct RfRowStepEpi {
     const V *sigma, *b;
     V *y, *ys;
     struct Pre { V yv, s, br, acc_s; };
+    static constexpr int NP = 0;
     __device__ __forceinline__ Pre pre(int r) const { return Pre{y[r], sigma[r], b[r], ys[r]}; }
     __device__ __forceinline__ void operator()(int r, int, const V (&acc)[1], const Pre& p) {
         const V y2 = rn_add(p.yv, rn_mul(p.s, rn_sub(p.br, acc[0])));
@@ -559,6 +578,9 @@ struct RfRowCheckEpi {
     bool avg;
     double p[2] = {0, 0};     // ||A x - b||^2, b^T y
     using Pre = NoPre;
+    static constexpr int NP = 2;
+    __device__ __forceinline__ void zero() { p[0] = p[1] = 0.0; }
+    __device__ __forceinline__ void export_to(double* d) const { d[0] = p[0]; d[1] = p[1]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int r, int, const double (&acc)[1], const Pre&) {
         const double res = acc[0] - double(b[r]);
@@ -594,6 +616,9 @@ struct RfColCheckEpi {
     bool avg;
     double p[2] = {0, 0};     // ||min(c - A^T y, 0)||^2, c^T x
     using Pre = NoPre;
+    static constexpr int NP = 2;
+    __device__ __forceinline__ void zero() { p[0] = p[1] = 0.0; }
+    __device__ __forceinline__ void export_to(double* d) const { d[0] = p[0]; d[1] = p[1]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int j, int, const double (&acc)[1], const Pre&) {
         const double rc = double(c[j]) - acc[0];
@@ -619,6 +644,8 @@ SPS_CHECK_KERNEL rf_col_check(Args<V> a, int mode) {
     double tc[2], tr[2];
     gather_partials<2>(tc, a.part_col, gridDim.x, sm);
     gather_partials<2>(tr, a.part_row, a.rows.total_blocks, sm);
+    add_segment_rows<2>(tc, a.csc, sm);
+    add_segment_rows<2>(tr, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_CHECK] = 0;
     const double rp = sqrt(tr[0]) * a.inv_nb;

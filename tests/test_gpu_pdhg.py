@@ -103,6 +103,23 @@ def test_graph_modes_agree_bitwise(graph_mode):
     np.testing.assert_array_equal(r.y, base.y)
 
 
+@pytest.mark.parametrize("max_blocks", [8, 0])
+def test_segmented_rows_deterministic(max_blocks):
+    """Rows longer than one 512-nonzero segment, with few blocks so each warp
+    handles several segments: results must be bit-identical run to run."""
+    p, _ = wl.transportation_lp(120, 1500, seed=4)      # supply rows of 1500 -> 3 segments
+    runs = []
+    for gm in (2, 0):
+        with sps.PDHGEngine(p, tol=1e-4, max_blocks=max_blocks, graph_mode=gm) as eng:
+            runs += [eng.solve(), eng.solve()]
+    for r in runs[1:]:
+        assert r.iterations == runs[0].iterations
+        np.testing.assert_array_equal(r.x, runs[0].x)
+        np.testing.assert_array_equal(r.y, runs[0].y)
+    assert runs[0].status == "optimal"
+    assert kkt.box_rel_kkt(p, runs[0].x, runs[0].y)["err"] < 1.5e-4
+
+
 def test_repeat_solve_is_deterministic_and_warm_start_helps():
     p, info = wl.planted_lp(seed=5)
     with sps.PDHGEngine(p, tol=1e-5) as eng:
