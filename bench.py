@@ -184,7 +184,8 @@ def run_ours(args, rank, world):
 
     p, info, cfg = make_workload(args.config, seed=args.seed + rank)
     hbm, peak_kind = peaks()
-    eng = sps.PDHGEngine(p, tol=args.tol, max_iters=args.max_iters, device=args.device)
+    eng = sps.PDHGEngine(p, tol=args.tol, max_iters=args.max_iters, device=args.device,
+                         graph_mode=args.graph_mode)
     for _ in range(args.warmup):
         r = eng.solve_raw()
     barrier(world)
@@ -211,7 +212,8 @@ def run_ours(args, rank, world):
         if a.size and a.ctypes.data not in seen and lib.sps_pin_host(a.ctypes.data, a.nbytes) == 0:
             pinned.append(a)
             seen.add(a.ctypes.data)
-    opts = pdhg.make_options(tol=args.tol, max_iters=args.max_iters, device=args.device)
+    opts = pdhg.make_options(tol=args.tol, max_iters=args.max_iters, device=args.device,
+                             graph_mode=args.graph_mode)
     xo, yo = np.empty(d.n), np.empty(d.m_ub + d.m_eq)
     for a in (xo, yo):
         if lib.sps_pin_host(a.ctypes.data, a.nbytes) == 0:
@@ -365,6 +367,9 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--graph-mode", type=int, default=2,
+                    help="2: one graph with a device-driven loop (default); 1: replayed window graph; "
+                         "0: plain launches (what a profiler's launch list can see kernel by kernel)")
     args = ap.parse_args()
     rank, world = init_dist()
     args.device = int(os.environ.get("LOCAL_RANK", "0"))
