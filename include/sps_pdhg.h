@@ -149,6 +149,35 @@ int sps_unpin_host(void *ptr);
 /* Library build string (arch, precision support). */
 const char *sps_version(void);
 
+/* An LP whose arrays already live in device memory (all pointers are device
+ * pointers): K = [A_ub; A_eq] in CSR with the m_ub '<=' rows first. */
+typedef struct {
+    int32_t n, m_ub, m_eq;
+    const int32_t *indptr;          /* m_ub + m_eq + 1 */
+    const int32_t *indices;
+    const double  *values;
+    const double  *c;               /* n */
+    const double  *rhs;             /* m_ub + m_eq: b_ub then b_eq */
+    const double  *lb, *ub;         /* n, +-INFINITY allowed */
+} sps_device_lp;
+
+/* Relative KKT error of a point (x, y) of a device-resident LP, computed in
+ * FP64 without allocating any device memory.  No counterpart in the
+ * reference.  For callers that cannot call cudaMalloc at that point: code
+ * inside another framework's memory pool or a fixed device-memory budget, or a
+ * latency-critical loop where an allocation would synchronise the device.
+ * x (n), y (m_ub + m_eq) and out are device pointers; out receives 6 doubles:
+ * rel_kkt, rel_primal, rel_dual, rel_gap, primal objective, dual objective —
+ * the same measure sps_solve reports (sps_result.rel_*).  Work is queued on
+ * `stream` (a cudaStream_t, NULL = default stream); the call does not wait.
+ * Scratch is a fixed ~2.1 MB device array inside the library (held by every
+ * GPU that loads it until exit), so n is limited to 262144 columns (larger n
+ * returns SPS_ERR_INVALID); rows are unlimited.  All calls share that array:
+ * calls that overlap on the GPU race — order them on one stream.  The first
+ * call on each device looks up the array's device address; make that first
+ * call before any stream capture.  Errors: sps_last_error(NULL). */
+int sps_kkt_noalloc(const sps_device_lp *lp, const double *x, const double *y, double *out, void *stream);
+
 /* Number of visible CUDA devices (0 when none or the driver is unusable).
  * Backs get_available_device (solver/lp/pdhg_gpu.py:42-67), without its
  * CuPy/MPS/CPU probing. */

@@ -55,6 +55,15 @@ class Result(C.Structure):
     ]
 
 
+class DeviceLP(C.Structure):
+    """sps_device_lp: every pointer is a device address (integers from the caller's allocator)."""
+    _fields_ = [
+        ("n", C.c_int32), ("m_ub", C.c_int32), ("m_eq", C.c_int32),
+        ("indptr", C.c_void_p), ("indices", C.c_void_p), ("values", C.c_void_p),
+        ("c", C.c_void_p), ("rhs", C.c_void_p), ("lb", C.c_void_p), ("ub", C.c_void_p),
+    ]
+
+
 _lib = None
 
 
@@ -87,6 +96,7 @@ def load() -> C.CDLL:
         "sps_version": (C.c_char_p, []),
         "sps_device_count": (C.c_int, []),
         "sps_time_iteration_kernels": (C.c_int, [H, C.c_int32, _f64p]),
+        "sps_kkt_noalloc": (C.c_int, [C.POINTER(DeviceLP), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

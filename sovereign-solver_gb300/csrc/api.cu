@@ -161,6 +161,11 @@ void build_standard(const sps_problem_desc* d, HostProblem& hp, StdMap& s) {
 
 }  // namespace
 
+namespace sps {
+// Message returned by sps_last_error(NULL) for calls without a handle.
+void set_create_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace sps
+
 extern "C" {
 
 int sps_options_init(sps_options* o) {
