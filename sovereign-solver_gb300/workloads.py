@@ -63,18 +63,24 @@ def _fill_empty_columns(rows: np.ndarray, cols: np.ndarray, m: int, n: int,
 
 
 def _distinct_per_group(group_sizes: np.ndarray, universe: int,
-                        rng: np.random.Generator) -> tuple[np.ndarray, np.ndarray]:
+                        rng: np.random.Generator, exact: bool = True) -> tuple[np.ndarray, np.ndarray]:
     """For each group g draw group_sizes[g] distinct members of range(universe).
 
     Draw with replacement, drop duplicates inside each group, redraw the
     shortfall, repeat; exact "without replacement" semantics for any size
-    ≤ universe.  Returns (group_id, member) pairs sorted by (group, member).
+    ≤ universe.  With ``exact=False`` the duplicates are only dropped (for
+    group sizes far below the universe, where they are rare).  Returns
+    (group_id, member) pairs sorted by (group, member).
     """
     k = np.minimum(group_sizes.astype(np.int64), universe)
     groups = np.repeat(np.arange(k.size, dtype=np.int64), k)
     members = rng.integers(0, universe, groups.size)
     while True:
-        key = np.unique(groups * universe + members)
+        key = groups * universe + members
+        key.sort()
+        key = key[np.concatenate(([True], key[1:] != key[:-1]))] if key.size else key
+        if not exact:
+            return key // universe, key % universe
         g = key // universe
         have = np.bincount(g, minlength=k.size)
         short = k - have
@@ -149,11 +155,21 @@ def powerlaw_lp(m: int = 1_000_000, n: int = 2_000_000, target_nnz: int | None =
     L = np.clip(rng.zipf(1.5, m), 2, 5000).astype(np.int64)
     if target_nnz is not None:
         L = np.maximum(2, np.floor(L * (target_nnz / L.sum()))).astype(np.int64)
-    rows, cols = _distinct_per_group(L, n, rng)
-    rows, cols = _fill_empty_columns(rows, cols, m, n, rng)
+    # rows of at most 5000 distinct columns out of 2M: duplicate draws are rare
+    # (≈ L²/2n per row) and are dropped rather than redrawn
+    rows, cols = _distinct_per_group(L, n, rng, exact=False)
+    present = np.zeros(n, dtype=bool)
+    present[cols] = True
+    empty = np.flatnonzero(~present)
+    if empty.size:   # one entry in a random row for every empty column, merged in row order
+        er = rng.integers(0, m, empty.size)
+        key = np.concatenate([rows * n + cols, er * n + empty])
+        key.sort()
+        rows, cols = key // n, key % n
     vals = rng.standard_normal(rows.size)
-    A = sp.csr_matrix((vals, (rows, cols)), shape=(m, n))
-    A.sort_indices()
+    indptr = np.zeros(m + 1, dtype=np.int64)
+    np.cumsum(np.bincount(rows, minlength=m), out=indptr[1:])
+    A = sp.csr_matrix((vals, cols.astype(np.int32), indptr.astype(np.int32)), shape=(m, n))
     b, c, xs, ys, obj = _plant(A, rng, u)
     p = Problem(c=c, A_ub=sp.csr_matrix((0, n)), b_ub=np.zeros(0), A_eq=A, b_eq=b,
                 lb=np.zeros(n), ub=np.full(n, u), integer_mask=np.zeros(n, dtype=bool),
