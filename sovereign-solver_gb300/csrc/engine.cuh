@@ -253,29 +253,93 @@ __device__ __forceinline__ void warp_dot(int s, int t, const Layout<V>& L, const
     for (int q = 0; q < NV; ++q) acc[q] = group_sum<32>(acc[q]);
 }
 
-template <int NV, class Acc, class V, class Gather, class Epi>
-__device__ __forceinline__ void visit_warp_row(const Bin& b, int unit, const Layout<V>& L, const Gather& g,
-                                               Epi& e) {
-    const int r = b.begin + unit;
-    const bool lead = (threadIdx.x & 31) == 0;
-    typename Epi::Pre pre;
-    if (lead) pre = e.pre(r);
-    Acc acc[NV];
-    warp_dot<NV, Acc>(__ldg(L.ptr + r), __ldg(L.ptr + r + 1), L, g, acc);
-    if (lead) e(r, b.kind, acc, pre);
+// Dot products of two nonzero ranges [s0, t0) and [s1, t1) with the warp, their
+// loads interleaved so both ranges' requests are in flight together.
+template <int NV, class Acc, class V, class Gather>
+__device__ __forceinline__ void warp_dot2(int s0, int t0, int s1, int t1, const Layout<V>& L, const Gather& g,
+                                          Acc (&acc)[2][NV]) {
+    constexpr int U = kUnroll / 2;
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[h][q] = Acc(0);
+    const int n0 = t0 - s0, n1 = t1 - s1, nmax = max(n0, n1);
+    for (int k = lane; k < nmax; k += 32 * U) {
+        int j[2][U];
+        Acc a[2][U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int kk = k + 32 * u;
+            const bool ok0 = kk < n0, ok1 = kk < n1;
+            j[0][u] = ok0 ? __ldg(L.idx + s0 + kk) : 0;
+            a[0][u] = ok0 ? Acc(__ldg(L.val + s0 + kk)) : Acc(0);
+            j[1][u] = ok1 ? __ldg(L.idx + s1 + kk) : 0;
+            a[1][u] = ok1 ? Acc(__ldg(L.val + s1 + kk)) : Acc(0);
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int u = 0; u < U; ++u)
+#pragma unroll
+                for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[h][q] = group_sum<32>(acc[h][q]);
 }
 
+// WARP: rows u0 and u1 of the bin (u1 may be past the bin: then it is skipped).
 template <int NV, class Acc, class V, class Gather, class Epi>
-__device__ __forceinline__ void visit_segment(const Bin& b, int unit, const Layout<V>& L, const Gather& g,
-                                              Epi& e) {
-    const int gseg = b.aux + unit;
-    const int r = __ldg(L.seg_row + gseg), kseg = __ldg(L.seg_k + gseg);
-    const int rs = __ldg(L.ptr + r), re = __ldg(L.ptr + r + 1);
-    const int s = rs + kseg * kSegment;
-    const int t = min(re, s + kSegment);
-    Acc acc[NV];
-    warp_dot<NV, Acc>(s, t, L, g, acc);
+__device__ __forceinline__ void visit_warp_row_pair(const Bin& b, int u0, int u1, const Layout<V>& L,
+                                                    const Gather& g, Epi& e) {
+    const bool has1 = u1 < b.units;
+    const int r0 = b.begin + u0, r1 = b.begin + (has1 ? u1 : u0);
+    const bool lead = (threadIdx.x & 31) == 0;
+    typename Epi::Pre pre0, pre1;
+    if (lead) {
+        pre0 = e.pre(r0);
+        if (has1) pre1 = e.pre(r1);
+    }
+    const int s0 = __ldg(L.ptr + r0), t0 = __ldg(L.ptr + r0 + 1);
+    const int s1 = __ldg(L.ptr + r1), t1 = has1 ? __ldg(L.ptr + r1 + 1) : s1;
+    Acc acc[2][NV];
+    warp_dot2<NV, Acc>(s0, t0, s1, t1, L, g, acc);
+    if (lead) {
+        e(r0, b.kind, acc[0], pre0);
+        if (has1) e(r1, b.kind, acc[1], pre1);
+    }
+}
+
+// SEGMENT: the dot products of segments u0 and u1 (u1 may be past the bin),
+// then each segment's share of its row.
+template <int NV, class Acc, class V, class Epi>
+__device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, int kseg, int rs, int re,
+                                               const Acc (&acc)[NV], const Layout<V>& L, Epi& e);
+
+template <int NV, class Acc, class V, class Gather, class Epi>
+__device__ __forceinline__ void visit_segment_pair(const Bin& b, int u0, int u1, const Layout<V>& L,
+                                                   const Gather& g, Epi& e) {
+    const bool has1 = u1 < b.units;
+    const int gs0 = b.aux + u0, gs1 = b.aux + (has1 ? u1 : u0);
+    const int r0 = __ldg(L.seg_row + gs0), k0 = __ldg(L.seg_k + gs0);
+    const int r1 = __ldg(L.seg_row + gs1), k1 = __ldg(L.seg_k + gs1);
+    const int rs0 = __ldg(L.ptr + r0), re0 = __ldg(L.ptr + r0 + 1);
+    const int rs1 = __ldg(L.ptr + r1), re1 = __ldg(L.ptr + r1 + 1);
+    const int s0 = rs0 + k0 * kSegment, t0 = min(re0, s0 + kSegment);
+    const int s1 = rs1 + k1 * kSegment, t1 = has1 ? min(re1, s1 + kSegment) : s1;
+    Acc acc[2][NV];
+    warp_dot2<NV, Acc>(s0, t0, s1, t1, L, g, acc);
     if ((threadIdx.x & 31) != 0) return;
+    finish_segment<NV, Acc>(b, gs0, r0, k0, rs0, re0, acc[0], L, e);
+    if (has1) finish_segment<NV, Acc>(b, gs1, r1, k1, rs1, re1, acc[1], L, e);
+}
+
+// One lane: publish a segment's partial; the row's last segment adds them all.
+template <int NV, class Acc, class V, class Epi>
+__device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, int kseg, int rs, int re,
+                                               const Acc (&acc)[NV], const Layout<V>& L, Epi& e) {
     Acc* part = reinterpret_cast<Acc*>(L.seg_part);
 #pragma unroll
     for (int q = 0; q < NV; ++q) part[(size_t)gseg * NV + q] = acc[q];
@@ -309,12 +373,25 @@ __device__ __forceinline__ void visit_segment(const Bin& b, int unit, const Layo
 // In a kernel's last block: add the SEGMENT rows' epilogue partials, in row order.
 template <int NP, class V>
 __device__ __forceinline__ void add_segment_rows(double (&tot)[NP], const Layout<V>& L, double* smem) {
+    // B rows' loads are issued before their adds: B round trips overlap instead
+    // of one L2 round trip per row (fixed order, so the sum stays deterministic)
+    constexpr int B = NP <= 2 ? 8 : 2;
     double s[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) s[p] = 0.0;
-    for (int k = threadIdx.x; k < L.nsegrows; k += kBlock)
+    for (int k0 = threadIdx.x; k0 < L.nsegrows; k0 += kBlock * B) {
+        double v[B][NP];
 #pragma unroll
-        for (int p = 0; p < NP; ++p) s[p] += __ldcg(L.seg_rowpart + (size_t)k * NP + p);
+        for (int u = 0; u < B; ++u) {
+            const int k = k0 + u * kBlock;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) v[u][p] = k < L.nsegrows ? __ldcg(L.seg_rowpart + (size_t)k * NP + p) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) s[p] += v[u][p];
+    }
     block_sum<NP>(s, smem);
     if (threadIdx.x == 0)
 #pragma unroll
@@ -338,9 +415,9 @@ __device__ __forceinline__ void visit_bins(const BinTable& bt, int block, const 
     if (b.mode == BM_SLICED) {
         for (int u = w0; u < b.units; u += 2 * stride) visit_slice_pair<NV, Acc>(b, u, u + stride, L, g, e);
     } else if (b.mode == BM_WARP) {
-        for (int u = w0; u < b.units; u += stride) visit_warp_row<NV, Acc>(b, u, L, g, e);
+        for (int u = w0; u < b.units; u += 2 * stride) visit_warp_row_pair<NV, Acc>(b, u, u + stride, L, g, e);
     } else {
-        for (int u = w0; u < b.units; u += stride) visit_segment<NV, Acc>(b, u, L, g, e);
+        for (int u = w0; u < b.units; u += 2 * stride) visit_segment_pair<NV, Acc>(b, u, u + stride, L, g, e);
     }
 }
 

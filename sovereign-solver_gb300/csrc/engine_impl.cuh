@@ -120,6 +120,10 @@ struct Engine : EngineBase {
         int32_t ntickets = 0;
     };
 
+    // Blocks that give every warp of the bin work for its first step (warps
+    // take two units per step).
+    static int64_t blocks_needed(const Bin& b) { return (b.units + 2 * kWarps - 1) / (2 * kWarps); }
+
     static int mode_of(int64_t len) {
         return len <= kSliceMax ? BM_SLICED : (len <= kSegment ? BM_WARP : BM_SEGMENT);
     }
@@ -147,6 +151,7 @@ struct Engine : EngineBase {
         P.fptr.assign(R + 1, 0);
         P.bt = BinTable{};
         int64_t off = 0;
+        std::vector<int64_t> bin_store;              // stored entries per bin
         for (int r = 0; r < R;) {
             const int kd = kind_of(P.perm[r]), md = mode_of(lens[P.perm[r]]);
             int e = r;
@@ -156,6 +161,7 @@ struct Engine : EngineBase {
             b.end = e;
             b.mode = md;
             b.kind = kd;
+            const int64_t bin_off0 = off;
             if (md == BM_SLICED) {
                 b.aux = (int32_t)P.soff.size();
                 for (int q = r; q < e; ++q) P.fptr[q] = (int32_t)off;
@@ -180,19 +186,31 @@ struct Engine : EngineBase {
                 b.units = (int32_t)P.seg_row.size() - b.aux;
                 P.ntickets += e - r;
             }
+            bin_store.push_back(off - bin_off0);
             P.bt.bin[P.bt.nbins++] = b;
             r = e;
         }
         P.fptr[R] = (int32_t)std::min<int64_t>(off, INT32_MAX);
         P.total = off;
-        int64_t want = 0;
-        for (int i = 0; i < P.bt.nbins; ++i) want += (P.bt.bin[i].units + kWarps - 1) / kWarps;
-        const double scale = want > block_cap ? double(block_cap) / double(want) : 1.0;
+        // Blocks: one resident wave shared by the bins in proportion to their
+        // work (stored entries plus a per-unit overhead of one 32-entry step),
+        // never more than one warp per unit.
+        int64_t need_total = 0;
+        double work_total = 0.0;
+        std::vector<double> work(P.bt.nbins);
+        for (int i = 0; i < P.bt.nbins; ++i) {
+            const Bin& b = P.bt.bin[i];
+            need_total += blocks_needed(b);
+            work[i] = double(bin_store[i]) + 32.0 * b.units;
+            work_total += work[i];
+        }
+        const int64_t budget = std::min<int64_t>(block_cap, need_total);
         int blocks = 0;
         for (int i = 0; i < P.bt.nbins; ++i) {
             Bin& b = P.bt.bin[i];
-            const int64_t need = (b.units + kWarps - 1) / kWarps;
-            b.nblocks = (int)std::max<int64_t>(1, (int64_t)std::ceil(need * scale));
+            const int64_t need = blocks_needed(b);
+            const int64_t share = (int64_t)std::ceil(budget * work[i] / std::max(work_total, 1.0));
+            b.nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(need, share));
             b.block_begin = blocks;
             blocks += b.nblocks;
         }
