@@ -79,8 +79,9 @@ typedef struct {
     int32_t graph_mode;       /* 0 = plain launches, 1 = replayed window graph,
                                  2 = one graph with a device-driven while loop (default) */
     int32_t device;           /* CUDA device ordinal */
-    int32_t max_blocks;       /* schedule tuning: blocks per matrix-pass launch, 0 = 16 per SM */
-    int32_t reserved[6];
+    int32_t max_blocks;       /* schedule tuning: blocks per matrix-pass launch, 0 = one resident wave */
+    int32_t batch_group;      /* batched solver: lanes per column (4, 8, 16, 32), 0 = autotune */
+    int32_t reserved[5];
 } sps_options;
 
 typedef struct {
@@ -148,6 +149,34 @@ int sps_unpin_host(void *ptr);
 
 /* Library build string (arch, precision support). */
 const char *sps_version(void);
+
+/* ---- batched solver: thousands of independent LPs in one persistent launch.
+ * New API surface (the reference solves one LP per call; its MILP strong
+ * branching, solver/milp/branching.py:132-210, is the natural batch caller).
+ * Adaptive mode, FP32 iterates, FP64 checks; every instance keeps its own step
+ * size, primal weight, restarts and termination. */
+typedef struct sps_batch sps_batch;
+
+typedef struct {
+    double  setup_ms;           /* sps_batch_create device work (upload excluded) */
+    double  solve_ms;           /* device time of the persistent launch */
+    int64_t total_iterations;   /* sum over instances */
+    int32_t optimal;            /* instances that reached tol */
+    int32_t lanes_per_column;   /* schedule used (autotuned or given) */
+    int32_t blocks;             /* persistent blocks */
+    int32_t reserved[5];
+} sps_batch_stats;
+
+/* Pack `count` problems, upload and scale them (one block per instance) and pick
+ * the schedule (opt->batch_group, or timed on a sample when 0). */
+int sps_batch_create(int32_t count, const sps_problem_desc *probs, const sps_options *opt, sps_batch **out);
+/* Solve every instance: one persistent launch, captured in a CUDA graph on the
+ * first call and replayed afterwards; blocking. */
+int sps_batch_solve(sps_batch *b, sps_batch_stats *stats);
+/* Instance k of the last solve: x (n, clipped to bounds), y (m_ub + m_eq), result. */
+int sps_batch_get(sps_batch *b, int32_t k, double *x, double *y, sps_result *res);
+const char *sps_batch_last_error(const sps_batch *b);
+void sps_batch_destroy(sps_batch *b);
 
 /* An LP whose arrays already live in device memory (all pointers are device
  * pointers): K = [A_ub; A_eq] in CSR with the m_ub '<=' rows first. */

@@ -11,7 +11,8 @@ from .problem import Problem
 from .result import SolveResult
 from .pdhg import PDHGEngine, get_available_device, solve_lp_pdhg, solve_lp_pdhg_gpu
 from .solver import Solver
+from .batch import PDHGBatch, solve_lp_pdhg_batch
 
 __version__ = "0.1.0"
 __all__ = ["Solver", "Problem", "SolveResult", "PDHGEngine", "solve_lp_pdhg",
-           "solve_lp_pdhg_gpu", "get_available_device"]
+           "solve_lp_pdhg_gpu", "get_available_device", "PDHGBatch", "solve_lp_pdhg_batch"]

@@ -40,7 +40,15 @@ class Options(C.Structure):
         ("mode", C.c_int32), ("precision", C.c_int32), ("max_iters", C.c_int64), ("tol", C.c_double),
         ("check_interval", C.c_int32), ("ruiz_iters", C.c_int32), ("time_limit_s", C.c_double),
         ("graph_mode", C.c_int32), ("device", C.c_int32), ("max_blocks", C.c_int32),
-        ("reserved", C.c_int32 * 6),
+        ("batch_group", C.c_int32), ("reserved", C.c_int32 * 5),
+    ]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [
+        ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("total_iterations", C.c_int64),
+        ("optimal", C.c_int32), ("lanes_per_column", C.c_int32), ("blocks", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 
@@ -97,6 +105,11 @@ def load() -> C.CDLL:
         "sps_device_count": (C.c_int, []),
         "sps_time_iteration_kernels": (C.c_int, [H, C.c_int32, _f64p]),
         "sps_kkt_noalloc": (C.c_int, [C.POINTER(DeviceLP), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+        "sps_batch_create": (C.c_int, [C.c_int32, C.POINTER(ProblemDesc), C.POINTER(Options), C.POINTER(H)]),
+        "sps_batch_solve": (C.c_int, [H, C.POINTER(BatchStats)]),
+        "sps_batch_get": (C.c_int, [H, C.c_int32, _f64p, _f64p, C.POINTER(Result)]),
+        "sps_batch_last_error": (C.c_char_p, [H]),
+        "sps_batch_destroy": (None, [H]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

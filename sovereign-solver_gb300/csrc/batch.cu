@@ -1,0 +1,840 @@
+// batch.cu — batched restarted PDHG (sps_batch_* in include/sps_pdhg.h).
+//
+// sps_batch_create packs thousands of box-form LPs (CSR of [A_ub; A_eq] plus a
+// CSC built on the host by a per-instance counting sort, spread over host
+// threads), uploads them once, and scales every instance on the device (one
+// block per instance: 10 Ruiz passes + one Pock-Chambolle pass, FP64).
+// sps_batch_solve is ONE persistent launch (captured once in a CUDA graph and
+// replayed on later calls): each block takes the next-largest unsolved
+// instance from an atomic counter and runs the whole adaptive PDHG loop on it
+// with per-instance step size, primal weight, restarts and termination.
+// The lanes-per-column of the column pass is chosen by a small autotuner that
+// times the candidates on a sample of the batch.
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <memory>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "batch.cuh"
+
+namespace sps {
+void set_create_error(const std::string& msg);
+namespace batch {
+
+struct Gather1 {
+    const float* x;
+    __device__ __forceinline__ float operator()(int, int j) const { return __ldg(x + j); }
+};
+
+struct Gather2 {
+    const float *s, *x;
+    double inv_w;
+    __device__ __forceinline__ double operator()(int q, int j) const {
+        return q == 0 ? double(__ldg(s + j)) * inv_w : double(__ldg(x + j));
+    }
+};
+
+struct StoreE {
+    float* out;
+    struct Pre {};
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int r, const float (&acc)[1], const Pre&) { out[r] = acc[0]; }
+};
+
+// row pass of a step attempt: K x' and y' = proj(y + sigma (b - (2 K x' - K x)))
+struct RowStepE {
+    const float *b, *axo, *yo;
+    const int8_t* kind;
+    float *axn, *yn;
+    float sigma;
+    float dy2 = 0.f, inter = 0.f;
+    struct Pre { float ao, yv, br; int kd; };
+    __device__ __forceinline__ Pre pre(int r) const { return Pre{axo[r], yo[r], b[r], kind[r]}; }
+    __device__ __forceinline__ void operator()(int r, const float (&acc)[1], const Pre& p) {
+        const float ax = acc[0];
+        axn[r] = ax;
+        float y2 = p.yv + sigma * (p.br - (ax + ax - p.ao));
+        if (p.kd) y2 = fminf(y2, 0.f);
+        yn[r] = y2;
+        const float dy = y2 - p.yv;
+        dy2 += dy * dy;
+        inter += dy * (ax - p.ao);
+    }
+};
+
+// column pass of an accepted attempt: K^T y', averages, next candidate
+struct ColStepE {
+    const float *xc, *c, *lo, *hi;
+    float *aty, *xn, *xs;
+    float tau, wgt;
+    float dx2 = 0.f;
+    struct Pre { float xj, cj, l, h, s; };
+    __device__ __forceinline__ Pre pre(int j) const { return Pre{xc[j], c[j], lo[j], hi[j], xs[j]}; }
+    __device__ __forceinline__ void operator()(int j, const float (&acc)[1], const Pre& p) {
+        aty[j] = acc[0];
+        xs[j] = p.s + wgt * p.xj;
+        const float x2 = fminf(fmaxf(p.xj - tau * (p.cj - acc[0]), p.l), p.h);
+        xn[j] = x2;
+        const float d = x2 - p.xj;
+        dx2 += d * d;
+    }
+};
+
+struct RowCheckE {
+    const float *b, *ys, *yc, *yl;
+    const double* dr;
+    const int8_t* kind;
+    float* axa;
+    double inv_w;
+    double p[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    struct Pre {};
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int r, const double (&acc)[2], const Pre&) {
+        const double br = b[r], d = dr[r];
+        axa[r] = float(acc[0]);
+        for (int q = 0; q < 2; ++q) {
+            double res = acc[q] - br;
+            if (kind[r]) res = fmax(res, 0.0);
+            p[4 * q + 0] += res * res;
+            p[4 * q + 1] += (res / d) * (res / d);
+            const double yv = q == 0 ? double(ys[r]) * inv_w : double(yc[r]);
+            p[4 * q + 2] += br * yv;
+            const double dd = yv - double(yl[r]);
+            p[4 * q + 3] += dd * dd;
+        }
+    }
+};
+
+struct ColCheckE {
+    const float *c, *lo, *hi, *xs, *xc, *xl;
+    const double* dc;
+    float* atya;
+    double inv_w;
+    double p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    struct Pre {};
+    __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
+    __device__ __forceinline__ void operator()(int j, const double (&acc)[2], const Pre&) {
+        const double cj = c[j], d = dc[j], l = lo[j], h = hi[j];
+        const bool hl = isfinite(l), hh = isfinite(h);
+        atya[j] = float(acc[0]);
+        for (int q = 0; q < 2; ++q) {
+            const double rc = cj - acc[q];
+            const double lam = (hl && hh) ? rc : hl ? fmax(rc, 0.0) : hh ? fmin(rc, 0.0) : 0.0;
+            const double dres = rc - lam;
+            p[5 * q + 0] += dres * dres;
+            p[5 * q + 1] += (dres / d) * (dres / d);
+            const double xv = q == 0 ? double(xs[j]) * inv_w : double(xc[j]);
+            p[5 * q + 2] += cj * xv;
+            p[5 * q + 3] += (hl ? l * fmax(lam, 0.0) : 0.0) + (hh ? h * fmin(lam, 0.0) : 0.0);
+            const double dd = xv - double(xl[j]);
+            p[5 * q + 4] += dd * dd;
+        }
+    }
+};
+
+struct View {                 // one instance's arrays
+    int n, m, G;
+    const int32_t *rptr, *ridx, *cptr, *cidx;
+    const float *rval, *cval;
+    const int8_t* kind;
+    const float *c, *lo, *hi, *b;
+    const double *dc, *dr;
+    float *X[2], *ATY[2], *xs, *xl, *atya;
+    float *Y[2], *AX[2], *ys, *yl, *axa;
+};
+
+__device__ __forceinline__ View make_view(const Args& A, const Inst& I, int G) {
+    const Arrays& a = A.a;
+    View v;
+    v.n = I.n; v.m = I.m; v.G = G;
+    v.rptr = a.rptr + I.rp; v.ridx = a.ridx + I.re; v.rval = a.rval + I.re;
+    v.cptr = a.cptr + I.cp; v.cidx = a.cidx + I.ce; v.cval = a.cval + I.ce;
+    v.kind = a.kind + I.vr;
+    v.c = a.c + I.vc; v.lo = a.lo + I.vc; v.hi = a.hi + I.vc; v.b = a.b + I.vr;
+    v.dc = a.dc + I.vc; v.dr = a.dr + I.vr;
+    v.X[0] = a.x0 + I.vc; v.X[1] = a.x1 + I.vc; v.ATY[0] = a.aty0 + I.vc; v.ATY[1] = a.aty1 + I.vc;
+    v.xs = a.xs + I.vc; v.xl = a.xl + I.vc; v.atya = a.atya + I.vc;
+    v.Y[0] = a.y0 + I.vr; v.Y[1] = a.y1 + I.vr; v.AX[0] = a.ax0 + I.vr; v.AX[1] = a.ax1 + I.vr;
+    v.ys = a.ys + I.vr; v.yl = a.yl + I.vr; v.axa = a.axa + I.vr;
+    return v;
+}
+
+// KKT check of average and current point, decision, and the restart copies.
+__device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm, const uint64_t* dl) {
+    const uint64_t deadline = *dl;
+    const bool has_avg = c.w_sum > 0.0;
+    const double inv_w = has_avg ? 1.0 / c.w_sum : 1.0;
+    const int cur = c.cur;
+    RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w};
+    group_rows<32, 2, double>(v.rptr, v.ridx, v.rval, v.m, Gather2{has_avg ? v.xs : v.X[cur], v.X[cur], inv_w}, er);
+    block_sum<8>(er.p, sm);
+    ColCheckE ec{v.c, v.lo, v.hi, has_avg ? v.xs : v.X[cur], v.X[cur], v.xl, v.dc, v.atya, inv_w};
+    group_rows_dyn<2, double>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather2{has_avg ? v.ys : v.Y[cur], v.Y[cur], inv_w}, ec);
+    block_sum<10>(ec.p, sm);
+    if (threadIdx.x == 0) {
+        const bool stop = deadline && global_ns() > deadline;
+        decide_check(c, ec.p, er.p, I.inv_nb, I.inv_nc, stop);
+    }
+    __syncthreads();
+    const int ap = c.apply;
+    if (ap == 0) return;
+    const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !c.done;
+    const double iw = c.w_sum > 0.0 ? 1.0 / c.w_sum : 0.0;
+    const float tau = float(c.eta / c.omega);
+    float dx2 = 0.f;
+    for (int j = threadIdx.x; j < v.n; j += kBlock) {
+        float xv;
+        if (load) {
+            xv = float(double(v.xs[j]) * iw);
+            v.X[cur][j] = xv;
+            v.ATY[cur][j] = v.atya[j];
+        } else {
+            xv = v.X[cur][j];
+        }
+        if (rst) { v.xl[j] = xv; v.xs[j] = 0.f; }
+        if (cand) {
+            const float x2 = fminf(fmaxf(xv - tau * (v.c[j] - v.ATY[cur][j]), v.lo[j]), v.hi[j]);
+            v.X[1 - cur][j] = x2;
+            dx2 += (x2 - xv) * (x2 - xv);
+        }
+    }
+    for (int i = threadIdx.x; i < v.m; i += kBlock) {
+        float yv;
+        if (load) {
+            yv = float(double(v.ys[i]) * iw);
+            v.Y[cur][i] = yv;
+            v.AX[cur][i] = v.axa[i];
+        } else {
+            yv = v.Y[cur][i];
+        }
+        if (rst) { v.yl[i] = yv; v.ys[i] = 0.f; }
+    }
+    double t[1] = {double(dx2)};
+    block_sum<1>(t, sm);
+    if (threadIdx.x == 0) {
+        if (cand) c.dx2 = t[0];
+        if (rst) c.w_sum = 0.0;
+        c.apply = 0;
+    }
+    __syncthreads();
+}
+
+__device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
+    const Inst I = A.inst[k];
+    const View v = make_view(A, I, G);
+    if (threadIdx.x == 0) {
+        c = Ctl{};
+        c.status = SPS_STATUS_ITERATION_LIMIT;
+        c.init_phase = 1;
+        c.max_iters = A.max_iters;
+        c.tol = A.tol;
+        c.eta = A.a.eta0[k];
+        c.omega = A.a.omega0[k];
+        c.kkt_last = INFINITY;
+    }
+    for (int j = threadIdx.x; j < v.n; j += kBlock) {
+        const float x = fminf(fmaxf(0.f, v.lo[j]), v.hi[j]);
+        v.X[0][j] = x;
+        v.xl[j] = x;
+        v.xs[j] = 0.f;
+        v.ATY[0][j] = 0.f;                      // K^T y0 with y0 = 0
+    }
+    for (int i = threadIdx.x; i < v.m; i += kBlock) { v.Y[0][i] = 0.f; v.yl[i] = 0.f; v.ys[i] = 0.f; }
+    __syncthreads();
+    StoreE st{v.AX[0]};
+    group_rows<32, 1, float>(v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[0]}, st);
+    __syncthreads();
+    check_and_apply(v, I, c, sm, A.deadline);
+    for (;;) {
+        for (int w = 0; w < A.check_interval; ++w) {
+            if (c.done || c.iters >= c.max_iters) break;
+            int cur = c.cur;
+            RowStepE er{v.b, v.AX[cur], v.Y[cur], v.kind, v.AX[1 - cur], v.Y[1 - cur], float(c.eta * c.omega)};
+            group_rows<32, 1, float>(v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur]}, er);
+            double t2[2] = {double(er.dy2), double(er.inter)};
+            block_sum<2>(t2, sm);
+            if (threadIdx.x == 0) decide_step(c, t2[0], t2[1]);
+            __syncthreads();
+            if (c.done) break;
+            cur = c.cur;
+            const float tau = float(c.eta / c.omega), wgt = float(c.eta_used);
+            float dx2;
+            if (c.accepted) {
+                ColStepE ec{v.X[cur], v.c, v.lo, v.hi, v.ATY[cur], v.X[1 - cur], v.xs, tau, wgt};
+                group_rows_dyn<1, float>(G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur]}, ec);
+                dx2 = ec.dx2;
+                for (int i = threadIdx.x; i < v.m; i += kBlock) v.ys[i] += wgt * v.Y[cur][i];
+            } else {
+                dx2 = 0.f;
+                for (int j = threadIdx.x; j < v.n; j += kBlock) {
+                    const float xj = v.X[cur][j];
+                    const float x2 = fminf(fmaxf(xj - tau * (v.c[j] - v.ATY[cur][j]), v.lo[j]), v.hi[j]);
+                    v.X[1 - cur][j] = x2;
+                    dx2 += (x2 - xj) * (x2 - xj);
+                }
+            }
+            double t1[1] = {double(dx2)};
+            block_sum<1>(t1, sm);
+            if (threadIdx.x == 0) { c.dx2 = t1[0]; c.apply = 0; }
+            __syncthreads();
+        }
+        if (c.done) break;
+        check_and_apply(v, I, c, sm, A.deadline);
+        if (c.done) break;
+    }
+    if (threadIdx.x == 0) A.out[k] = c;
+}
+
+__global__ void __launch_bounds__(kBlock) k_batch_solve(Args A, int G) {
+    __shared__ Ctl c;
+    __shared__ double sm[kWarps * 10];
+    __shared__ int s_inst;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t q = atomicAdd(A.counter, 1u);
+            s_inst = q < (uint32_t)A.count ? A.order[q] : -1;
+        }
+        __syncthreads();
+        const int k = s_inst;
+        if (k < 0) return;
+        solve_one(A, k, G, c, sm);
+        __syncthreads();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Per-instance scaling, one block per instance.
+struct SetupArgs {
+    const Inst* inst;
+    const int32_t *rptr, *ridx, *cptr, *cidx;
+    const double *rv64, *cv64;            // original values
+    const double *c64, *lo64, *hi64, *b64;
+    double *dr, *dc;
+    float *rmax, *cmax;                   // scratch (per row / per column)
+    float *rval, *cval, *c, *lo, *hi, *b;
+    double *eta0, *omega0;
+    int32_t ruiz;
+};
+
+// per row (warp each): stat = d_own[r] * max|v d_other| (or the sum)
+__device__ void row_stat(const int32_t* ptr, const int32_t* idx, const double* v, const double* d_own,
+                         const double* d_other, int rows, bool sum, float* out) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r < rows; r += kWarps) {
+        double a = 0.0;
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) {
+            const double t = fabs(v[k] * d_other[idx[k]]);
+            a = sum ? a + t : fmax(a, t);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double u = __shfl_xor_sync(0xffffffffu, a, o);
+            a = sum ? a + u : fmax(a, u);
+        }
+        if (lane == 0) out[r] = float(a * d_own[r]);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_batch_setup(SetupArgs S) {
+    const int k = blockIdx.x;
+    const Inst I = S.inst[k];
+    const int32_t *rptr = S.rptr + I.rp, *ridx = S.ridx + I.re, *cptr = S.cptr + I.cp, *cidx = S.cidx + I.ce;
+    const double *rv = S.rv64 + I.re, *cv = S.cv64 + I.ce;
+    double *dr = S.dr + I.vr, *dc = S.dc + I.vc;
+    float *rm = S.rmax + I.vr, *cm = S.cmax + I.vc;
+    for (int j = threadIdx.x; j < I.n; j += kBlock) dc[j] = 1.0;
+    for (int i = threadIdx.x; i < I.m; i += kBlock) dr[i] = 1.0;
+    __syncthreads();
+    for (int it = 0; it <= S.ruiz; ++it) {
+        const bool pc = it == S.ruiz;           // last pass: Pock-Chambolle (sums), before it Ruiz (max)
+        row_stat(rptr, ridx, rv, dr, dc, I.m, pc, rm);
+        row_stat(cptr, cidx, cv, dc, dr, I.n, pc, cm);
+        __syncthreads();
+        for (int i = threadIdx.x; i < I.m; i += kBlock)
+            if (rm[i] > 0.f) dr[i] /= sqrt(double(rm[i]));
+        for (int j = threadIdx.x; j < I.n; j += kBlock)
+            if (cm[j] > 0.f) dc[j] /= sqrt(double(cm[j]));
+        __syncthreads();
+    }
+    double mx = 0.0, sc = 0.0, sb = 0.0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int r = warp; r < I.m; r += kWarps)
+        for (int q = rptr[r] + lane; q < rptr[r + 1]; q += 32) {
+            const float v = float(rv[q] * dr[r] * dc[ridx[q]]);
+            S.rval[I.re + q] = v;
+            mx = fmax(mx, fabs(double(v)));
+        }
+    for (int j = warp; j < I.n; j += kWarps)
+        for (int q = cptr[j] + lane; q < cptr[j + 1]; q += 32) S.cval[I.ce + q] = float(cv[q] * dc[j] * dr[cidx[q]]);
+    for (int j = threadIdx.x; j < I.n; j += kBlock) {
+        const double cs = S.c64[I.vc + j] * dc[j];
+        S.c[I.vc + j] = float(cs);
+        S.lo[I.vc + j] = float(S.lo64[I.vc + j] / dc[j]);
+        S.hi[I.vc + j] = float(S.hi64[I.vc + j] / dc[j]);
+        sc += cs * cs;
+    }
+    for (int i = threadIdx.x; i < I.m; i += kBlock) {
+        const double bs = S.b64[I.vr + i] * dr[i];
+        S.b[I.vr + i] = float(bs);
+        sb += bs * bs;
+    }
+    __shared__ double sm[kWarps * 3];
+    __shared__ double smx[kWarps];
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (lane == 0) smx[warp] = mx;
+    double s2[2] = {sc, sb};
+    block_sum<2>(s2, sm);
+    if (threadIdx.x == 0) {
+        for (int w = 1; w < kWarps; ++w) mx = fmax(mx, smx[w]);
+        mx = fmax(mx, smx[0]);
+        S.eta0[k] = mx > 0.0 ? 1.0 / mx : 1.0;
+        S.omega0[k] = (s2[0] > 1e-20 && s2[1] > 1e-20) ? sqrt(s2[0]) / sqrt(s2[1]) : 1.0;
+    }
+}
+
+// Absolute device deadline of a batched solve (0 = none), set at the start of
+// the solve so a replayed graph measures the limit from its own launch.
+__global__ void k_set_deadline(uint64_t* dl, uint64_t limit_ns) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *dl = limit_ns ? global_ns() + limit_ns : 0;
+}
+
+// Unscaled solution of every instance (one block per instance), FP64.
+__global__ void __launch_bounds__(kBlock) k_batch_extract(const Inst* inst, const Ctl* out, Arrays a, double* xo,
+                                                          double* yo) {
+    const int k = blockIdx.x;
+    const Inst I = inst[k];
+    const int cur = out[k].cur;
+    const float* X = (cur ? a.x1 : a.x0) + I.vc;
+    const float* Y = (cur ? a.y1 : a.y0) + I.vr;
+    for (int j = threadIdx.x; j < I.n; j += kBlock) xo[I.vc + j] = double(X[j]) * a.dc[I.vc + j];
+    for (int i = threadIdx.x; i < I.m; i += kBlock) yo[I.vr + i] = double(Y[i]) * a.dr[I.vr + i];
+}
+
+}  // namespace batch
+}  // namespace sps
+
+// ===========================================================================
+// Host side
+// ===========================================================================
+using sps::Ctl;
+using sps::batch::Inst;
+
+struct sps_batch {
+    int32_t count = 0;
+    sps_options opt{};
+    int32_t G = 8, blocks = 0;
+    cudaStream_t st = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    std::vector<Inst> inst;
+    std::vector<int32_t> order;
+    std::vector<void*> dev;                 // device allocations
+    Inst* d_inst = nullptr;
+    int32_t* d_order = nullptr;
+    Ctl* d_out = nullptr;
+    uint32_t* d_counter = nullptr;
+    double *d_xo = nullptr, *d_yo = nullptr;
+    sps::batch::Arrays arr{};
+    int64_t sum_n = 0, sum_m = 0;
+    std::vector<double> c_all, lb_all, ub_all;   // original data, packed like the column vectors
+    std::vector<double> xo, yo;
+    std::vector<Ctl> out;
+    cudaGraphExec_t gexec = nullptr;
+    int32_t gexec_G = -1;
+    uint64_t gexec_tl = 0;
+    uint64_t* d_deadline = nullptr;
+    double setup_ms = 0.0, solve_ms = 0.0;
+    bool solved = false;
+    std::string err;
+
+    ~sps_batch() {
+        if (gexec) cudaGraphExecDestroy(gexec);
+        for (void* p : dev) cudaFree(p);
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (st) cudaStreamDestroy(st);
+    }
+    template <class T>
+    cudaError_t alloc(T** p, size_t count_) {
+        void* q = nullptr;
+        const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count_, 1) * sizeof(T));
+        if (e == cudaSuccess) dev.push_back(q);
+        *p = static_cast<T*>(q);
+        return e;
+    }
+    int fail(int code, const std::string& m) {
+        err = m;
+        return code;
+    }
+};
+
+namespace {
+
+#define SPB_CK(call)                                                                           \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return b->fail(e_ == cudaErrorMemoryAllocation ? SPS_ERR_OOM : SPS_ERR_CUDA,        \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+// Host validation of one instance; also sizes.
+bool check_instance(const sps_problem_desc& d, std::string& why) {
+    if (d.n < 0 || d.m_ub < 0 || d.m_eq < 0) { why = "negative dimension"; return false; }
+    auto csr_ok = [&](const int32_t* p, const int32_t* ix, const double* v, int32_t rows) {
+        if (rows == 0) return true;
+        if (!p || p[0] != 0) return false;
+        for (int32_t i = 0; i < rows; ++i)
+            if (p[i + 1] < p[i]) return false;
+        return p[rows] == 0 || (ix && v);
+    };
+    if (!csr_ok(d.ub_indptr, d.ub_indices, d.ub_values, d.m_ub) || !csr_ok(d.eq_indptr, d.eq_indices, d.eq_values, d.m_eq)) {
+        why = "malformed CSR";
+        return false;
+    }
+    if (d.n > 0 && (!d.c || !d.lb || !d.ub)) { why = "null c/lb/ub"; return false; }
+    if ((d.m_ub && !d.b_ub) || (d.m_eq && !d.b_eq)) { why = "null rhs"; return false; }
+    for (int32_t j = 0; j < d.n; ++j) {
+        const double l = d.lb[j], u = d.ub[j];
+        if (!std::isfinite(d.c[j]) || std::isnan(l) || std::isnan(u) || l == INFINITY || u == -INFINITY || l > u + 1e-12) {
+            why = "invalid objective or bounds at variable " + std::to_string(j);
+            return false;
+        }
+    }
+    for (int32_t i = 0; i < d.m_ub; ++i)
+        if (!std::isfinite(d.b_ub[i])) { why = "non-finite right-hand side"; return false; }
+    for (int32_t i = 0; i < d.m_eq; ++i)
+        if (!std::isfinite(d.b_eq[i])) { why = "non-finite right-hand side"; return false; }
+    return true;
+}
+
+}  // namespace
+
+extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, const sps_options* opt_in,
+                                sps_batch** out) {
+    if (!out || count <= 0 || !probs) {
+        sps::set_create_error("sps_batch_create: need count > 0, problems and an output pointer");
+        return SPS_ERR_INVALID;
+    }
+    *out = nullptr;
+    sps_options opt;
+    if (opt_in) opt = *opt_in; else sps_options_init(&opt);
+    if (opt.mode != SPS_MODE_ADAPTIVE || opt.precision != SPS_FP32) {
+        sps::set_create_error("sps_batch_create: the batched solver runs the adaptive mode with FP32 iterates");
+        return SPS_ERR_INVALID;
+    }
+    auto b = std::make_unique<sps_batch>();
+    b->count = count;
+    b->opt = opt;
+    // ---- sizes and validation
+    b->inst.resize(count);
+    int64_t rp = 0, re = 0, cp = 0, vc = 0, vr = 0;
+    for (int32_t k = 0; k < count; ++k) {
+        std::string why;
+        if (!check_instance(probs[k], why)) {
+            sps::set_create_error("instance " + std::to_string(k) + ": " + why);
+            return SPS_ERR_INVALID;
+        }
+        const sps_problem_desc& d = probs[k];
+        Inst& I = b->inst[k];
+        I.n = d.n;
+        I.m = d.m_ub + d.m_eq;
+        I.m_ub = d.m_ub;
+        const int64_t nz = (int64_t)(d.m_ub ? d.ub_indptr[d.m_ub] : 0) + (d.m_eq ? d.eq_indptr[d.m_eq] : 0);
+        I.rp = rp; I.re = re; I.cp = cp; I.ce = re; I.vc = vc; I.vr = vr;
+        rp += I.m + 1; cp += I.n + 1; re += nz; vc += I.n; vr += I.m;
+    }
+    if (re > INT32_MAX) {
+        sps::set_create_error("sps_batch_create: a batch holds at most 2^31-1 nonzeros in total");
+        return SPS_ERR_INVALID;
+    }
+    const int64_t NNZ = re;
+    b->sum_n = vc;
+    b->sum_m = vr;
+    // ---- host packing (CSR of [A_ub; A_eq] and a CSC by counting sort), spread over host threads
+    std::vector<int32_t> rptr(rp), ridx(NNZ), cptr(cp), cidx(NNZ);
+    std::vector<double> rv(NNZ), cv(NNZ), c64(vc), lo64(vc), hi64(vc), b64(vr);
+    std::vector<int8_t> kind(vr);
+    std::vector<std::string> errs(count);
+    auto pack = [&](int32_t k) {
+        const sps_problem_desc& d = probs[k];
+        Inst& I = b->inst[k];
+        int32_t* P = rptr.data() + I.rp;
+        int64_t q = 0;
+        P[0] = 0;
+        for (int part = 0; part < 2; ++part) {
+            const int32_t rows = part ? d.m_eq : d.m_ub;
+            const int32_t* ip = part ? d.eq_indptr : d.ub_indptr;
+            const int32_t* ix = part ? d.eq_indices : d.ub_indices;
+            const double* v = part ? d.eq_values : d.ub_values;
+            for (int32_t i = 0; i < rows; ++i) {
+                for (int32_t t = ip[i]; t < ip[i + 1]; ++t) {
+                    const int32_t j = ix[t];
+                    if (j < 0 || j >= d.n) { errs[k] = "column index out of range"; return; }
+                    if (!std::isfinite(v[t])) { errs[k] = "non-finite matrix value"; return; }
+                    ridx[I.re + q] = j;
+                    rv[I.re + q] = v[t];
+                    ++q;
+                }
+                const int32_t r = part ? d.m_ub + i : i;
+                P[r + 1] = (int32_t)q;
+                kind[I.vr + r] = part ? 0 : 1;
+                b64[I.vr + r] = part ? d.b_eq[i] : d.b_ub[i];
+            }
+        }
+        int32_t* C = cptr.data() + I.cp;
+        std::fill(C, C + I.n + 1, 0);
+        for (int64_t t = 0; t < q; ++t) C[ridx[I.re + t] + 1]++;
+        for (int32_t j = 0; j < I.n; ++j) C[j + 1] += C[j];
+        std::vector<int32_t> fill(C, C + I.n);
+        for (int32_t r = 0; r < I.m; ++r)
+            for (int32_t t = P[r]; t < P[r + 1]; ++t) {
+                const int32_t j = ridx[I.re + t];
+                const int32_t pos = fill[j]++;
+                cidx[I.ce + pos] = r;
+                cv[I.ce + pos] = rv[I.re + t];
+            }
+        for (int32_t j = 0; j < I.n; ++j) {
+            c64[I.vc + j] = d.c[j];
+            lo64[I.vc + j] = d.lb[j];
+            hi64[I.vc + j] = d.ub[j];
+        }
+        double nb = 0, nc = 0;
+        for (int32_t r = 0; r < I.m; ++r) nb += b64[I.vr + r] * b64[I.vr + r];
+        for (int32_t j = 0; j < I.n; ++j) nc += d.c[j] * d.c[j];
+        I.inv_nb = 1.0 / (1.0 + std::sqrt(nb));
+        I.inv_nc = 1.0 / (1.0 + std::sqrt(nc));
+    };
+    {
+        const int nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+        std::vector<std::thread> pool;
+        std::atomic<int32_t> next{0};
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back([&]() {
+                for (int32_t k; (k = next.fetch_add(1)) < count;) pack(k);
+            });
+        for (auto& th : pool) th.join();
+    }
+    for (int32_t k = 0; k < count; ++k)
+        if (!errs[k].empty()) {
+            sps::set_create_error("instance " + std::to_string(k) + ": " + errs[k]);
+            return SPS_ERR_INVALID;
+        }
+    b->c_all = c64;
+    b->lb_all = lo64;
+    b->ub_all = hi64;
+    // hand-out order: largest instances (nonzeros + rows + columns) first
+    std::vector<int64_t> work(count);
+    for (int32_t k = 0; k < count; ++k)
+        work[k] = ((k + 1 < count ? b->inst[k + 1].re : NNZ) - b->inst[k].re) + b->inst[k].m + b->inst[k].n;
+    b->order.resize(count);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int32_t a, int32_t c) { return work[a] > work[c]; });
+
+    // ---- device
+    sps_batch* bp = b.get();
+    {
+        sps_batch* b = bp;
+        SPB_CK(cudaSetDevice(opt.device));
+        SPB_CK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+        SPB_CK(cudaEventCreate(&b->e0));
+        SPB_CK(cudaEventCreate(&b->e1));
+        SPB_CK(cudaEventRecord(b->e0, b->st));
+        sps::batch::Arrays& a = b->arr;
+        int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx;
+        float *d_rval, *d_cval, *d_c, *d_lo, *d_hi, *d_b;
+        int8_t* d_kind;
+        double *d_dr, *d_dc, *d_eta0, *d_om0;
+        SPB_CK(b->alloc(&d_rptr, rp)); SPB_CK(b->alloc(&d_ridx, NNZ));
+        SPB_CK(b->alloc(&d_cptr, cp)); SPB_CK(b->alloc(&d_cidx, NNZ));
+        SPB_CK(b->alloc(&d_rval, NNZ)); SPB_CK(b->alloc(&d_cval, NNZ));
+        SPB_CK(b->alloc(&d_c, vc)); SPB_CK(b->alloc(&d_lo, vc)); SPB_CK(b->alloc(&d_hi, vc));
+        SPB_CK(b->alloc(&d_b, vr)); SPB_CK(b->alloc(&d_kind, vr));
+        SPB_CK(b->alloc(&d_dr, vr)); SPB_CK(b->alloc(&d_dc, vc));
+        SPB_CK(b->alloc(&d_eta0, count)); SPB_CK(b->alloc(&d_om0, count));
+        float* st_f[14];
+        for (int q = 0; q < 7; ++q) SPB_CK(b->alloc(&st_f[q], vc));
+        for (int q = 7; q < 14; ++q) SPB_CK(b->alloc(&st_f[q], vr));
+        SPB_CK(b->alloc(&b->d_inst, count));
+        SPB_CK(b->alloc(&b->d_order, count));
+        SPB_CK(b->alloc(&b->d_out, count));
+        SPB_CK(b->alloc(&b->d_counter, 1));
+        SPB_CK(b->alloc(&b->d_deadline, 1));
+        SPB_CK(cudaMemsetAsync(b->d_deadline, 0, sizeof(uint64_t), b->st));
+        SPB_CK(b->alloc(&b->d_xo, vc));
+        SPB_CK(b->alloc(&b->d_yo, vr));
+        double *t_rv, *t_cv, *t_c, *t_lo, *t_hi, *t_b;
+        SPB_CK(cudaMalloc(&t_rv, sizeof(double) * std::max<int64_t>(NNZ, 1)));
+        SPB_CK(cudaMalloc(&t_cv, sizeof(double) * std::max<int64_t>(NNZ, 1)));
+        SPB_CK(cudaMalloc(&t_c, sizeof(double) * (3 * (size_t)vc + vr + 1)));
+        t_lo = t_c + vc; t_hi = t_lo + vc; t_b = t_hi + vc;
+        auto up = [&](void* dst, const void* src, size_t bytes) {
+            return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, b->st) : cudaSuccess;
+        };
+        SPB_CK(up(d_rptr, rptr.data(), 4 * rp)); SPB_CK(up(d_ridx, ridx.data(), 4 * NNZ));
+        SPB_CK(up(d_cptr, cptr.data(), 4 * cp)); SPB_CK(up(d_cidx, cidx.data(), 4 * NNZ));
+        SPB_CK(up(t_rv, rv.data(), 8 * NNZ)); SPB_CK(up(t_cv, cv.data(), 8 * NNZ));
+        SPB_CK(up(t_c, c64.data(), 8 * vc)); SPB_CK(up(t_lo, lo64.data(), 8 * vc));
+        SPB_CK(up(t_hi, hi64.data(), 8 * vc)); SPB_CK(up(t_b, b64.data(), 8 * vr));
+        SPB_CK(up(d_kind, kind.data(), vr));
+        SPB_CK(up(b->d_inst, b->inst.data(), sizeof(Inst) * count));
+        SPB_CK(up(b->d_order, b->order.data(), 4 * (size_t)count));
+        sps::batch::SetupArgs S{b->d_inst, d_rptr, d_ridx, d_cptr, d_cidx, t_rv, t_cv, t_c, t_lo, t_hi, t_b,
+                                d_dr, d_dc, /*row stats*/ st_f[7], /*column stats*/ st_f[0], d_rval, d_cval, d_c,
+                                d_lo, d_hi, d_b, d_eta0, d_om0,
+                                opt.ruiz_iters >= 0 ? opt.ruiz_iters : 10};
+        sps::batch::k_batch_setup<<<count, sps::kBlock, 0, b->st>>>(S);
+        SPB_CK(cudaGetLastError());
+        SPB_CK(cudaStreamSynchronize(b->st));
+        cudaFree(t_rv); cudaFree(t_cv); cudaFree(t_c);
+        a = sps::batch::Arrays{d_rptr, d_ridx, d_cptr, d_cidx, d_rval, d_cval, d_kind, d_c, d_lo, d_hi, d_b,
+                               d_dc, d_dr, d_eta0, d_om0,
+                               st_f[0], st_f[1], st_f[2], st_f[3], st_f[4], st_f[5], st_f[6],
+                               st_f[7], st_f[8], st_f[9], st_f[10], st_f[11], st_f[12], st_f[13]};
+        int nb = 0, dev = opt.device, sms = 152;
+        SPB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sps::batch::k_batch_solve, sps::kBlock, 0));
+        SPB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        b->blocks = std::max(1, std::min(count, nb * sms));
+        SPB_CK(cudaEventRecord(b->e1, b->st));
+        SPB_CK(cudaStreamSynchronize(b->st));
+        float ms = 0;
+        cudaEventElapsedTime(&ms, b->e0, b->e1);
+        b->setup_ms = ms;
+    }
+    // ---- lanes per column: given, or timed on a sample of the batch
+    if (opt.batch_group == 4 || opt.batch_group == 8 || opt.batch_group == 16 || opt.batch_group == 32) {
+        b->G = opt.batch_group;
+    } else {
+        sps_batch* bb = bp;
+        const int32_t sample = std::min<int32_t>(count, 2 * bb->blocks);
+        double best = 1e300;
+        for (int G : {4, 8, 16, 32}) {
+            sps::batch::Args A{bb->d_inst, bb->d_order, sample, 64, 128, 0.0, bb->d_deadline, bb->arr, bb->d_out,
+                               bb->d_counter};
+            cudaMemsetAsync(bb->d_counter, 0, sizeof(uint32_t), bb->st);
+            cudaEventRecord(bb->e0, bb->st);
+            sps::batch::k_batch_solve<<<std::min(bb->blocks, sample), sps::kBlock, 0, bb->st>>>(A, G);
+            cudaEventRecord(bb->e1, bb->st);
+            if (cudaStreamSynchronize(bb->st) != cudaSuccess) {
+                sps::set_create_error(std::string("autotune: ") + cudaGetErrorString(cudaGetLastError()));
+                return SPS_ERR_CUDA;
+            }
+            float ms = 0;
+            cudaEventElapsedTime(&ms, bb->e0, bb->e1);
+            if (ms < best) { best = ms; bb->G = G; }
+        }
+    }
+    *out = b.release();
+    return SPS_OK;
+}
+
+extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
+    if (!b) return SPS_ERR_INVALID;
+    SPB_CK(cudaSetDevice(b->opt.device));
+    const int64_t W = b->opt.check_interval > 0 ? b->opt.check_interval : 64;
+    const uint64_t tl = b->opt.time_limit_s > 0 ? (uint64_t)(b->opt.time_limit_s * 1e9) : 0;
+    sps::batch::Args A{b->d_inst, b->d_order, b->count, (int32_t)W, b->opt.max_iters, b->opt.tol, b->d_deadline,
+                       b->arr, b->d_out, b->d_counter};
+    auto enqueue = [&](cudaStream_t s) {
+        cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
+        sps::batch::k_set_deadline<<<1, 32, 0, s>>>(b->d_deadline, tl);
+        sps::batch::k_batch_solve<<<b->blocks, sps::kBlock, 0, s>>>(A, b->G);
+    };
+    SPB_CK(cudaEventRecord(b->e0, b->st));
+    if (b->opt.graph_mode != 0) {
+        // one graph (counter reset, deadline, persistent solve), built once per
+        // schedule and time limit and replayed by later solves
+        if (!b->gexec || b->gexec_G != b->G || b->gexec_tl != tl) {
+            if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
+            cudaGraph_t g;
+            cudaStream_t cap;
+            SPB_CK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+            cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+            if (e == cudaSuccess) {
+                enqueue(cap);
+                e = cudaStreamEndCapture(cap, &g);
+            }
+            if (e == cudaSuccess) {
+                e = cudaGraphInstantiate(&b->gexec, g, 0);
+                cudaGraphDestroy(g);
+            }
+            cudaStreamDestroy(cap);
+            SPB_CK(e);
+            b->gexec_G = b->G;
+            b->gexec_tl = tl;
+        }
+        SPB_CK(cudaGraphLaunch(b->gexec, b->st));
+    } else {
+        enqueue(b->st);
+        SPB_CK(cudaGetLastError());
+    }
+    SPB_CK(cudaEventRecord(b->e1, b->st));
+    sps::batch::k_batch_extract<<<b->count, sps::kBlock, 0, b->st>>>(b->d_inst, b->d_out, b->arr, b->d_xo, b->d_yo);
+    SPB_CK(cudaGetLastError());
+    b->out.resize(b->count);
+    b->xo.resize(b->sum_n);
+    b->yo.resize(b->sum_m);
+    SPB_CK(cudaMemcpyAsync(b->out.data(), b->d_out, sizeof(Ctl) * b->count, cudaMemcpyDeviceToHost, b->st));
+    SPB_CK(cudaMemcpyAsync(b->xo.data(), b->d_xo, sizeof(double) * b->sum_n, cudaMemcpyDeviceToHost, b->st));
+    SPB_CK(cudaMemcpyAsync(b->yo.data(), b->d_yo, sizeof(double) * b->sum_m, cudaMemcpyDeviceToHost, b->st));
+    SPB_CK(cudaStreamSynchronize(b->st));
+    float ms = 0;
+    cudaEventElapsedTime(&ms, b->e0, b->e1);
+    b->solve_ms = ms;
+    b->solved = true;
+    if (stats) {
+        std::memset(stats, 0, sizeof(*stats));
+        stats->setup_ms = b->setup_ms;
+        stats->solve_ms = ms;
+        stats->lanes_per_column = b->G;
+        stats->blocks = b->blocks;
+        for (const Ctl& c : b->out) {
+            stats->total_iterations += c.iters;
+            if (c.status == SPS_STATUS_OPTIMAL) stats->optimal += 1;
+        }
+    }
+    return SPS_OK;
+}
+
+extern "C" int sps_batch_get(sps_batch* b, int32_t k, double* x, double* y, sps_result* res) {
+    if (!b || k < 0 || k >= b->count) return SPS_ERR_INVALID;
+    if (!b->solved) return b->fail(SPS_ERR_STATE, "call sps_batch_solve first");
+    const Inst& I = b->inst[k];
+    const Ctl& c = b->out[k];
+    double obj = 0.0;
+    for (int32_t j = 0; j < I.n; ++j) {
+        const double lo = std::isfinite(b->lb_all[I.vc + j]) ? b->lb_all[I.vc + j] : -1e30;
+        const double hi = std::isfinite(b->ub_all[I.vc + j]) ? b->ub_all[I.vc + j] : 1e30;
+        const double v = std::min(std::max(b->xo[I.vc + j], lo), hi);
+        if (x) x[j] = v;
+        obj += b->c_all[I.vc + j] * v;
+    }
+    if (y) std::memcpy(y, b->yo.data() + I.vr, sizeof(double) * I.m);
+    if (res) {
+        std::memset(res, 0, sizeof(*res));
+        res->status = c.status;
+        res->restarts = c.restarts;
+        res->iterations = c.iters;
+        res->accepted_steps = c.accepted_total;
+        res->objective = obj;
+        res->rel_kkt = c.rel_kkt;
+        res->rel_primal = c.rel_p;
+        res->rel_dual = c.rel_d;
+        res->rel_gap = c.rel_gap;
+        res->primal_weight = c.omega;
+        res->step_size = c.eta;
+        res->setup_ms = b->setup_ms;
+        res->solve_ms = b->solve_ms;
+        res->kernel_launches = 1;
+        res->returned_average = c.choice;
+    }
+    return SPS_OK;
+}
+
+extern "C" const char* sps_batch_last_error(const sps_batch* b) { return b ? b->err.c_str() : ""; }
+
+extern "C" void sps_batch_destroy(sps_batch* b) { delete b; }

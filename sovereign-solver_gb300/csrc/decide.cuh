@@ -1,0 +1,121 @@
+// decide.cuh — the scalar decisions of adaptive restarted PDHG, shared by the
+// single-LP kernels (taken by a kernel's last block) and the batched kernel
+// (taken by thread 0 of the block that owns an instance).  All FP64.
+#pragma once
+
+#include "engine.cuh"
+#include "../../include/sps_pdhg.h"
+
+namespace sps {
+
+enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4, AP_STEP_PENDING = 8 };
+
+// Adaptive step (PDLP): limit = ||dz||_w^2 / (2 |dy^T K dx|); the attempt is
+// accepted if eta <= limit; next eta = min((1 - (k+1)^-0.3) limit, (1 + (k+1)^-0.6) eta).
+// Returns false (and marks the state done) when the movement is not finite.
+__device__ __forceinline__ bool decide_step(Ctl& c, double dy2, double inter_signed) {
+    const double w = c.omega, eta = c.eta, dx2 = c.dx2, inter = fabs(inter_signed);
+    const double move = w * dx2 + dy2 / w;
+    const int64_t k = c.iters + 1;
+    if (!isfinite(move) || !isfinite(inter)) {
+        c.done = 1;
+        c.status = SPS_STATUS_NUMERIC_ERROR;
+        c.iters = k;
+        return false;
+    }
+    const double lim = inter > 0.0 ? move / (2.0 * inter) : INFINITY;
+    const float kk = float(k + 1);
+    const double next = fmin((1.0 - double(powf(kk, -0.3f))) * lim, (1.0 + double(powf(kk, -0.6f))) * eta);
+    const bool acc = (eta <= lim) || move == 0.0;
+    c.iters = k;
+    c.window += 1;
+    c.accepted = acc;
+    if (acc) {
+        c.cur = 1 - c.cur;
+        c.eta_used = eta;
+        c.w_sum += eta;
+        c.accepted_total += 1;
+    }
+    c.eta = next;
+    c.apply = AP_STEP_PENDING;
+    return true;
+}
+
+// Check of the average (point 0) and the current iterate (point 1).
+//   tr[4q + 0..3]: scaled primal residual^2, original primal residual^2, b^T y, ||y - y_last||^2
+//   tc[5q + 0..4]: scaled dual residual^2, original dual residual^2, c^T x, bound terms, ||x - x_last||^2
+// Termination on the relative KKT error of the original problem; restart on the
+// weighted KKT of the scaled problem (to the better of average and current) when
+// it dropped below 0.2x the last restart's, or below 0.8x while rising, or after
+// 0.36x of all attempts; primal weight updated at restarts.  Sets c.apply.
+__device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], const double (&tr)[8], double inv_nb,
+                                             double inv_nc, bool stop) {
+    const bool has_avg = c.w_sum > 0.0;
+    const double w = c.omega;
+    double rel[2], kw[2], rp[2], rd[2], gp[2], po[2], dob[2];
+    for (int q = 0; q < 2; ++q) {
+        po[q] = tc[5 * q + 2];
+        dob[q] = tr[4 * q + 2] + tc[5 * q + 3];
+        rp[q] = sqrt(tr[4 * q + 1]) * inv_nb;
+        rd[q] = sqrt(tc[5 * q + 1]) * inv_nc;
+        gp[q] = fabs(po[q] - dob[q]) / (1.0 + fabs(po[q]) + fabs(dob[q]));
+        rel[q] = fmax(rp[q], fmax(rd[q], gp[q]));
+        const double g = po[q] - dob[q];
+        kw[q] = sqrt(w * w * tr[4 * q + 0] + tc[5 * q + 0] / (w * w) + g * g);
+        if (!isfinite(rel[q])) rel[q] = INFINITY;
+        if (!isfinite(kw[q])) kw[q] = INFINITY;
+    }
+    c.last_avg_kkt = rel[0];
+    c.last_cur_kkt = rel[1];
+    if (c.init_phase) {
+        c.init_phase = 0;
+        c.kkt_last = kw[1];
+        c.kkt_prev_cand = kw[1];
+        c.rel_kkt = rel[1]; c.rel_p = rp[1]; c.rel_d = rd[1]; c.rel_gap = gp[1];
+        c.pobj = po[1]; c.dobj = dob[1];
+        c.apply = AP_CANDIDATE;
+        return;
+    }
+    const int best = (has_avg && rel[0] < rel[1]) ? 0 : 1;
+    const bool bad = !isfinite(rel[1]) && !(has_avg && isfinite(rel[0]));
+    bool finish = false;
+    if (bad) {
+        c.status = SPS_STATUS_NUMERIC_ERROR; finish = true;
+    } else if (rel[best] < c.tol) {
+        c.status = SPS_STATUS_OPTIMAL; finish = true;
+    } else if (c.iters >= c.max_iters) {
+        c.status = SPS_STATUS_ITERATION_LIMIT; finish = true;
+    } else if (stop) {
+        c.status = SPS_STATUS_TIME_LIMIT; finish = true;
+    }
+    if (finish) {
+        c.done = 1;
+        c.choice = best == 0 ? 1 : 0;
+        c.rel_kkt = rel[best]; c.rel_p = rp[best]; c.rel_d = rd[best]; c.rel_gap = gp[best];
+        c.pobj = po[best]; c.dobj = dob[best];
+        c.apply = best == 0 ? AP_LOAD_AVG : 0;
+        return;
+    }
+    const int cand = (has_avg && kw[0] < kw[1]) ? 0 : 1;
+    const double kc = kw[cand];
+    const bool restart = kc <= 0.2 * c.kkt_last || (kc <= 0.8 * c.kkt_last && kc > c.kkt_prev_cand) ||
+                         double(c.window) >= 0.36 * double(c.iters);
+    c.kkt_prev_cand = kc;
+    int apply = 0;
+    if (restart) {
+        const double dx = sqrt(tc[5 * cand + 4]), dy = sqrt(tr[4 * cand + 3]);
+        if (dx > 1e-10 && dy > 1e-10) {
+            const double nw = exp(0.5 * log(dy / dx) + 0.5 * log(w));
+            if (isfinite(nw) && nw > 0.0) c.omega = nw;
+        }
+        c.kkt_last = kc;
+        c.kkt_prev_cand = kc;
+        c.restarts += 1;
+        c.window = 0;
+        c.last_restart_iter = c.iters;
+        apply = AP_RESTART | AP_CANDIDATE | (cand == 0 ? AP_LOAD_AVG : 0);
+    }
+    c.apply = apply;
+}
+
+}  // namespace sps

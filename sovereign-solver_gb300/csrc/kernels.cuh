@@ -21,8 +21,7 @@
 // FP64, decision in the last block), rf_apply.
 #pragma once
 
-#include "engine.cuh"
-#include "../../include/sps_pdhg.h"
+#include "decide.cuh"
 
 namespace sps {
 
@@ -50,7 +49,6 @@ struct Args {
     int64_t max_windows;
 };
 
-enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4, AP_STEP_PENDING = 8 };
 
 // iteration kernels: register budget for kPassMinBlocks resident blocks per SM;
 // check kernels (FP64 accumulators, once per window) get the default budget
@@ -137,33 +135,7 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     add_segment_rows<2>(t, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_ROW_STEP] = 0;
-    // adaptive step (PDLP): limit = ||dz||_w^2 / (2 |dy^T K dx|); accept if eta <= limit;
-    // next eta = min((1 - (k+1)^-0.3) limit, (1 + (k+1)^-0.6) eta)
-    const double w = ctl->omega, eta = ctl->eta;
-    const double dy2 = t[0], inter = fabs(t[1]), dx2 = ctl->dx2;
-    const double move = w * dx2 + dy2 / w;
-    const int64_t k = ctl->iters + 1;
-    if (!isfinite(move) || !isfinite(inter)) {
-        ctl->done = 1;
-        ctl->status = SPS_STATUS_NUMERIC_ERROR;
-        ctl->iters = k;
-        return;
-    }
-    const double lim = inter > 0.0 ? move / (2.0 * inter) : INFINITY;
-    const float kk = float(k + 1);
-    const double next = fmin((1.0 - double(powf(kk, -0.3f))) * lim, (1.0 + double(powf(kk, -0.6f))) * eta);
-    const bool acc = (eta <= lim) || move == 0.0;
-    ctl->iters = k;
-    ctl->window += 1;
-    ctl->accepted = acc;
-    if (acc) {
-        ctl->cur = 1 - cur;
-        ctl->eta_used = eta;
-        ctl->w_sum += eta;
-        ctl->accepted_total += 1;
-    }
-    ctl->eta = next;
-    ctl->apply = AP_STEP_PENDING;
+    decide_step(*ctl, t[0], t[1]);
 }
 
 template <class V>
@@ -345,75 +317,7 @@ SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     add_segment_rows<8>(tr, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_CHECK] = 0;
-
-    const double w = ctl->omega;
-    double rel[2], kw[2], rp[2], rd[2], gp[2], po[2], dob[2];
-    for (int q = 0; q < 2; ++q) {
-        po[q] = tc[5 * q + 2];
-        dob[q] = tr[4 * q + 2] + tc[5 * q + 3];
-        rp[q] = sqrt(tr[4 * q + 1]) * a.inv_nb;
-        rd[q] = sqrt(tc[5 * q + 1]) * a.inv_nc;
-        gp[q] = fabs(po[q] - dob[q]) / (1.0 + fabs(po[q]) + fabs(dob[q]));
-        rel[q] = fmax(rp[q], fmax(rd[q], gp[q]));
-        const double g = po[q] - dob[q];
-        kw[q] = sqrt(w * w * tr[4 * q + 0] + tc[5 * q + 0] / (w * w) + g * g);
-        if (!isfinite(rel[q])) rel[q] = INFINITY;
-        if (!isfinite(kw[q])) kw[q] = INFINITY;
-    }
-    ctl->last_avg_kkt = rel[0];
-    ctl->last_cur_kkt = rel[1];
-    int apply = 0;
-    if (ctl->init_phase) {
-        ctl->init_phase = 0;
-        ctl->kkt_last = kw[1];
-        ctl->kkt_prev_cand = kw[1];
-        const int q = 1;
-        ctl->rel_kkt = rel[q]; ctl->rel_p = rp[q]; ctl->rel_d = rd[q]; ctl->rel_gap = gp[q];
-        ctl->pobj = po[q]; ctl->dobj = dob[q];
-        ctl->apply = AP_CANDIDATE;
-        return;
-    }
-    const int best = (has_avg && rel[0] < rel[1]) ? 0 : 1;
-    const bool bad = !isfinite(rel[1]) && !(has_avg && isfinite(rel[0]));
-    bool finish = false;
-    if (bad) {
-        ctl->status = SPS_STATUS_NUMERIC_ERROR; finish = true;
-    } else if (rel[best] < ctl->tol) {
-        ctl->status = SPS_STATUS_OPTIMAL; finish = true;
-    } else if (ctl->iters >= ctl->max_iters) {
-        ctl->status = SPS_STATUS_ITERATION_LIMIT; finish = true;
-    } else if (stop_requested(ctl, a.abort_flag)) {
-        ctl->status = SPS_STATUS_TIME_LIMIT; finish = true;
-    }
-    if (finish) {
-        ctl->done = 1;
-        ctl->choice = best == 0 ? 1 : 0;
-        ctl->rel_kkt = rel[best]; ctl->rel_p = rp[best]; ctl->rel_d = rd[best]; ctl->rel_gap = gp[best];
-        ctl->pobj = po[best]; ctl->dobj = dob[best];
-        ctl->apply = best == 0 ? AP_LOAD_AVG : 0;
-        return;
-    }
-    // restart decision on the weighted KKT (scaled space)
-    const int cand = (has_avg && kw[0] < kw[1]) ? 0 : 1;
-    const double kc = kw[cand];
-    const bool restart = kc <= 0.2 * ctl->kkt_last ||
-                         (kc <= 0.8 * ctl->kkt_last && kc > ctl->kkt_prev_cand) ||
-                         double(ctl->window) >= 0.36 * double(ctl->iters);
-    ctl->kkt_prev_cand = kc;
-    if (restart) {
-        const double dx = sqrt(tc[5 * cand + 4]), dy = sqrt(tr[4 * cand + 3]);
-        if (dx > 1e-10 && dy > 1e-10) {
-            const double nw = exp(0.5 * log(dy / dx) + 0.5 * log(w));
-            if (isfinite(nw) && nw > 0.0) ctl->omega = nw;
-        }
-        ctl->kkt_last = kc;
-        ctl->kkt_prev_cand = kc;
-        ctl->restarts += 1;
-        ctl->window = 0;
-        ctl->last_restart_iter = ctl->iters;
-        apply = AP_RESTART | AP_CANDIDATE | (cand == 0 ? AP_LOAD_AVG : 0);
-    }
-    ctl->apply = apply;
+    decide_check(*ctl, tc, tr, a.inv_nb, a.inv_nc, stop_requested(ctl, a.abort_flag));
 }
 
 template <class V>

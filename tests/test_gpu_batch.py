@@ -1,0 +1,69 @@
+"""Batched PDHG on the GPU: every instance checked by the CPU oracle in FP64.
+
+The batch mixes planted equality LPs of uneven sizes (the batched workload's
+construction at smaller sizes), small transportation LPs (<= rows, unbounded
+columns) and the mixed-bounds fixture (free / boxed / one-sided columns).
+"""
+
+import numpy as np
+import pytest
+
+import sovereign_solver_gb300 as sps
+import sovereign_solver_gb300.workloads as wl
+from fixtures import load_problems
+from oracle import kkt
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def _batch():
+    probs, stars = [], []
+    for k in range(40):
+        p, info = wl.batch_planted_lp(k, m_range=(20, 400))
+        probs.append(p)
+        stars.append(info["obj_star"])
+    for s in range(6):
+        probs.append(wl.transportation_lp(20 + 5 * s, 40 + 7 * s, seed=s)[0])
+        stars.append(None)
+    probs.append(load_problems()["mixed_bounds"])
+    stars.append(None)
+    return probs, stars
+
+
+@pytest.mark.parametrize("group", [0, 4, 32])
+def test_batch_solves_every_instance(group):
+    probs, stars = _batch()
+    with sps.PDHGBatch(probs, tol=TOL, max_iters=200000, batch_group=group) as b:
+        res = b.solve()
+        st = b.stats
+    assert st.optimal == len(probs)
+    assert group == 0 or st.lanes_per_column == group
+    for p, r, star in zip(probs, res, stars):
+        assert r.status == "optimal", (p.name, r)
+        box = kkt.box_rel_kkt(p, r.x, r.y)
+        assert box["err"] < 1.5 * TOL, (p.name, box)
+        if star is not None:
+            assert abs(r.objective - star) <= 20 * TOL * (1 + abs(star)), (p.name, r.objective, star)
+
+
+def test_batch_matches_single_and_is_deterministic():
+    probs, _ = _batch()
+    probs = probs[:12]
+    with sps.PDHGBatch(probs, tol=TOL, batch_group=8) as b:
+        a = b.solve()
+        c = b.solve()                    # graph replay
+    for r1, r2 in zip(a, c):
+        assert r1.iterations == r2.iterations
+        np.testing.assert_array_equal(r1.x, r2.x)
+    for p, r in zip(probs, a):
+        s = sps.solve_lp_pdhg(p, tol=TOL)
+        assert abs(s.objective - r.objective) <= 20 * TOL * (1 + abs(s.objective))
+
+
+def test_batch_iteration_limit():
+    probs, _ = _batch()
+    res = sps.solve_lp_pdhg_batch(probs[:5], tol=1e-12, max_iters=128)
+    for r in res:
+        assert r.status == "iteration_limit" and r.iterations == 128
