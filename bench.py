@@ -123,7 +123,7 @@ def iteration_bytes(p) -> dict:
 
     row pass  (K x' + dual update):   8 nnz + 4(m+1) + 4n + 20m
     col pass  (K^T y' + primal update + averages):
-              8 nnz + 4(n+1) + 4m + 24n (+8n with per-column bounds) + 12m
+              8 nnz + 4(n+1) + 4m + 28n (+8n with per-column bounds) + 16m
     Vectors gathered through the SpMV are counted once (L2-resident gather).
     """
     n, m = p.n_vars, p.n_ineq + p.n_eq
@@ -132,7 +132,7 @@ def iteration_bytes(p) -> dict:
     uniform = (np.all(lb == lb[0]) and np.all(ub == ub[0]) and (lb[0] == 0 or np.isinf(lb[0]))
                and np.isinf(ub[0]) and ub[0] > 0)
     row = 8 * nnz + 4 * (m + 1) + 4 * n + 20 * m
-    col = 8 * nnz + 4 * (n + 1) + 4 * m + 24 * n + (0 if uniform else 8 * n) + 12 * m
+    col = 8 * nnz + 4 * (n + 1) + 4 * m + 28 * n + (0 if uniform else 8 * n) + 16 * m
     spmv_row = 8 * nnz + 4 * (m + 1) + 4 * n + 4 * m
     spmv_col = 8 * nnz + 4 * (n + 1) + 4 * m + 4 * n
     return {"row": row, "col": col, "spmv_row": spmv_row, "spmv_col": spmv_col, "nnz": nnz}

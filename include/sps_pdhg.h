@@ -39,6 +39,8 @@ extern "C" {
 #define SPS_STATUS_ITERATION_LIMIT  1
 #define SPS_STATUS_TIME_LIMIT       2
 #define SPS_STATUS_NUMERIC_ERROR    3   /* NaN/Inf appeared in the iterates */
+#define SPS_STATUS_STALLED          4   /* FP32 iterates stopped making progress (returned
+                                           only with sps_options.escalate = 2) */
 
 /* algorithm */
 #define SPS_MODE_REFERENCE  0  /* the reference's rules: standard form with bound rows and
@@ -81,7 +83,12 @@ typedef struct {
     int32_t device;           /* CUDA device ordinal */
     int32_t max_blocks;       /* schedule tuning: blocks per matrix-pass launch, 0 = one resident wave */
     int32_t batch_group;      /* batched solver: lanes per column (4, 8, 16, 32), 0 = autotune */
-    int32_t reserved[5];
+    int32_t escalate;         /* adaptive FP32 stall handling.  A solve stalls when its best
+                                 relative KKT error has not halved for max(2048, k/2) attempts
+                                 (k = attempt of the last halving).  1 (default): continue in
+                                 FP64 from the best point seen, with the primal weight it had;
+                                 2: stop with SPS_STATUS_STALLED; 0: no stall test (FP32 only) */
+    int32_t reserved[4];
 } sps_options;
 
 typedef struct {
@@ -100,7 +107,9 @@ typedef struct {
     double  solve_ms;         /* device time of sps_solve */
     int64_t kernel_launches;  /* kernels launched by sps_solve (graph nodes executed count once per run) */
     int32_t returned_average; /* 1 if the returned point is the ergodic average */
-    int32_t reserved[5];
+    int32_t escalated;        /* 1 if the solve stalled in FP32 and was finished in FP64; the
+                                 iteration, restart and time fields then cover both parts */
+    int32_t reserved[4];
 } sps_result;
 
 typedef struct sps_handle sps_handle;
@@ -164,7 +173,9 @@ typedef struct {
     int32_t optimal;            /* instances that reached tol */
     int32_t lanes_per_column;   /* schedule used (autotuned or given) */
     int32_t blocks;             /* persistent blocks */
-    int32_t reserved[5];
+    int32_t escalated;          /* instances that stalled in FP32 and were finished in FP64 by the
+                                   single-LP engine after the persistent launch (in solve_ms) */
+    int32_t reserved[4];
 } sps_batch_stats;
 
 /* Pack `count` problems, upload and scale them (one block per instance) and pick

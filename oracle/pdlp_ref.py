@@ -9,7 +9,13 @@ Used to check the engine's trajectory on small problems and to study the
 effect of the iterate precision.
 
 ``interaction``: "difference" forms K Δx as K x' − K x of the two products (as
-the engine's FP32 path did first), "direct" forms it as K (x' − x).
+the engine does), "direct" forms it as K (x' − x).
+
+The averages are kept as the engine keeps them, as offsets from the restart
+point (x̄ = x_last + Σ w_k (x_k − x_last) / Σ w_k): with FP32 iterates a plain
+FP32 sum Σ w_k x_k loses the digits that the restart tests need near
+convergence and the method stalls near KKT 1e-3 on some planted LPs, which
+the offset form (and FP64 sums) avoid.
 """
 
 from __future__ import annotations
@@ -100,15 +106,15 @@ def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="di
             lim = move / (2 * inter) if inter > 0 else np.inf
             nxt = min((1 - (k + 1) ** -0.3) * lim, (1 + (k + 1) ** -0.6) * eta)
             if eta <= lim or move == 0:
-                xs = (xs + dtype(eta) * x2).astype(dtype)
-                ys = (ys + dtype(eta) * y2).astype(dtype)
+                xs = (xs + dtype(eta) * (x2 - xl)).astype(dtype)
+                ys = (ys + dtype(eta) * (y2 - yl)).astype(dtype)
                 wsum += eta
                 x, y, ax = x2, y2, ax2
                 aty = (KT @ y).astype(dtype)
             eta = nxt
         has_avg = wsum > 0
-        xa = (xs / wsum).astype(dtype) if has_avg else x
-        ya = (ys / wsum).astype(dtype) if has_avg else y
+        xa = (xl + xs.astype(float) / wsum).astype(dtype) if has_avg else x
+        ya = (yl + ys.astype(float) / wsum).astype(dtype) if has_avg else y
         ea, ka, axa, atya = metrics(xa, ya)
         ec, kc_, _, _ = metrics(x, y)
         best_avg = has_avg and ea < ec

@@ -21,7 +21,8 @@ ERRORS = {
     -4: "SPS_ERR_STATE",
     -5: "SPS_ERR_TIMEOUT",
 }
-STATUS = {0: "optimal", 1: "iteration_limit", 2: "time_limit", 3: "numeric_error"}
+STATUS = {0: "optimal", 1: "iteration_limit", 2: "time_limit", 3: "numeric_error", 4: "stalled"}
+ESCALATE = {"off": 0, "fp64": 1, "stop": 2}
 MODES = {"reference": 0, "adaptive": 1}
 PRECISIONS = {"fp32": 0, "fp64": 1}
 
@@ -40,7 +41,7 @@ class Options(C.Structure):
         ("mode", C.c_int32), ("precision", C.c_int32), ("max_iters", C.c_int64), ("tol", C.c_double),
         ("check_interval", C.c_int32), ("ruiz_iters", C.c_int32), ("time_limit_s", C.c_double),
         ("graph_mode", C.c_int32), ("device", C.c_int32), ("max_blocks", C.c_int32),
-        ("batch_group", C.c_int32), ("reserved", C.c_int32 * 5),
+        ("batch_group", C.c_int32), ("escalate", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -48,7 +49,7 @@ class BatchStats(C.Structure):
     _fields_ = [
         ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("total_iterations", C.c_int64),
         ("optimal", C.c_int32), ("lanes_per_column", C.c_int32), ("blocks", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("escalated", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 
@@ -59,7 +60,7 @@ class Result(C.Structure):
         ("rel_primal", C.c_double), ("rel_dual", C.c_double), ("rel_gap", C.c_double),
         ("primal_weight", C.c_double), ("step_size", C.c_double), ("setup_ms", C.c_double),
         ("solve_ms", C.c_double), ("kernel_launches", C.c_int64), ("returned_average", C.c_int32),
-        ("reserved", C.c_int32 * 5),
+        ("escalated", C.c_int32), ("reserved", C.c_int32 * 4),
     ]
 
 

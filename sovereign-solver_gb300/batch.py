@@ -4,7 +4,9 @@ New API surface (the reference solves one LP per call).  Each instance keeps
 its own step size, primal weight, restarts and termination; the batch is
 packed and scaled on the GPU once (``PDHGBatch``), then solved by one
 persistent kernel launch replayed from a CUDA graph (``PDHGBatch.solve``).
-Adaptive mode with FP32 iterates and FP64 checks only.
+Adaptive mode with FP32 iterates and FP64 checks; an instance whose error
+stops halving in FP32 is finished in FP64 by the single-LP engine after the
+launch, warm-started from its best point (``escalate="fp64"``, the default).
 """
 
 from __future__ import annotations
@@ -24,11 +26,13 @@ class PDHGBatch:
 
     ``batch_group`` picks the lanes per column of the column pass (4, 8, 16,
     32); 0 lets the library time the candidates on a sample of the batch.
+    ``escalate``: "fp64" (FP64 continuation of stalled instances), "stop"
+    (status "stalled") or "off" (FP32 to the iteration limit).
     """
 
     def __init__(self, problems: Sequence, tol: float = 1e-4, max_iters: int = MAX_PDHG_ITERS,
                  batch_group: int = 0, time_limit: float = 0.0, check_interval: int = 0,
-                 graph_mode: int = 2, device: int = 0, ruiz_iters: int = 10):
+                 graph_mode: int = 2, device: int = 0, ruiz_iters: int = 10, escalate: str = "fp64"):
         self.lib = N.load()
         self.problems = list(problems)
         if not self.problems:
@@ -37,7 +41,7 @@ class PDHGBatch:
         arr = (N.ProblemDesc * len(self._descs))(*[d.desc for d in self._descs])
         o = make_options(tol=tol, max_iters=max_iters, time_limit=time_limit,
                          check_interval=check_interval, graph_mode=graph_mode, device=device,
-                         ruiz_iters=ruiz_iters)
+                         ruiz_iters=ruiz_iters, escalate=escalate)
         o.batch_group = int(batch_group)
         h = C.c_void_p()
         N.check(self.lib.sps_batch_create(len(self._descs), arr, C.byref(o), C.byref(h)), None)

@@ -2,15 +2,29 @@
 // include/sps_pdhg.h): input validation, the reference standard-form
 // conversion for SPS_MODE_REFERENCE, and handle management.
 #include <cmath>
+#include <chrono>
 #include <cstring>
+#include <memory>
 #include <string>
 
 #include "engine_impl.cuh"
 
 using namespace sps;
 
+// A caller problem copied into owned storage (the descriptor's arrays are only
+// valid during sps_create); kept when a stalled FP32 solve may continue in FP64.
+struct ProblemCopy {
+    sps_problem_desc d{};
+    std::vector<int32_t> ubp, ubi, eqp, eqi;
+    std::vector<double> ubv, eqv, c, bub, beq, lb, ub;
+};
+
 struct sps_handle {
     EngineBase* eng = nullptr;
+    sps_options opt{};
+    std::unique_ptr<ProblemCopy> copy;   // set when escalation is possible
+    sps_handle* esc = nullptr;           // FP64 continuation, created at the first stall
+    bool last_esc = false;               // the last solve finished in esc
 };
 
 namespace {
@@ -159,6 +173,71 @@ void build_standard(const sps_problem_desc* d, HostProblem& hp, StdMap& s) {
     hp.ub = hp.own_ub.data();
 }
 
+std::unique_ptr<ProblemCopy> copy_problem(const sps_problem_desc* d) {
+    auto p = std::make_unique<ProblemCopy>();
+    const int64_t nub = d->m_ub ? d->ub_indptr[d->m_ub] : 0, neq = d->m_eq ? d->eq_indptr[d->m_eq] : 0;
+    auto take = [](auto& v, const auto* src, int64_t len) {
+        if (src && len > 0) v.assign(src, src + len);
+        return v.empty() ? nullptr : v.data();
+    };
+    p->d = *d;
+    p->d.ub_indptr = take(p->ubp, d->ub_indptr, d->m_ub ? d->m_ub + 1 : 0);
+    p->d.ub_indices = take(p->ubi, d->ub_indices, nub);
+    p->d.ub_values = take(p->ubv, d->ub_values, nub);
+    p->d.eq_indptr = take(p->eqp, d->eq_indptr, d->m_eq ? d->m_eq + 1 : 0);
+    p->d.eq_indices = take(p->eqi, d->eq_indices, neq);
+    p->d.eq_values = take(p->eqv, d->eq_values, neq);
+    p->d.c = take(p->c, d->c, d->n);
+    p->d.b_ub = take(p->bub, d->b_ub, d->m_ub);
+    p->d.b_eq = take(p->beq, d->b_eq, d->m_eq);
+    p->d.lb = take(p->lb, d->lb, d->n);
+    p->d.ub = take(p->ub, d->ub, d->n);
+    return p;
+}
+
+// A stalled FP32 solve continues in FP64 from the best point it saw, with the
+// primal weight it had there, within the iteration and time limits left.
+int escalate(sps_handle* h, sps_result* res) {
+    const auto t0 = std::chrono::steady_clock::now();
+    EngineBase* e = h->eng;
+    if (!h->esc) {
+        sps_options o = h->opt;
+        o.precision = SPS_FP64;
+        o.escalate = 0;
+        const int rc = sps_create(&h->copy->d, &o, &h->esc);
+        if (rc != SPS_OK) return e->fail(rc, "FP64 continuation: " + g_create_error);
+    }
+    std::vector<double> x(std::max(e->n_user, 1)), y(std::max(e->m_user, 1));
+    double omega = 0.0;
+    if (int rc = e->get_best(x.data(), y.data(), &omega)) return rc;
+    EngineBase* f = h->esc->eng;
+    if (int rc = f->warm(x.data(), y.data(), omega)) return e->fail(rc, "FP64 continuation: " + f->err);
+    double tl = 0.0;
+    if (h->opt.time_limit_s > 0) {
+        const double used = res->solve_ms * 1e-3 +
+                            std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        tl = h->opt.time_limit_s - used;
+        if (tl <= 0) {
+            res->status = SPS_STATUS_TIME_LIMIT;
+            return SPS_OK;
+        }
+    }
+    f->set_limits(std::max<int64_t>(h->opt.max_iters - res->iterations, 1), tl);
+    sps_result r2;
+    f->err.clear();
+    if (int rc = f->solve(&r2)) return e->fail(rc, "FP64 continuation: " + f->err);
+    r2.iterations += res->iterations;
+    r2.accepted_steps += res->accepted_steps;
+    r2.restarts += res->restarts;
+    r2.kernel_launches += res->kernel_launches;
+    r2.setup_ms = res->setup_ms;
+    r2.solve_ms = res->solve_ms + 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    r2.escalated = 1;
+    *res = r2;
+    h->last_esc = true;
+    return SPS_OK;
+}
+
 }  // namespace
 
 namespace sps {
@@ -181,6 +260,7 @@ int sps_options_init(sps_options* o) {
     o->graph_mode = 2;
     o->device = 0;
     o->max_blocks = 0;
+    o->escalate = 1;
     return SPS_OK;
 }
 
@@ -208,6 +288,8 @@ int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_hand
     else build_box(prob, hp);
 
     sps_handle* h = new sps_handle();
+    h->opt = opt;
+    if (opt.mode == SPS_MODE_ADAPTIVE && opt.precision == SPS_FP32 && opt.escalate == 1) h->copy = copy_problem(prob);
     h->eng = opt.precision == SPS_FP32 ? make_engine_f32() : make_engine_f64();
     EngineBase* e = h->eng;
     e->n_user = prob->n;
@@ -235,7 +317,10 @@ int sps_set_warm_start(sps_handle* h, const double* x0, const double* y0, double
 int sps_solve(sps_handle* h, sps_result* res) {
     if (!h || !res) return SPS_ERR_INVALID;
     h->eng->err.clear();
-    return h->eng->solve(res);
+    h->last_esc = false;
+    const int rc = h->eng->solve(res);
+    if (rc != SPS_OK || res->status != SPS_STATUS_STALLED || !h->copy) return rc;
+    return escalate(h, res);
 }
 
 int sps_time_iteration_kernels(sps_handle* h, int32_t reps, double* out) {
@@ -245,6 +330,11 @@ int sps_time_iteration_kernels(sps_handle* h, int32_t reps, double* out) {
 
 int sps_get_solution(sps_handle* h, double* x, double* y) {
     if (!h) return SPS_ERR_INVALID;
+    if (h->last_esc) {
+        const int rc = h->esc->eng->get(x, y);
+        if (rc) h->eng->err = h->esc->eng->err;
+        return rc;
+    }
     return h->eng->get(x, y);
 }
 
@@ -254,6 +344,7 @@ const char* sps_last_error(const sps_handle* h) {
 
 void sps_destroy(sps_handle* h) {
     if (!h) return;
+    if (h->esc) sps_destroy(h->esc);
     delete h->eng;
     delete h;
 }

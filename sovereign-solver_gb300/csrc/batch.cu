@@ -32,11 +32,20 @@ struct Gather1 {
     __device__ __forceinline__ float operator()(int, int j) const { return __ldg(x + j); }
 };
 
+// Point 0 of a check is the average, kept as an offset from the restart point
+// (x_last + x_sum / w_sum, x_sum = sum of w_k (x_k - x_last)) so that FP32 sums
+// stay accurate near convergence; l = null when there is no average yet and
+// point 0 aliases the current iterate.
+__device__ __forceinline__ double avg_at(const float* s, const float* l, double inv_w, int j) {
+    const double v = double(__ldg(s + j)) * inv_w;
+    return l ? v + double(__ldg(l + j)) : v;
+}
+
 struct Gather2 {
-    const float *s, *x;
+    const float *s, *l, *x;
     double inv_w;
     __device__ __forceinline__ double operator()(int q, int j) const {
-        return q == 0 ? double(__ldg(s + j)) * inv_w : double(__ldg(x + j));
+        return q == 0 ? avg_at(s, l, inv_w, j) : double(__ldg(x + j));
     }
 };
 
@@ -70,15 +79,15 @@ struct RowStepE {
 
 // column pass of an accepted attempt: K^T y', averages, next candidate
 struct ColStepE {
-    const float *xc, *c, *lo, *hi;
+    const float *xc, *c, *lo, *hi, *xl;
     float *aty, *xn, *xs;
     float tau, wgt;
     float dx2 = 0.f;
-    struct Pre { float xj, cj, l, h, s; };
-    __device__ __forceinline__ Pre pre(int j) const { return Pre{xc[j], c[j], lo[j], hi[j], xs[j]}; }
+    struct Pre { float xj, cj, l, h, s, r; };
+    __device__ __forceinline__ Pre pre(int j) const { return Pre{xc[j], c[j], lo[j], hi[j], xs[j], xl[j]}; }
     __device__ __forceinline__ void operator()(int j, const float (&acc)[1], const Pre& p) {
         aty[j] = acc[0];
-        xs[j] = p.s + wgt * p.xj;
+        xs[j] = p.s + wgt * (p.xj - p.r);
         const float x2 = fminf(fmaxf(p.xj - tau * (p.cj - acc[0]), p.l), p.h);
         xn[j] = x2;
         const float d = x2 - p.xj;
@@ -87,7 +96,7 @@ struct ColStepE {
 };
 
 struct RowCheckE {
-    const float *b, *ys, *yc, *yl;
+    const float *b, *ys, *ylb, *yc, *yl;
     const double* dr;
     const int8_t* kind;
     float* axa;
@@ -103,7 +112,7 @@ struct RowCheckE {
             if (kind[r]) res = fmax(res, 0.0);
             p[4 * q + 0] += res * res;
             p[4 * q + 1] += (res / d) * (res / d);
-            const double yv = q == 0 ? double(ys[r]) * inv_w : double(yc[r]);
+            const double yv = q == 0 ? avg_at(ys, ylb, inv_w, r) : double(yc[r]);
             p[4 * q + 2] += br * yv;
             const double dd = yv - double(yl[r]);
             p[4 * q + 3] += dd * dd;
@@ -112,7 +121,7 @@ struct RowCheckE {
 };
 
 struct ColCheckE {
-    const float *c, *lo, *hi, *xs, *xc, *xl;
+    const float *c, *lo, *hi, *xs, *xlb, *xc, *xl;
     const double* dc;
     float* atya;
     double inv_w;
@@ -129,7 +138,7 @@ struct ColCheckE {
             const double dres = rc - lam;
             p[5 * q + 0] += dres * dres;
             p[5 * q + 1] += (dres / d) * (dres / d);
-            const double xv = q == 0 ? double(xs[j]) * inv_w : double(xc[j]);
+            const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
             p[5 * q + 2] += cj * xv;
             p[5 * q + 3] += (hl ? l * fmax(lam, 0.0) : 0.0) + (hh ? h * fmin(lam, 0.0) : 0.0);
             const double dd = xv - double(xl[j]);
@@ -147,6 +156,7 @@ struct View {                 // one instance's arrays
     const double *dc, *dr;
     float *X[2], *ATY[2], *xs, *xl, *atya;
     float *Y[2], *AX[2], *ys, *yl, *axa;
+    float *xb, *yb;
 };
 
 __device__ __forceinline__ View make_view(const Args& A, const Inst& I, int G) {
@@ -162,6 +172,8 @@ __device__ __forceinline__ View make_view(const Args& A, const Inst& I, int G) {
     v.xs = a.xs + I.vc; v.xl = a.xl + I.vc; v.atya = a.atya + I.vc;
     v.Y[0] = a.y0 + I.vr; v.Y[1] = a.y1 + I.vr; v.AX[0] = a.ax0 + I.vr; v.AX[1] = a.ax1 + I.vr;
     v.ys = a.ys + I.vr; v.yl = a.yl + I.vr; v.axa = a.axa + I.vr;
+    v.xb = a.xb ? a.xb + I.vc : nullptr;
+    v.yb = a.yb ? a.yb + I.vr : nullptr;
     return v;
 }
 
@@ -171,11 +183,13 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     const bool has_avg = c.w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / c.w_sum : 1.0;
     const int cur = c.cur;
-    RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w};
-    group_rows<32, 2, double>(v.rptr, v.ridx, v.rval, v.m, Gather2{has_avg ? v.xs : v.X[cur], v.X[cur], inv_w}, er);
+    RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w};
+    group_rows<32, 2, double>(v.rptr, v.ridx, v.rval, v.m,
+                              Gather2{has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], inv_w}, er);
     block_sum<8>(er.p, sm);
-    ColCheckE ec{v.c, v.lo, v.hi, has_avg ? v.xs : v.X[cur], v.X[cur], v.xl, v.dc, v.atya, inv_w};
-    group_rows_dyn<2, double>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather2{has_avg ? v.ys : v.Y[cur], v.Y[cur], inv_w}, ec);
+    ColCheckE ec{v.c, v.lo, v.hi, has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], v.xl, v.dc, v.atya, inv_w};
+    group_rows_dyn<2, double>(v.G, v.cptr, v.cidx, v.cval, v.n,
+                              Gather2{has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], inv_w}, ec);
     block_sum<10>(ec.p, sm);
     if (threadIdx.x == 0) {
         const bool stop = deadline && global_ns() > deadline;
@@ -185,13 +199,15 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     const int ap = c.apply;
     if (ap == 0) return;
     const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !c.done;
+    const bool save = (ap & AP_SAVE_BEST) && v.xb, save_avg = ap & AP_SAVE_AVG;
     const double iw = c.w_sum > 0.0 ? 1.0 / c.w_sum : 0.0;
     const float tau = float(c.eta / c.omega);
     float dx2 = 0.f;
     for (int j = threadIdx.x; j < v.n; j += kBlock) {
+        if (save) v.xb[j] = save_avg ? float(double(v.xl[j]) + double(v.xs[j]) * iw) : v.X[cur][j];
         float xv;
         if (load) {
-            xv = float(double(v.xs[j]) * iw);
+            xv = float(double(v.xl[j]) + double(v.xs[j]) * iw);
             v.X[cur][j] = xv;
             v.ATY[cur][j] = v.atya[j];
         } else {
@@ -205,9 +221,10 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
         }
     }
     for (int i = threadIdx.x; i < v.m; i += kBlock) {
+        if (save) v.yb[i] = save_avg ? float(double(v.yl[i]) + double(v.ys[i]) * iw) : v.Y[cur][i];
         float yv;
         if (load) {
-            yv = float(double(v.ys[i]) * iw);
+            yv = float(double(v.yl[i]) + double(v.ys[i]) * iw);
             v.Y[cur][i] = yv;
             v.AX[cur][i] = v.axa[i];
         } else {
@@ -237,6 +254,7 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
         c.eta = A.a.eta0[k];
         c.omega = A.a.omega0[k];
         c.kkt_last = INFINITY;
+        c.stall_on = A.stall_on;
     }
     for (int j = threadIdx.x; j < v.n; j += kBlock) {
         const float x = fminf(fmaxf(0.f, v.lo[j]), v.hi[j]);
@@ -266,10 +284,10 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
             const float tau = float(c.eta / c.omega), wgt = float(c.eta_used);
             float dx2;
             if (c.accepted) {
-                ColStepE ec{v.X[cur], v.c, v.lo, v.hi, v.ATY[cur], v.X[1 - cur], v.xs, tau, wgt};
+                ColStepE ec{v.X[cur], v.c, v.lo, v.hi, v.xl, v.ATY[cur], v.X[1 - cur], v.xs, tau, wgt};
                 group_rows_dyn<1, float>(G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur]}, ec);
                 dx2 = ec.dx2;
-                for (int i = threadIdx.x; i < v.m; i += kBlock) v.ys[i] += wgt * v.Y[cur][i];
+                for (int i = threadIdx.x; i < v.m; i += kBlock) v.ys[i] += wgt * (v.Y[cur][i] - v.yl[i]);
             } else {
                 dx2 = 0.f;
                 for (int j = threadIdx.x; j < v.n; j += kBlock) {
@@ -409,8 +427,10 @@ __global__ void __launch_bounds__(kBlock) k_batch_extract(const Inst* inst, cons
     const int k = blockIdx.x;
     const Inst I = inst[k];
     const int cur = out[k].cur;
-    const float* X = (cur ? a.x1 : a.x0) + I.vc;
-    const float* Y = (cur ? a.y1 : a.y0) + I.vr;
+    // a stalled instance hands its best point to the FP64 continuation
+    const bool best = out[k].status == SPS_STATUS_STALLED && out[k].best_saved && a.xb;
+    const float* X = best ? a.xb + I.vc : (cur ? a.x1 : a.x0) + I.vc;
+    const float* Y = best ? a.yb + I.vr : (cur ? a.y1 : a.y0) + I.vr;
     for (int j = threadIdx.x; j < I.n; j += kBlock) xo[I.vc + j] = double(X[j]) * a.dc[I.vc + j];
     for (int i = threadIdx.x; i < I.m; i += kBlock) yo[I.vr + i] = double(Y[i]) * a.dr[I.vr + i];
 }
@@ -441,8 +461,13 @@ struct sps_batch {
     sps::batch::Arrays arr{};
     int64_t sum_n = 0, sum_m = 0;
     std::vector<double> c_all, lb_all, ub_all;   // original data, packed like the column vectors
+    // original rows (local CSR offsets, columns, values) and right-hand sides,
+    // kept for the FP64 continuation of stalled instances
+    std::vector<int32_t> h_rptr, h_ridx;
+    std::vector<double> h_rv, h_b;
     std::vector<double> xo, yo;
     std::vector<Ctl> out;
+    std::vector<int8_t> escalated;
     cudaGraphExec_t gexec = nullptr;
     int32_t gexec_G = -1;
     uint64_t gexec_tl = 0;
@@ -510,6 +535,68 @@ bool check_instance(const sps_problem_desc& d, std::string& why) {
     for (int32_t i = 0; i < d.m_eq; ++i)
         if (!std::isfinite(d.b_eq[i])) { why = "non-finite right-hand side"; return false; }
     return true;
+}
+
+// FP64 continuation of stalled instance k (after the persistent launch): the
+// single-LP engine solves it in FP64, warm-started from the best point of the
+// FP32 stall test (in xo / yo) with the primal weight it had there, within the
+// iterations and time left; its result replaces the instance's.
+int continue_fp64(sps_batch* b, int32_t k, double used_s) {
+    const Inst& I = b->inst[k];
+    Ctl& c = b->out[k];
+    if (b->opt.time_limit_s > 0 && used_s >= b->opt.time_limit_s) {
+        c.status = SPS_STATUS_TIME_LIMIT;
+        return SPS_OK;
+    }
+    const int32_t* P = b->h_rptr.data() + I.rp;
+    const int32_t m_eq = I.m - I.m_ub;
+    std::vector<int32_t> eqp(m_eq + 1);
+    for (int32_t i = 0; i <= m_eq; ++i) eqp[i] = P[I.m_ub + i] - P[I.m_ub];
+    sps_problem_desc d{};
+    d.n = I.n;
+    d.m_ub = I.m_ub;
+    d.m_eq = m_eq;
+    d.ub_indptr = P;
+    d.ub_indices = b->h_ridx.data() + I.re;
+    d.ub_values = b->h_rv.data() + I.re;
+    d.eq_indptr = eqp.data();
+    d.eq_indices = b->h_ridx.data() + I.re + P[I.m_ub];
+    d.eq_values = b->h_rv.data() + I.re + P[I.m_ub];
+    d.c = b->c_all.data() + I.vc;
+    d.lb = b->lb_all.data() + I.vc;
+    d.ub = b->ub_all.data() + I.vc;
+    d.b_ub = b->h_b.data() + I.vr;
+    d.b_eq = b->h_b.data() + I.vr + I.m_ub;
+    sps_options o = b->opt;
+    o.precision = SPS_FP64;
+    o.escalate = 0;
+    o.max_iters = std::max<int64_t>(b->opt.max_iters - c.iters, 1);
+    o.time_limit_s = b->opt.time_limit_s > 0 ? b->opt.time_limit_s - used_s : 0.0;
+    sps_handle* h = nullptr;
+    int rc = sps_create(&d, &o, &h);
+    if (rc != SPS_OK) return b->fail(rc, "instance " + std::to_string(k) + " FP64 continuation: " + sps_last_error(nullptr));
+    sps_result r;
+    double* x = b->xo.data() + I.vc;
+    double* y = b->yo.data() + I.vr;
+    rc = sps_set_warm_start(h, x, y, c.omega_best);
+    if (rc == SPS_OK) rc = sps_solve(h, &r);
+    if (rc == SPS_OK) rc = sps_get_solution(h, x, y);
+    if (rc != SPS_OK) {
+        const std::string why = sps_last_error(h);
+        sps_destroy(h);
+        return b->fail(rc, "instance " + std::to_string(k) + " FP64 continuation: " + why);
+    }
+    sps_destroy(h);
+    c.status = r.status;
+    c.iters += r.iterations;
+    c.accepted_total += r.accepted_steps;
+    c.restarts += r.restarts;
+    c.rel_kkt = r.rel_kkt; c.rel_p = r.rel_primal; c.rel_d = r.rel_dual; c.rel_gap = r.rel_gap;
+    c.omega = r.primal_weight;
+    c.eta = r.step_size;
+    c.choice = r.returned_average;
+    b->escalated[k] = 1;
+    return SPS_OK;
 }
 
 }  // namespace
@@ -667,6 +754,8 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         SPB_CK(cudaMemsetAsync(b->d_deadline, 0, sizeof(uint64_t), b->st));
         SPB_CK(b->alloc(&b->d_xo, vc));
         SPB_CK(b->alloc(&b->d_yo, vr));
+        float *d_xb = nullptr, *d_yb = nullptr;
+        if (opt.escalate != 0) { SPB_CK(b->alloc(&d_xb, vc)); SPB_CK(b->alloc(&d_yb, vr)); }
         double *t_rv, *t_cv, *t_c, *t_lo, *t_hi, *t_b;
         SPB_CK(cudaMalloc(&t_rv, sizeof(double) * std::max<int64_t>(NNZ, 1)));
         SPB_CK(cudaMalloc(&t_cv, sizeof(double) * std::max<int64_t>(NNZ, 1)));
@@ -694,7 +783,13 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         a = sps::batch::Arrays{d_rptr, d_ridx, d_cptr, d_cidx, d_rval, d_cval, d_kind, d_c, d_lo, d_hi, d_b,
                                d_dc, d_dr, d_eta0, d_om0,
                                st_f[0], st_f[1], st_f[2], st_f[3], st_f[4], st_f[5], st_f[6],
-                               st_f[7], st_f[8], st_f[9], st_f[10], st_f[11], st_f[12], st_f[13]};
+                               st_f[7], st_f[8], st_f[9], st_f[10], st_f[11], st_f[12], st_f[13], d_xb, d_yb};
+        if (opt.escalate == 1) {
+            b->h_rptr = std::move(rptr);
+            b->h_ridx = std::move(ridx);
+            b->h_rv = std::move(rv);
+            b->h_b = std::move(b64);
+        }
         int nb = 0, dev = opt.device, sms = 152;
         SPB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sps::batch::k_batch_solve, sps::kBlock, 0));
         SPB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -714,7 +809,7 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         double best = 1e300;
         for (int G : {4, 8, 16, 32}) {
             sps::batch::Args A{bb->d_inst, bb->d_order, sample, 64, 128, 0.0, bb->d_deadline, bb->arr, bb->d_out,
-                               bb->d_counter};
+                               bb->d_counter, 0};
             cudaMemsetAsync(bb->d_counter, 0, sizeof(uint32_t), bb->st);
             cudaEventRecord(bb->e0, bb->st);
             sps::batch::k_batch_solve<<<std::min(bb->blocks, sample), sps::kBlock, 0, bb->st>>>(A, G);
@@ -738,7 +833,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     const int64_t W = b->opt.check_interval > 0 ? b->opt.check_interval : 64;
     const uint64_t tl = b->opt.time_limit_s > 0 ? (uint64_t)(b->opt.time_limit_s * 1e9) : 0;
     sps::batch::Args A{b->d_inst, b->d_order, b->count, (int32_t)W, b->opt.max_iters, b->opt.tol, b->d_deadline,
-                       b->arr, b->d_out, b->d_counter};
+                       b->arr, b->d_out, b->d_counter, b->opt.escalate != 0 ? 1 : 0};
     auto enqueue = [&](cudaStream_t s) {
         cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
         sps::batch::k_set_deadline<<<1, 32, 0, s>>>(b->d_deadline, tl);
@@ -784,14 +879,28 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     SPB_CK(cudaStreamSynchronize(b->st));
     float ms = 0;
     cudaEventElapsedTime(&ms, b->e0, b->e1);
-    b->solve_ms = ms;
+    b->escalated.assign(b->count, 0);
+    int32_t n_esc = 0;
+    double esc_ms = 0.0;
+    if (b->opt.escalate == 1) {
+        const auto t0 = std::chrono::steady_clock::now();
+        for (int32_t k = 0; k < b->count; ++k) {
+            if (b->out[k].status != SPS_STATUS_STALLED) continue;
+            const double used = ms * 1e-3 + std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (int rc = continue_fp64(b, k, used)) return rc;
+            ++n_esc;
+        }
+        esc_ms = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    b->solve_ms = ms + esc_ms;
     b->solved = true;
     if (stats) {
         std::memset(stats, 0, sizeof(*stats));
         stats->setup_ms = b->setup_ms;
-        stats->solve_ms = ms;
+        stats->solve_ms = b->solve_ms;
         stats->lanes_per_column = b->G;
         stats->blocks = b->blocks;
+        stats->escalated = n_esc;
         for (const Ctl& c : b->out) {
             stats->total_iterations += c.iters;
             if (c.status == SPS_STATUS_OPTIMAL) stats->optimal += 1;
@@ -831,6 +940,7 @@ extern "C" int sps_batch_get(sps_batch* b, int32_t k, double* x, double* y, sps_
         res->solve_ms = b->solve_ms;
         res->kernel_launches = 1;
         res->returned_average = c.choice;
+        res->escalated = b->escalated[k];
     }
     return SPS_OK;
 }

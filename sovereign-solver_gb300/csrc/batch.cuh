@@ -33,6 +33,7 @@ struct Arrays {
     const double *eta0, *omega0;
     float *x0, *x1, *aty0, *aty1, *xs, *xl, *atya;
     float *y0, *y1, *ax0, *ax1, *ys, *yl, *axa;
+    float *xb, *yb;           // best point of the stall test (null when it is off)
 };
 
 struct Args {
@@ -46,6 +47,7 @@ struct Args {
     Arrays a;
     Ctl* out;                 // per instance final state
     uint32_t* counter;
+    int32_t stall_on;         // stall test on (FP64 continuation on the host)
 };
 
 // ---------------------------------------------------------------------------

@@ -8,7 +8,13 @@
 
 namespace sps {
 
-enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4, AP_STEP_PENDING = 8 };
+enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4, AP_STEP_PENDING = 8,
+                 AP_SAVE_BEST = 16,   // copy the best point of this check to xb / yb
+                 AP_SAVE_AVG = 32 };  // ... and that point is the average
+
+// Stall test: the best relative KKT error has not halved for
+// max(kStallMin, anchor / 2) attempts, anchor = attempt of the last halving.
+constexpr int64_t kStallMin = 2048;
 
 // Adaptive step (PDLP): limit = ||dz||_w^2 / (2 |dy^T K dx|); the attempt is
 // accepted if eta <= limit; next eta = min((1 - (k+1)^-0.3) limit, (1 + (k+1)^-0.6) eta).
@@ -47,7 +53,11 @@ __device__ __forceinline__ bool decide_step(Ctl& c, double dy2, double inter_sig
 // Termination on the relative KKT error of the original problem; restart on the
 // weighted KKT of the scaled problem (to the better of average and current) when
 // it dropped below 0.2x the last restart's, or below 0.8x while rising, or after
-// 0.36x of all attempts; primal weight updated at restarts.  Sets c.apply.
+// 0.36x of all attempts; primal weight updated at restarts.  With c.stall_on the
+// best point of every check that improves on all earlier ones is marked for
+// copying (AP_SAVE_BEST, with the primal weight in c.omega_best) and the solve
+// finishes with SPS_STATUS_STALLED when the best error stops halving (FP32
+// precision floor; the host continues in FP64 from the saved point).  Sets c.apply.
 __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], const double (&tr)[8], double inv_nb,
                                              double inv_nc, bool stop) {
     const bool has_avg = c.w_sum > 0.0;
@@ -69,6 +79,9 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], con
     c.last_cur_kkt = rel[1];
     if (c.init_phase) {
         c.init_phase = 0;
+        c.anchor_rel = rel[1];
+        c.anchor_iter = 0;
+        c.best_rel = INFINITY;
         c.kkt_last = kw[1];
         c.kkt_prev_cand = kw[1];
         c.rel_kkt = rel[1]; c.rel_p = rp[1]; c.rel_d = rd[1]; c.rel_gap = gp[1];
@@ -78,6 +91,23 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], con
     }
     const int best = (has_avg && rel[0] < rel[1]) ? 0 : 1;
     const bool bad = !isfinite(rel[1]) && !(has_avg && isfinite(rel[0]));
+    bool stalled = false;
+    int save = 0;
+    if (c.stall_on && !bad) {
+        const double r = rel[best];
+        if (r < c.best_rel) {
+            c.best_rel = r;
+            c.omega_best = w;
+            c.best_saved = 1;
+            save = AP_SAVE_BEST | (best == 0 ? AP_SAVE_AVG : 0);
+        }
+        if (r <= 0.5 * c.anchor_rel) {
+            c.anchor_rel = r;
+            c.anchor_iter = c.iters;
+        } else if (c.iters - c.anchor_iter >= (c.anchor_iter / 2 > kStallMin ? c.anchor_iter / 2 : kStallMin)) {
+            stalled = true;
+        }
+    }
     bool finish = false;
     if (bad) {
         c.status = SPS_STATUS_NUMERIC_ERROR; finish = true;
@@ -87,13 +117,15 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], con
         c.status = SPS_STATUS_ITERATION_LIMIT; finish = true;
     } else if (stop) {
         c.status = SPS_STATUS_TIME_LIMIT; finish = true;
+    } else if (stalled) {
+        c.status = SPS_STATUS_STALLED; finish = true;
     }
     if (finish) {
         c.done = 1;
         c.choice = best == 0 ? 1 : 0;
         c.rel_kkt = rel[best]; c.rel_p = rp[best]; c.rel_d = rd[best]; c.rel_gap = gp[best];
         c.pobj = po[best]; c.dobj = dob[best];
-        c.apply = best == 0 ? AP_LOAD_AVG : 0;
+        c.apply = (best == 0 ? AP_LOAD_AVG : 0) | save;
         return;
     }
     const int cand = (has_avg && kw[0] < kw[1]) ? 0 : 1;
@@ -115,7 +147,7 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], con
         c.last_restart_iter = c.iters;
         apply = AP_RESTART | AP_CANDIDATE | (cand == 0 ? AP_LOAD_AVG : 0);
     }
-    c.apply = apply;
+    c.apply = apply | save;
 }
 
 }  // namespace sps

@@ -95,6 +95,13 @@ struct Ctl {
     uint32_t ticket[8];      // last-block tickets, one per kernel kind
     int32_t abort_seen;
     int32_t windows;         // window bodies executed (loop guard)
+    // stall test (adaptive FP32 with escalation)
+    int32_t stall_on;        // 1: finish with SPS_STATUS_STALLED when the best error stops halving
+    int32_t best_saved;      // 1 once a best point has been copied to xb / yb
+    int64_t anchor_iter;     // attempt at which the best error last halved
+    double anchor_rel;       // best error at that attempt
+    double best_rel;         // best relative KKT error seen at a check
+    double omega_best;       // primal weight when the best point was taken
 };
 
 enum TicketSlot { T_ROW_STEP = 0, T_COL_STEP, T_ROW_CHECK, T_COL_CHECK, T_APPLY, T_AUX0, T_AUX1, T_AUX2 };

@@ -48,6 +48,10 @@ struct EngineBase {
     virtual int warm(const double* x0, const double* y0, double omega0) = 0;
     virtual int get(double* x, double* y) = 0;
     virtual int time_kernels(int reps, double* out) = 0;
+    // Best point of the last solve's stall test in the caller's space, and the
+    // primal weight it was taken with (the returned point when none was saved).
+    virtual int get_best(double* x, double* y, double* omega) = 0;
+    virtual void set_limits(int64_t max_iters, double time_limit_s) = 0;
     std::string err;
     int fail(int code, const std::string& msg) { err = msg; return code; }
 };
@@ -339,6 +343,7 @@ struct Engine : EngineBase {
         uint32_t* d_tickets;
         V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
         V *xs, *ys, *xl = nullptr, *yl = nullptr, *AXa = nullptr, *ATYa = nullptr, *xbar = nullptr;
+        V *xb = nullptr, *yb = nullptr;
 
         // uniform bounds: every column [L, U] with L in {0, -inf}, U = +inf
         bool uniform = true;
@@ -383,6 +388,7 @@ struct Engine : EngineBase {
             add(&ATY0, sizeof(V) * n); add(&ATY1, sizeof(V) * n);
             add(&xl, sizeof(V) * n); add(&yl, sizeof(V) * m);
             add(&AXa, sizeof(V) * m); add(&ATYa, sizeof(V) * n);
+            if (stall_test()) { add(&xb, sizeof(V) * n); add(&yb, sizeof(V) * m); }
         } else {
             add(&xbar, sizeof(V) * n);
             add(&d_tau, sizeof(V) * n);
@@ -564,6 +570,7 @@ struct Engine : EngineBase {
         a.X[0] = X0; a.X[1] = X1; a.Y[0] = Y0; a.Y[1] = Y1;
         a.AX[0] = AX0; a.AX[1] = AX1; a.ATY[0] = ATY0; a.ATY[1] = ATY1;
         a.xs = xs; a.ys = ys; a.xl = xl; a.yl = yl; a.AXa = AXa; a.ATYa = ATYa; a.xbar = xbar;
+        a.xb = xb; a.yb = yb;
         a.part_row = d_pr; a.part_col = d_pc; a.part_aux = d_pa;
         a.ctl = d_ctl;
         a.abort_flag = d_abort;
@@ -715,6 +722,7 @@ struct Engine : EngineBase {
         c0.eta = eta0;
         c0.omega = (adaptive && warm_omega > 0) ? warm_omega : omega0;
         c0.kkt_last = INFINITY;
+        c0.stall_on = stall_test() ? 1 : 0;
         *h_ctl = c0;
         *(volatile int32_t*)h_abort = 0;
         launches = 0;
@@ -890,6 +898,34 @@ struct Engine : EngineBase {
         out[0] = row / reps;
         out[1] = col / reps;
         out[2] = mode == SPS_MODE_ADAPTIVE ? double(after.accepted_total - saved.accepted_total) / reps : 1.0;
+        return SPS_OK;
+    }
+
+    // The stall test runs for adaptive FP32 solves unless escalation is off.
+    bool stall_test() const { return mode == SPS_MODE_ADAPTIVE && sizeof(V) == 4 && opt.escalate != 0; }
+
+    void set_limits(int64_t max_iters, double time_limit_s) override {
+        opt.max_iters = max_iters;
+        opt.time_limit_s = time_limit_s;
+    }
+
+    int get_best(double* x, double* y, double* omega) override {
+        if (!solved) return fail(SPS_ERR_STATE, "no solution: call sps_solve first");
+        if (trivial || !args.xb || !h_ctl->best_saved) {
+            *omega = h_ctl->omega;
+            return get(x, y);
+        }
+        SPS_CK(cudaSetDevice(opt.device));
+        k_extract<V><<<args.apply_blocks, kBlock, 0, st>>>(args.xb, args.yb, args.dc, args.dr, d_perm_col,
+                                                           d_perm_row, d_xout, d_yout, n, m);
+        SPS_CK(cudaGetLastError());
+        std::vector<double> xo(n), yo(m);
+        SPS_CK(cudaMemcpyAsync(xo.data(), d_xout, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaMemcpyAsync(yo.data(), d_yout, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        SPS_CK(cudaStreamSynchronize(st));
+        for (int j = 0; j < n_user; ++j) x[j] = std::min(std::max(xo[j], lb_user[j]), ub_user[j]);
+        for (int i = 0; i < m_user; ++i) y[i] = yo[i];
+        *omega = h_ctl->omega_best;
         return SPS_OK;
     }
 

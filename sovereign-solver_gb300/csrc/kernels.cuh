@@ -40,6 +40,7 @@ struct Args {
     double inv_nb, inv_nc;     // normalisers of the reported relative error
     V* X[2]; V* Y[2]; V* AX[2]; V* ATY[2];
     V* xs; V* ys; V* xl; V* yl; V* AXa; V* ATYa; V* xbar;
+    V* xb; V* yb;              // best point of the stall test (null unless it is on)
     double* part_row; double* part_col; double* part_aux;
     Ctl* ctl;
     const volatile int32_t* abort_flag;
@@ -142,11 +143,12 @@ template <class V>
 struct AdColStepEpi {
     const Args<V>* a;
     const V *xc, *cc, *atyo;
+    const V* xl;
     V *aty, *xn, *xs;
     V tau, wgt;
     bool accepted;
     V dx2 = V(0);
-    struct Pre { V xj, cj, lo, hi, s; };
+    struct Pre { V xj, cj, lo, hi, s, l; };
     static constexpr int NP = 1;
     __device__ __forceinline__ void zero() { dx2 = V(0); }
     __device__ __forceinline__ void export_to(double* d) const { d[0] = double(dx2); }
@@ -157,10 +159,11 @@ struct AdColStepEpi {
         p.lo = lo_at(*a, j);
         p.hi = hi_at(*a, j);
         p.s = accepted ? xs[j] : V(0);
+        p.l = accepted ? xl[j] : V(0);
         return p;
     }
     __device__ __forceinline__ void finish(int j, V atyj, const Pre& p) {
-        if (accepted) { aty[j] = atyj; xs[j] = p.s + wgt * p.xj; }
+        if (accepted) { aty[j] = atyj; xs[j] = p.s + wgt * (p.xj - p.l); }
         const V x2 = clampv(p.xj - tau * (p.cj - atyj), p.lo, p.hi);
         xn[j] = x2;
         const V d = x2 - p.xj;
@@ -177,7 +180,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     __shared__ bool last;
     const int cur = ctl->cur;
     const bool acc = ctl->accepted;
-    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.ATY[cur], a.X[1 - cur], a.xs,
+    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.xl, a.ATY[cur], a.X[1 - cur], a.xs,
                       V(ctl->eta / ctl->omega), V(ctl->eta_used), acc};
     const int colblocks = a.cols.total_blocks;
     if ((int)blockIdx.x < colblocks) {
@@ -191,7 +194,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
         const V wgt = V(ctl->eta_used);
         const V* yc = a.Y[cur];
         for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
-            a.ys[i] += wgt * yc[i];
+            a.ys[i] += wgt * (yc[i] - a.yl[i]);
     }
     double v[1] = {double(e.dx2)};
     if (!publish_partials<1>(v, a.part_col, &ctl->ticket[T_COL_STEP], sm, &last)) return;
@@ -205,21 +208,32 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
 }
 
 // ---- checks -----------------------------------------------------------------
-// Point 0 = weighted average (x_sum / w_sum), point 1 = current iterate.
+// Point 0 = weighted average, point 1 = current iterate.  The average is kept
+// as an offset from the restart point: x_avg = x_last + x_sum / w_sum with
+// x_sum = sum of w_k (x_k - x_last).  Near convergence the offsets are small,
+// so FP32 sums keep the average accurate where a plain FP32 sum of w_k x_k
+// loses the last digits and stalls the restarts.  With no average yet point 0
+// aliases the current iterate (s = current, l = null, inv_w = 1).
+
+template <class V>
+__device__ __forceinline__ double avg_at(const V* s, const V* l, double inv_w, int j) {
+    const double v = double(__ldg(s + j)) * inv_w;
+    return l ? v + double(__ldg(l + j)) : v;
+}
 
 template <class V>
 struct GatherTwo {
-    const V *s, *x;
+    const V *s, *l, *x;
     double inv_w;
     __device__ __forceinline__ double operator()(int q, int j) const {
-        return q == 0 ? double(__ldg(s + j)) * inv_w : double(__ldg(x + j));
+        return q == 0 ? avg_at(s, l, inv_w, j) : double(__ldg(x + j));
     }
 };
 
 template <class V>
 struct AdRowCheckEpi {
     const Args<V>* a;
-    const V *ys, *yc, *yl;
+    const V *ys, *ylb, *yc, *yl;
     V* axa;
     double inv_w;
     double p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // per point q: res_scaled^2, res_orig^2, b^T y, ||y - y_last||^2
@@ -238,7 +252,7 @@ struct AdRowCheckEpi {
             p[4 * q + 0] += res * res;
             const double ro = res / dr;
             p[4 * q + 1] += ro * ro;
-            const double yv = q == 0 ? double(ys[r]) * inv_w : double(yc[r]);
+            const double yv = q == 0 ? avg_at(ys, ylb, inv_w, r) : double(yc[r]);
             p[4 * q + 2] += br * yv;
             const double d = yv - double(yl[r]);
             p[4 * q + 3] += d * d;
@@ -255,8 +269,8 @@ SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
     // with no average yet, point 0 aliases the current iterate
     const bool has_avg = ctl->w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
-    GatherTwo<V> g{has_avg ? a.xs : a.X[cur], a.X[cur], inv_w};
-    AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], a.Y[cur], a.yl, a.AXa, inv_w};
+    GatherTwo<V> g{has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], inv_w};
+    AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], a.yl, a.AXa, inv_w};
     visit_bins<2, double>(a.rows, blockIdx.x, a.csr, g, e);
     block_sum<8>(e.p, sm);
     if (threadIdx.x == 0)
@@ -266,7 +280,7 @@ SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
 template <class V>
 struct AdColCheckEpi {
     const Args<V>* a;
-    const V *xs, *xc, *xl;
+    const V *xs, *xlb, *xc, *xl;
     V* atya;
     double inv_w;
     double p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // per point: dres_s^2, dres_o^2, c^T x, bound terms, ||x - x_last||^2
@@ -288,7 +302,7 @@ struct AdColCheckEpi {
             p[5 * q + 0] += dres * dres;
             const double dor = dres / dc;
             p[5 * q + 1] += dor * dor;
-            const double xv = q == 0 ? double(xs[j]) * inv_w : double(xc[j]);
+            const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
             p[5 * q + 2] += cj * xv;
             p[5 * q + 3] += (hl ? lo * fmax(lam, 0.0) : 0.0) + (hh ? hi * fmin(lam, 0.0) : 0.0);
             const double d = xv - double(xl[j]);
@@ -306,8 +320,8 @@ SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     const int cur = ctl->cur;
     const bool has_avg = ctl->w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
-    GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], a.Y[cur], inv_w};
-    AdColCheckEpi<V> e{&a, has_avg ? a.xs : a.X[cur], a.X[cur], a.xl, a.ATYa, inv_w};
+    GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], inv_w};
+    AdColCheckEpi<V> e{&a, has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], a.xl, a.ATYa, inv_w};
     visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e);
     if (!publish_partials<10>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
     double tc[10], tr[8];
@@ -329,14 +343,16 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
     if (ap != 0 && ap != AP_STEP_PENDING) {
         const int cur = ctl->cur;
         const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !ctl->done;
+        const bool save = (ap & AP_SAVE_BEST) && a.xb, save_avg = ap & AP_SAVE_AVG;
         const double inv_w = ctl->w_sum > 0.0 ? 1.0 / ctl->w_sum : 0.0;
         const V tau = V(ctl->eta / ctl->omega);
         V dx2 = V(0);
         const int stride = gridDim.x * kBlock;
         for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += stride) {
+            if (save) a.xb[j] = save_avg ? V(double(a.xl[j]) + double(a.xs[j]) * inv_w) : a.X[cur][j];
             V xv;
             if (load) {
-                xv = V(double(a.xs[j]) * inv_w);
+                xv = V(double(a.xl[j]) + double(a.xs[j]) * inv_w);
                 a.X[cur][j] = xv;
                 a.ATY[cur][j] = a.ATYa[j];
             } else {
@@ -351,9 +367,10 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
             }
         }
         for (int i = blockIdx.x * kBlock + threadIdx.x; i < a.m; i += stride) {
+            if (save) a.yb[i] = save_avg ? V(double(a.yl[i]) + double(a.ys[i]) * inv_w) : a.Y[cur][i];
             V yv;
             if (load) {
-                yv = V(double(a.ys[i]) * inv_w);
+                yv = V(double(a.yl[i]) + double(a.ys[i]) * inv_w);
                 a.Y[cur][i] = yv;
                 a.AX[cur][i] = a.AXa[i];
             } else {

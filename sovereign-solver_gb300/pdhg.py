@@ -90,11 +90,16 @@ class _Desc:
 
 def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, tol=PDHG_TOL,
                  check_interval=0, ruiz_iters=10, time_limit=0.0, graph_mode=2, device=0,
-                 max_blocks=0) -> N.Options:
+                 max_blocks=0, escalate="fp64") -> N.Options:
+    """Options for ``sps_create``.  ``escalate`` (adaptive FP32): "fp64" continues a
+    stalled solve in FP64 from its best point, "stop" ends it with status
+    "stalled", "off" keeps iterating in FP32."""
     if mode not in N.MODES:
         raise ValueError(f"Unknown mode {mode!r}. Choose 'adaptive' or 'reference'.")
     if precision not in N.PRECISIONS:
         raise ValueError(f"Unknown precision {precision!r}. Choose 'fp32' or 'fp64'.")
+    if escalate not in N.ESCALATE:
+        raise ValueError(f"Unknown escalate {escalate!r}. Choose 'fp64', 'stop' or 'off'.")
     o = N.Options()
     N.load().sps_options_init(C.byref(o))
     o.mode, o.precision = N.MODES[mode], N.PRECISIONS[precision]
@@ -102,6 +107,7 @@ def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, to
     o.check_interval, o.ruiz_iters = int(check_interval), int(ruiz_iters)
     o.time_limit_s, o.graph_mode, o.device = float(time_limit), int(graph_mode), int(device)
     o.max_blocks = int(max_blocks)
+    o.escalate = N.ESCALATE[escalate]
     return o
 
 
@@ -181,6 +187,7 @@ def to_result(problem, r: N.Result, x, y, mode, precision) -> SolveResult:
         "primal_weight": float(r.primal_weight), "step_size": float(r.step_size),
         "setup_ms": float(r.setup_ms), "solve_ms": float(r.solve_ms),
         "kernel_launches": int(r.kernel_launches), "returned_average": bool(r.returned_average),
+        "escalated": bool(r.escalated),
     }
     msg = f"{mode}/{precision} PDHG on GPU: rel_kkt={r.rel_kkt:.3e}"
     return SolveResult(status, x, obj, int(r.iterations), message=msg, y=y,
@@ -190,15 +197,17 @@ def to_result(problem, r: N.Result, x, y, mode, precision) -> SolveResult:
 def solve_lp_pdhg(problem, max_iters: int = MAX_PDHG_ITERS, tol: float = PDHG_TOL, *,
                   mode: str = "adaptive", precision: str = "fp32", warm_start=None,
                   time_limit: float = 0.0, graph_mode: int = 2, check_interval: int = 0,
-                  device: int = 0) -> SolveResult:
+                  device: int = 0, escalate: str = "fp64") -> SolveResult:
     """Solve an LP with restarted PDHG on the GPU (``solver/lp/pdhg.py:152``).
 
     ``warm_start`` = (x0, y0, omega0) starts from a given point (adaptive mode).
-    Non-convergence is not an error: status ``"iteration_limit"``.
+    Non-convergence is not an error: status ``"iteration_limit"``.  With FP32
+    iterates a solve whose error stops halving continues in FP64 from its best
+    point (``escalate="fp64"``; ``stats["escalated"]`` tells).
     """
     with PDHGEngine(problem, mode=mode, precision=precision, max_iters=max_iters, tol=tol,
                     time_limit=time_limit, graph_mode=graph_mode, check_interval=check_interval,
-                    device=device) as eng:
+                    device=device, escalate=escalate) as eng:
         if warm_start is not None:
             x0, y0, w0 = (tuple(warm_start) + (None, None, 0.0))[:3]
             eng.warm_start(x0, y0, w0 or 0.0)
