@@ -184,7 +184,9 @@ int sps_batch_create(int32_t count, const sps_problem_desc *probs, const sps_opt
 /* Solve every instance: one persistent launch, captured in a CUDA graph on the
  * first call and replayed afterwards; blocking. */
 int sps_batch_solve(sps_batch *b, sps_batch_stats *stats);
-/* Instance k of the last solve: x (n, clipped to bounds), y (m_ub + m_eq), result. */
+/* Instance k of the last solve: x (n, clipped to bounds), y (m_ub + m_eq), result.
+ * res->solve_ms is the instance's own device time inside the persistent launch
+ * (plus its FP64 continuation, if any); setup_ms is the batch's. */
 int sps_batch_get(sps_batch *b, int32_t k, double *x, double *y, sps_result *res);
 const char *sps_batch_last_error(const sps_batch *b);
 void sps_batch_destroy(sps_batch *b);

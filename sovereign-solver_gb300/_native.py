@@ -13,6 +13,7 @@ from . import _build
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
+_f32p = C.POINTER(C.c_float)
 
 ERRORS = {
     -1: "SPS_ERR_INVALID",
@@ -73,6 +74,23 @@ class DeviceLP(C.Structure):
     ]
 
 
+class GnnGraph(C.Structure):
+    _fields_ = [
+        ("n_var", C.c_int32), ("n_con", C.c_int32),
+        ("con_ptr", _i32p), ("con_idx", _i32p), ("con_val", C.POINTER(C.c_float)),
+        ("f_var", C.c_int32), ("f_con", C.c_int32),
+    ]
+
+
+class GnnOptions(C.Structure):
+    _fields_ = [
+        ("hidden", C.c_int32), ("layers", C.c_int32), ("seed", C.c_uint64),
+        ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
+        ("loss_x", C.c_float), ("loss_y", C.c_float), ("loss_omega", C.c_float),
+        ("max_batch", C.c_int32), ("device", C.c_int32), ("reserved", C.c_int32 * 6),
+    ]
+
+
 _lib = None
 
 
@@ -111,6 +129,16 @@ def load() -> C.CDLL:
         "sps_batch_get": (C.c_int, [H, C.c_int32, _f64p, _f64p, C.POINTER(Result)]),
         "sps_batch_last_error": (C.c_char_p, [H]),
         "sps_batch_destroy": (None, [H]),
+        "sps_gnn_options_init": (C.c_int, [C.POINTER(GnnOptions)]),
+        "sps_gnn_create": (C.c_int, [C.POINTER(GnnGraph), C.POINTER(GnnOptions), C.POINTER(H)]),
+        "sps_gnn_predict": (C.c_int, [H, C.c_int32, _f32p, _f32p, _f32p, _f32p, _f32p]),
+        "sps_gnn_loss_grad": (C.c_int, [H, C.c_int32, _f32p, _f32p, _f32p, _f32p, _f32p, _f64p, _f32p]),
+        "sps_gnn_train_step": (C.c_int, [H, C.c_int32, _f32p, _f32p, _f32p, _f32p, _f32p, _f64p]),
+        "sps_gnn_num_params": (C.c_int64, [H]),
+        "sps_gnn_get_params": (C.c_int, [H, _f32p]),
+        "sps_gnn_set_params": (C.c_int, [H, _f32p]),
+        "sps_gnn_last_error": (C.c_char_p, [H]),
+        "sps_gnn_destroy": (None, [H]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -132,6 +160,10 @@ def check(rc: int, handle=None) -> None:
 
 def f64p(a):
     return a.ctypes.data_as(_f64p) if a is not None and a.size else None
+
+
+def f32p(a):
+    return a.ctypes.data_as(_f32p) if a is not None and a.size else None
 
 
 def i32p(a):

@@ -255,6 +255,7 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
         c.omega = A.a.omega0[k];
         c.kkt_last = INFINITY;
         c.stall_on = A.stall_on;
+        c.t_begin = global_ns();
     }
     for (int j = threadIdx.x; j < v.n; j += kBlock) {
         const float x = fminf(fmaxf(0.f, v.lo[j]), v.hi[j]);
@@ -306,7 +307,10 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
         check_and_apply(v, I, c, sm, A.deadline);
         if (c.done) break;
     }
-    if (threadIdx.x == 0) A.out[k] = c;
+    if (threadIdx.x == 0) {
+        c.t_end = global_ns();
+        A.out[k] = c;
+    }
 }
 
 __global__ void __launch_bounds__(kBlock) k_batch_solve(Args A, int G) {
@@ -468,6 +472,7 @@ struct sps_batch {
     std::vector<double> xo, yo;
     std::vector<Ctl> out;
     std::vector<int8_t> escalated;
+    std::vector<double> esc_ms;             // wall time of each instance's FP64 continuation
     cudaGraphExec_t gexec = nullptr;
     int32_t gexec_G = -1;
     uint64_t gexec_tl = 0;
@@ -880,14 +885,17 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     float ms = 0;
     cudaEventElapsedTime(&ms, b->e0, b->e1);
     b->escalated.assign(b->count, 0);
+    b->esc_ms.assign(b->count, 0.0);
     int32_t n_esc = 0;
     double esc_ms = 0.0;
     if (b->opt.escalate == 1) {
         const auto t0 = std::chrono::steady_clock::now();
         for (int32_t k = 0; k < b->count; ++k) {
             if (b->out[k].status != SPS_STATUS_STALLED) continue;
-            const double used = ms * 1e-3 + std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            const auto t1 = std::chrono::steady_clock::now();
+            const double used = ms * 1e-3 + std::chrono::duration<double>(t1 - t0).count();
             if (int rc = continue_fp64(b, k, used)) return rc;
+            b->esc_ms[k] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
             ++n_esc;
         }
         esc_ms = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -937,7 +945,7 @@ extern "C" int sps_batch_get(sps_batch* b, int32_t k, double* x, double* y, sps_
         res->primal_weight = c.omega;
         res->step_size = c.eta;
         res->setup_ms = b->setup_ms;
-        res->solve_ms = b->solve_ms;
+        res->solve_ms = 1e-6 * double(c.t_end - c.t_begin) + (b->escalated[k] ? b->esc_ms[k] : 0.0);
         res->kernel_launches = 1;
         res->returned_average = c.choice;
         res->escalated = b->escalated[k];

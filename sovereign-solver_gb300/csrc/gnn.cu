@@ -1,0 +1,880 @@
+// gnn.cu — the learned warm start's network (sps_gnn_* in include/sps_gnn.h):
+// forward, hand-written backward, loss and Adam, all as CUDA kernels.
+//
+// Activations are kept per instance and node, row-major with the hidden width
+// innermost ([instance][node][H], FP32), so every per-node kernel runs over the
+// flattened node list of the whole batch and the weight gradients are sums
+// over it.  Aggregations are CSR SpMMs (warp per destination row, float2 per
+// lane); the dense node updates stage 32 nodes and both 64x64 weight matrices
+// in shared memory (BF16 weights widened to FP32, FP32 accumulation).  Every
+// reduction (weight gradients, losses, pooling) writes per-block partials that
+// a second kernel sums in block order: training is bitwise reproducible.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sps_gnn.h"
+
+namespace {
+
+constexpr int kT = 256;          // threads per block
+constexpr int kTile = 32;        // nodes per tile in the dense kernels
+constexpr int kMaxF = 8;         // input feature width limit
+
+__device__ __forceinline__ float relu(float v) { return v > 0.f ? v : 0.f; }
+
+// ---- input layer: h = relu(W f + b), W is H x F ------------------------------------
+template <int H>
+__global__ void __launch_bounds__(kT) k_input(const float* __restrict__ f, int64_t nodes, int F,
+                                              const __nv_bfloat16* __restrict__ W, const float* __restrict__ bias,
+                                              float* __restrict__ h) {
+    const int64_t total = nodes * H;
+    for (int64_t t = blockIdx.x * (int64_t)kT + threadIdx.x; t < total; t += (int64_t)gridDim.x * kT) {
+        const int64_t v = t / H;
+        const int o = int(t % H);
+        float acc = bias[o];
+        for (int q = 0; q < F; ++q) acc += __bfloat162float(W[o * F + q]) * f[v * F + q];
+        h[t] = relu(acc);
+    }
+}
+
+// ---- aggregation: out[s, r] (+)= sum_k val[k] * in[s, idx[k]] ----------------------
+// One warp per destination row of one instance; lane l owns features 2l, 2l+1
+// (H = 64) or l (H = 32).
+template <int H>
+__global__ void __launch_bounds__(kT) k_agg(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
+                                            const float* __restrict__ val, const float* __restrict__ in,
+                                            float* __restrict__ out, int n_dst, int n_src, int batch, int accumulate) {
+    const int lane = threadIdx.x & 31;
+    const int64_t rows = (int64_t)n_dst * batch;
+    for (int64_t w = (blockIdx.x * (int64_t)kT + threadIdx.x) >> 5; w < rows; w += ((int64_t)gridDim.x * kT) >> 5) {
+        const int64_t s = w / n_dst;
+        const int r = int(w % n_dst);
+        const float* src = in + s * (int64_t)n_src * H;
+        const int b = ptr[r], e = ptr[r + 1];
+        if (H == 64) {
+            float2 acc = make_float2(0.f, 0.f);
+            int k = b;
+            for (; k + 4 <= e; k += 4) {
+                float2 v[4];
+                float a[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    a[u] = __ldg(val + k + u);
+                    v[u] = __ldg(reinterpret_cast<const float2*>(src + (int64_t)__ldg(idx + k + u) * H) + lane);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) { acc.x += a[u] * v[u].x; acc.y += a[u] * v[u].y; }
+            }
+            for (; k < e; ++k) {
+                const float a = __ldg(val + k);
+                const float2 v = __ldg(reinterpret_cast<const float2*>(src + (int64_t)__ldg(idx + k) * H) + lane);
+                acc.x += a * v.x;
+                acc.y += a * v.y;
+            }
+            float2* o = reinterpret_cast<float2*>(out + w * H) + lane;
+            if (accumulate) { const float2 p = *o; acc.x += p.x; acc.y += p.y; }
+            *o = acc;
+        } else {
+            float acc = 0.f;
+            for (int k = b; k < e; ++k) acc += __ldg(val + k) * __ldg(src + (int64_t)__ldg(idx + k) * H + lane);
+            float* o = out + w * H + lane;
+            if (accumulate) acc += *o;
+            *o = acc;
+        }
+    }
+}
+
+// ---- dense node update: out = relu(U h + M a + b) ---------------------------------
+// A block stages U^T and M^T (FP32) and a tile of 32 nodes (h | a, padded rows);
+// thread t computes node t / 8, outputs (t % 8) + 8 i.
+template <int H>
+__global__ void __launch_bounds__(kT) k_update(const float* __restrict__ h, const float* __restrict__ a,
+                                               const __nv_bfloat16* __restrict__ U,
+                                               const __nv_bfloat16* __restrict__ M, const float* __restrict__ bias,
+                                               float* __restrict__ out, int64_t nodes) {
+    constexpr int OP = H / 8;                 // outputs per thread
+    constexpr int XS = 2 * H + 1;             // padded tile row
+    extern __shared__ float sm[];
+    float* Ut = sm;                           // [k][o]
+    float* Mt = Ut + H * H;
+    float* X = Mt + H * H;                    // [kTile][XS]
+    for (int t = threadIdx.x; t < H * H; t += kT) {
+        const int o = t / H, k = t % H;
+        Ut[k * H + o] = __bfloat162float(U[t]);
+        Mt[k * H + o] = __bfloat162float(M[t]);
+    }
+    const int node = threadIdx.x >> 3, g = threadIdx.x & 7;
+    float bo[OP];
+#pragma unroll
+    for (int i = 0; i < OP; ++i) bo[i] = bias[g + 8 * i];
+    const int64_t tiles = (nodes + kTile - 1) / kTile;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int64_t base = tile * kTile;
+        __syncthreads();
+        for (int t = threadIdx.x; t < kTile * H; t += kT) {
+            const int nd = t / H, k = t % H;
+            const int64_t v = base + nd;
+            X[nd * XS + k] = v < nodes ? h[v * H + k] : 0.f;
+            X[nd * XS + H + k] = v < nodes ? a[v * H + k] : 0.f;
+        }
+        __syncthreads();
+        float acc[OP];
+#pragma unroll
+        for (int i = 0; i < OP; ++i) acc[i] = bo[i];
+        const float* x = X + node * XS;
+        for (int k = 0; k < H; ++k) {
+            const float xh = x[k], xa = x[H + k];
+#pragma unroll
+            for (int i = 0; i < OP; ++i) acc[i] += Ut[k * H + g + 8 * i] * xh + Mt[k * H + g + 8 * i] * xa;
+        }
+        const int64_t v = base + node;
+        if (v < nodes) {
+#pragma unroll
+            for (int i = 0; i < OP; ++i) out[v * H + g + 8 * i] = relu(acc[i]);
+        }
+    }
+}
+
+// ---- heads: out[v] = w . h[v] + b (warp per node) ----------------------------------
+template <int H>
+__global__ void __launch_bounds__(kT) k_head(const float* __restrict__ h, const __nv_bfloat16* __restrict__ w,
+                                             const float* __restrict__ b, float* __restrict__ out, int64_t nodes) {
+    const int lane = threadIdx.x & 31;
+    float w0 = __bfloat162float(w[lane]), w1 = H == 64 ? __bfloat162float(w[lane + 32]) : 0.f;
+    for (int64_t v = (blockIdx.x * (int64_t)kT + threadIdx.x) >> 5; v < nodes; v += ((int64_t)gridDim.x * kT) >> 5) {
+        float s = h[v * H + lane] * w0;
+        if (H == 64) s += h[v * H + lane + 32] * w1;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) out[v] = s + b[0];
+    }
+}
+
+// ---- per-instance column sums of h over nodes (pooling), block partials ------------
+// part[(s * nb + blk) * H + f] over node chunks of instance s (grid.y = instance).
+template <int H>
+__global__ void __launch_bounds__(kT) k_colsum_part(const float* __restrict__ h, int n, float* __restrict__ part) {
+    const int s = blockIdx.y, f = threadIdx.x % H, lanes = kT / H, sub = threadIdx.x / H;
+    __shared__ float red[kT];
+    float acc = 0.f;
+    for (int64_t v = blockIdx.x * (int64_t)lanes + sub; v < n; v += (int64_t)gridDim.x * lanes)
+        acc += h[((int64_t)s * n + v) * H + f];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    if (sub == 0) {
+        for (int q = 1; q < lanes; ++q) acc += red[q * H + f];
+        part[((int64_t)s * gridDim.x + blockIdx.x) * H + f] = acc;
+    }
+}
+
+// pool[s][0:H] = mean over constraints, pool[s][H:2H] = mean over variables;
+// log_omega[s] = wo . pool + bo
+template <int H>
+__global__ void k_pool_finish(const float* __restrict__ pc, int nbc, const float* __restrict__ pv, int nbv, int m,
+                              int n, const __nv_bfloat16* __restrict__ wo, const float* __restrict__ bo,
+                              float* __restrict__ pool, float* __restrict__ lw) {
+    const int s = blockIdx.x, f = threadIdx.x;
+    __shared__ float red[2 * H];
+    if (f < 2 * H) {
+        float acc = 0.f;
+        if (f < H) { for (int b = 0; b < nbc; ++b) acc += pc[((int64_t)s * nbc + b) * H + f]; acc /= float(m); }
+        else { for (int b = 0; b < nbv; ++b) acc += pv[((int64_t)s * nbv + b) * H + f - H]; acc /= float(n); }
+        pool[s * 2 * H + f] = acc;
+        red[f] = acc * __bfloat162float(wo[f]);
+    }
+    __syncthreads();
+    if (f == 0) {
+        float t = 0.f;
+        for (int q = 0; q < 2 * H; ++q) t += red[q];
+        lw[s] = t + bo[0];
+    }
+}
+
+// ---- loss and output gradients --------------------------------------------------------
+// d = out - target; dout = coef * d; block partial of sum d^2 (per block, in order)
+__global__ void __launch_bounds__(kT) k_sq_loss(const float* __restrict__ out, const float* __restrict__ tgt,
+                                                int64_t count, float coef, float* __restrict__ dout,
+                                                double* __restrict__ part) {
+    __shared__ double red[kT];
+    double acc = 0.0;
+    for (int64_t t = blockIdx.x * (int64_t)kT + threadIdx.x; t < count; t += (int64_t)gridDim.x * kT) {
+        const float d = out[t] - tgt[t];
+        dout[t] = coef * d;
+        acc += double(d) * double(d);
+    }
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int o = kT / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// ---- head backward: dh[v] = dout[v] w + dlw[s] wo_part / N; partials of dw, db -------
+// part[blk][0:H] = sum dout h, part[blk][H] = sum dout (H+1 per block)
+template <int H>
+__global__ void __launch_bounds__(kT) k_head_back(const float* __restrict__ h, const float* __restrict__ dout,
+                                                  const __nv_bfloat16* __restrict__ w, const float* __restrict__ dlw,
+                                                  const __nv_bfloat16* __restrict__ wo_part, int n, int batch,
+                                                  float* __restrict__ dh, float* __restrict__ part) {
+    const int f = threadIdx.x % H, lanes = kT / H, sub = threadIdx.x / H;
+    const float wf = __bfloat162float(w[f]), wof = __bfloat162float(wo_part[f]) / float(n);
+    const int64_t nodes = (int64_t)n * batch;
+    float gw = 0.f, gb = 0.f;
+    for (int64_t v = blockIdx.x * (int64_t)lanes + sub; v < nodes; v += (int64_t)gridDim.x * lanes) {
+        const float d = dout[v];
+        dh[v * H + f] = d * wf + dlw[v / n] * wof;
+        gw += d * h[v * H + f];
+        if (f == 0) gb += d;
+    }
+    __shared__ float red[kT];
+    __shared__ float redb[kT / 32 + 1];
+    red[threadIdx.x] = gw;
+    if (f == 0) redb[sub] = gb;
+    __syncthreads();
+    if (sub == 0) {
+        for (int q = 1; q < lanes; ++q) gw += red[q * H + f];
+        part[(int64_t)blockIdx.x * (H + 1) + f] = gw;
+        if (f == 0) {
+            for (int q = 1; q < lanes; ++q) gb += redb[q];
+            part[(int64_t)blockIdx.x * (H + 1) + H] = gb;
+        }
+    }
+}
+
+// ---- dense node update backward ------------------------------------------------------
+// z = U h + M a + b, out = relu(z), dz = dout * (out > 0):
+//   dh (=/+=) U^T dz, da = M^T dz, partials of dU = sum dz h^T, dM = sum dz a^T, db = sum dz.
+// Thread t: node t / 8 and input features (t % 8) + 8 i for dh / da; weight-gradient
+// entries o = t / 4, k = (t % 4) + 4 i (16 of dU and 16 of dM per thread for H = 64).
+template <int H>
+__global__ void __launch_bounds__(kT) k_update_back(const float* __restrict__ dout, const float* __restrict__ out,
+                                                    const float* __restrict__ h, const float* __restrict__ a,
+                                                    const __nv_bfloat16* __restrict__ U,
+                                                    const __nv_bfloat16* __restrict__ M, float* __restrict__ dh,
+                                                    int dh_accumulate, float* __restrict__ da,
+                                                    float* __restrict__ part, int64_t nodes) {
+    constexpr int OP = H / 8;
+    constexpr int ZS = H + 1;
+    constexpr int WO = kT / 4 >= H ? 1 : H / (kT / 4);         // weight rows per thread
+    constexpr int WK = H / 4;                                  // weight columns per thread
+    extern __shared__ float sm[];
+    float* Us = sm;                 // [o][k]
+    float* Ms = Us + H * H;
+    float* Z = Ms + H * H;          // dz tile [kTile][ZS]
+    float* Hs = Z + kTile * ZS;     // h tile
+    float* As = Hs + kTile * ZS;    // a tile
+    for (int t = threadIdx.x; t < H * H; t += kT) {
+        Us[t] = __bfloat162float(U[t]);
+        Ms[t] = __bfloat162float(M[t]);
+    }
+    const int node = threadIdx.x >> 3, g = threadIdx.x & 7;
+    const int wo0 = threadIdx.x >> 2, wk0 = threadIdx.x & 3;   // weight-gradient ownership
+    float gU[WO][WK], gM[WO][WK], gb[WO];
+#pragma unroll
+    for (int r = 0; r < WO; ++r) {
+        gb[r] = 0.f;
+#pragma unroll
+        for (int i = 0; i < WK; ++i) { gU[r][i] = 0.f; gM[r][i] = 0.f; }
+    }
+    const int64_t tiles = (nodes + kTile - 1) / kTile;
+    for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const int64_t base = tile * kTile;
+        __syncthreads();
+        for (int t = threadIdx.x; t < kTile * H; t += kT) {
+            const int nd = t / H, k = t % H;
+            const int64_t v = base + nd;
+            const bool ok = v < nodes;
+            Z[nd * ZS + k] = ok && out[v * H + k] > 0.f ? dout[v * H + k] : 0.f;
+            Hs[nd * ZS + k] = ok ? h[v * H + k] : 0.f;
+            As[nd * ZS + k] = ok ? a[v * H + k] : 0.f;
+        }
+        __syncthreads();
+        // input gradients of this thread's node
+        float gh[OP], ga[OP];
+#pragma unroll
+        for (int i = 0; i < OP; ++i) { gh[i] = 0.f; ga[i] = 0.f; }
+        const float* z = Z + node * ZS;
+        for (int o = 0; o < H; ++o) {
+            const float zo = z[o];
+#pragma unroll
+            for (int i = 0; i < OP; ++i) {
+                gh[i] += Us[o * H + g + 8 * i] * zo;
+                ga[i] += Ms[o * H + g + 8 * i] * zo;
+            }
+        }
+        const int64_t v = base + node;
+        if (v < nodes) {
+#pragma unroll
+            for (int i = 0; i < OP; ++i) {
+                const int64_t q = v * H + g + 8 * i;
+                dh[q] = dh_accumulate ? dh[q] + gh[i] : gh[i];
+                da[q] = ga[i];
+            }
+        }
+        // weight gradients over the tile
+        for (int nd = 0; nd < kTile; ++nd) {
+#pragma unroll
+            for (int r = 0; r < WO; ++r) {
+                const int o = wo0 + r * (kT / 4);
+                if (o >= H) continue;
+                const float zo = Z[nd * ZS + o];
+                if (wk0 == 0) gb[r] += zo;
+#pragma unroll
+                for (int i = 0; i < WK; ++i) {
+                    const int k = wk0 + 4 * i;
+                    gU[r][i] += zo * Hs[nd * ZS + k];
+                    gM[r][i] += zo * As[nd * ZS + k];
+                }
+            }
+        }
+    }
+    // block partial: [dU (H*H) | dM (H*H) | db (H)]
+    float* P = part + (int64_t)blockIdx.x * (2 * H * H + H);
+#pragma unroll
+    for (int r = 0; r < WO; ++r) {
+        const int o = wo0 + r * (kT / 4);
+        if (o >= H) continue;
+#pragma unroll
+        for (int i = 0; i < WK; ++i) {
+            const int k = wk0 + 4 * i;
+            P[o * H + k] = gU[r][i];
+            P[H * H + o * H + k] = gM[r][i];
+        }
+        if (wk0 == 0) P[2 * H * H + o] = gb[r];
+    }
+}
+
+// input layer backward: dz = dout * (h > 0); partials of dW (H x F) and db (H)
+template <int H>
+__global__ void __launch_bounds__(kT) k_input_back(const float* __restrict__ dout, const float* __restrict__ h,
+                                                   const float* __restrict__ f, int F, int64_t nodes,
+                                                   float* __restrict__ part) {
+    const int o = threadIdx.x % H, lanes = kT / H, sub = threadIdx.x / H;
+    float gw[kMaxF], gb = 0.f;
+    for (int q = 0; q < kMaxF; ++q) gw[q] = 0.f;
+    for (int64_t v = blockIdx.x * (int64_t)lanes + sub; v < nodes; v += (int64_t)gridDim.x * lanes) {
+        const float z = h[v * H + o] > 0.f ? dout[v * H + o] : 0.f;
+        gb += z;
+        for (int q = 0; q < F; ++q) gw[q] += z * f[v * F + q];
+    }
+    __shared__ float red[kT * (kMaxF + 1)];
+    for (int q = 0; q < F; ++q) red[q * kT + threadIdx.x] = gw[q];
+    red[kMaxF * kT + threadIdx.x] = gb;
+    __syncthreads();
+    if (sub == 0) {
+        float* P = part + (int64_t)blockIdx.x * (H * F + H);
+        for (int q = 0; q < F; ++q) {
+            float s = 0.f;
+            for (int l = 0; l < lanes; ++l) s += red[q * kT + l * H + o];
+            P[o * F + q] = s;
+        }
+        float s = 0.f;
+        for (int l = 0; l < lanes; ++l) s += red[kMaxF * kT + l * H + o];
+        P[H * F + o] = s;
+    }
+}
+
+// grad[p] += scale * sum_b part[b][p] (blocks in order)
+__global__ void k_sum_parts(const float* __restrict__ part, int nb, int width, float scale, float* __restrict__ grad) {
+    for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < width; p += gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int b = 0; b < nb; ++b) s += part[(int64_t)b * width + p];
+        grad[p] += scale * s;
+    }
+}
+
+// log-omega head gradients: dwo += sum_s dlw[s] pool[s], dbo += sum_s dlw[s]
+template <int H>
+__global__ void k_omega_back(const float* __restrict__ dlw, const float* __restrict__ pool, int batch,
+                             float* __restrict__ gwo, float* __restrict__ gbo) {
+    const int f = threadIdx.x;
+    if (f < 2 * H) {
+        float s = 0.f;
+        for (int b = 0; b < batch; ++b) s += dlw[b] * pool[b * 2 * H + f];
+        gwo[f] += s;
+    }
+    if (f == 0) {
+        float s = 0.f;
+        for (int b = 0; b < batch; ++b) s += dlw[b];
+        gbo[0] += s;
+    }
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, __nv_bfloat16* __restrict__ pb, int64_t count, float lr, float b1,
+                       float b2, float eps, float c1, float c2) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x) {
+        const float gt = g[t];
+        const float a = b1 * m1[t] + (1.f - b1) * gt;
+        const float b = b2 * m2[t] + (1.f - b2) * gt * gt;
+        m1[t] = a;
+        m2[t] = b;
+        const float v = p[t] - lr * (a / c1) / (sqrtf(b / c2) + eps);
+        p[t] = v;
+        pb[t] = __float2bfloat16_rn(v);
+    }
+}
+
+__global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict__ pb, int64_t count) {
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < count; t += (int64_t)gridDim.x * blockDim.x)
+        pb[t] = __float2bfloat16_rn(p[t]);
+}
+
+}  // namespace
+
+// ===========================================================================
+// Host object
+// ===========================================================================
+struct sps_gnn {
+    sps_gnn_graph g{};
+    sps_gnn_options opt{};
+    int H = 64, L = 3, Fv = 1, Fc = 1, n = 0, m = 0, B = 1;
+    int64_t nnz = 0, np = 0;
+    cudaStream_t st = nullptr;
+    std::vector<void*> dev;
+    std::string err;
+    // graph: CSR by constraint (a_c and a_v values), CSR by variable (a_v and a_c values)
+    int32_t *cptr, *cidx, *vptr, *vidx;
+    float *ac_c, *av_c, *av_v, *ac_v;
+    // parameters
+    float *P, *G, *M1, *M2;
+    __nv_bfloat16* PB;
+    int64_t step = 0;
+    // offsets into the parameter vector
+    int64_t oWv, obv, oWc, obc, oL0, per_layer, oWx, obx, oWy, oby, oWo, obo;
+    // activations (max batch)
+    float *fv, *fc, *xt, *yt, *lt;
+    std::vector<float*> HV, HC, AV, AC;
+    float *dHV, *dHC, *dHV2, *dHC2, *dA;
+    float *x0, *y0, *lw, *pool, *dx0, *dy0, *dlw;
+    float *part;              // weight-gradient block partials
+    double* lpart;            // loss partials
+    float *pcp, *pvp;         // pooling partials
+    int nb_dense = 0, nb_pool_c = 0, nb_pool_v = 0, nb_loss = 0;
+    int64_t part_floats = 0;
+
+    ~sps_gnn() {
+        for (void* p : dev) cudaFree(p);
+        if (st) cudaStreamDestroy(st);
+    }
+    template <class T>
+    cudaError_t alloc(T** p, size_t count) {
+        void* q = nullptr;
+        const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+        if (e == cudaSuccess) dev.push_back(q);
+        *p = static_cast<T*>(q);
+        return e;
+    }
+    int fail(int code, const std::string& msg) {
+        err = msg;
+        return code;
+    }
+    int64_t layer_off(int l) const { return oL0 + per_layer * l; }
+};
+
+namespace {
+
+thread_local std::string g_gnn_create_error;
+
+#define GNN_CK(call)                                                                         \
+    do {                                                                                     \
+        cudaError_t e_ = (call);                                                             \
+        if (e_ != cudaSuccess)                                                               \
+            return g->fail(e_ == cudaErrorMemoryAllocation ? -3 : -2,                        \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));              \
+    } while (0)
+
+template <int H>
+size_t update_smem() { return sizeof(float) * (2 * H * H + kTile * (2 * H + 1)); }
+template <int H>
+size_t update_back_smem() { return sizeof(float) * (2 * H * H + 3 * kTile * (H + 1)); }
+
+template <int H>
+int set_smem_attrs() {
+    if (cudaFuncSetAttribute(k_update<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)update_smem<H>()) !=
+        cudaSuccess)
+        return -2;
+    if (cudaFuncSetAttribute(k_update_back<H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)update_back_smem<H>()) != cudaSuccess)
+        return -2;
+    return 0;
+}
+
+int grid_for(int64_t work, int per_block) {
+    const int64_t b = (work + per_block - 1) / per_block;
+    return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 8));
+}
+
+// Forward pass over `batch` instances whose features are already on the device.
+template <int H>
+int forward(sps_gnn* g, int batch) {
+    const int n = g->n, m = g->m, L = g->L;
+    const int64_t NV = (int64_t)n * batch, NC = (int64_t)m * batch;
+    const __nv_bfloat16* W = g->PB;
+    const float* P = g->P;
+    cudaStream_t st = g->st;
+    k_input<H><<<grid_for(NV * H, kT), kT, 0, st>>>(g->fv, NV, g->Fv, W + g->oWv, P + g->obv, g->HV[0]);
+    k_input<H><<<grid_for(NC * H, kT), kT, 0, st>>>(g->fc, NC, g->Fc, W + g->oWc, P + g->obc, g->HC[0]);
+    for (int l = 0; l < L; ++l) {
+        const int64_t o = g->layer_off(l);
+        const int64_t oUc = o, oMc = o + H * H, obc = o + 2 * H * H;
+        const int64_t oUv = obc + H, oMv = oUv + H * H, obv = oMv + H * H;
+        k_agg<H><<<grid_for(NC * 32, kT), kT, 0, st>>>(g->cptr, g->cidx, g->ac_c, g->HV[l], g->AC[l], m, n, batch, 0);
+        k_update<H><<<g->nb_dense, kT, update_smem<H>(), st>>>(g->HC[l], g->AC[l], W + oUc, W + oMc, P + obc,
+                                                               g->HC[l + 1], NC);
+        k_agg<H><<<grid_for(NV * 32, kT), kT, 0, st>>>(g->vptr, g->vidx, g->av_v, g->HC[l + 1], g->AV[l], n, m, batch,
+                                                       0);
+        k_update<H><<<g->nb_dense, kT, update_smem<H>(), st>>>(g->HV[l], g->AV[l], W + oUv, W + oMv, P + obv,
+                                                               g->HV[l + 1], NV);
+    }
+    k_head<H><<<grid_for(NV * 32, kT), kT, 0, st>>>(g->HV[L], W + g->oWx, P + g->obx, g->x0, NV);
+    k_head<H><<<grid_for(NC * 32, kT), kT, 0, st>>>(g->HC[L], W + g->oWy, P + g->oby, g->y0, NC);
+    k_colsum_part<H><<<dim3(g->nb_pool_c, batch), kT, 0, st>>>(g->HC[L], m, g->pcp);
+    k_colsum_part<H><<<dim3(g->nb_pool_v, batch), kT, 0, st>>>(g->HV[L], n, g->pvp);
+    k_pool_finish<H><<<batch, 2 * H, 0, st>>>(g->pcp, g->nb_pool_c, g->pvp, g->nb_pool_v, m, n, W + g->oWo,
+                                              P + g->obo, g->pool, g->lw);
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? 0 : g->fail(-2, std::string("forward: ") + cudaGetErrorString(e));
+}
+
+// Loss (host value) and gradient into g->G (zeroed here) for `batch` instances
+// whose features and targets are on the device.
+template <int H>
+int backward(sps_gnn* g, int batch, double* loss) {
+    const int n = g->n, m = g->m, L = g->L;
+    const int64_t NV = (int64_t)n * batch, NC = (int64_t)m * batch;
+    const __nv_bfloat16* W = g->PB;
+    cudaStream_t st = g->st;
+    const float ax = g->opt.loss_x, ay = g->opt.loss_y, ao = g->opt.loss_omega;
+    GNN_CK(cudaMemsetAsync(g->G, 0, sizeof(float) * g->np, st));
+    // output gradients: loss = (1/B) sum_s [ax/n |x0-xt|^2 + ay/m |y0-yt|^2 + ao (lw-lt)^2]
+    const int nbl = g->nb_loss;
+    k_sq_loss<<<nbl, kT, 0, st>>>(g->x0, g->xt, NV, 2.f * ax / (float(n) * batch), g->dx0, g->lpart);
+    k_sq_loss<<<nbl, kT, 0, st>>>(g->y0, g->yt, NC, 2.f * ay / (float(m) * batch), g->dy0, g->lpart + nbl);
+    k_sq_loss<<<1, kT, 0, st>>>(g->lw, g->lt, batch, 2.f * ao / float(batch), g->dlw, g->lpart + 2 * nbl);
+    // heads
+    const int nbh = g->nb_dense;
+    k_head_back<H><<<nbh, kT, 0, st>>>(g->HV[L], g->dx0, W + g->oWx, g->dlw, W + g->oWo + H, n, batch, g->dHV,
+                                       g->part);
+    k_sum_parts<<<4, 256, 0, st>>>(g->part, nbh, H + 1, 1.f, g->G + g->oWx);
+    k_head_back<H><<<nbh, kT, 0, st>>>(g->HC[L], g->dy0, W + g->oWy, g->dlw, W + g->oWo, m, batch, g->dHC, g->part);
+    k_sum_parts<<<4, 256, 0, st>>>(g->part, nbh, H + 1, 1.f, g->G + g->oWy);
+    k_omega_back<H><<<1, 2 * H, 0, st>>>(g->dlw, g->pool, batch, g->G + g->oWo, g->G + g->obo);
+    // layers, last to first.  dHV / dHC hold the gradient of HV[l+1] / HC[l+1].
+    float *dhv = g->dHV, *dhc = g->dHC, *dhv_next = g->dHV2, *dhc_next = g->dHC2;
+    const int width = 2 * H * H + H;
+    for (int l = L - 1; l >= 0; --l) {
+        const int64_t o = g->layer_off(l);
+        const int64_t oUc = o, oMc = o + H * H;
+        const int64_t oUv = oMc + H * H + H, oMv = oUv + H * H;
+        // variable update: HV[l+1] = relu(Uv HV[l] + Mv AV[l] + bv)
+        k_update_back<H><<<nbh, kT, update_back_smem<H>(), st>>>(dhv, g->HV[l + 1], g->HV[l], g->AV[l], W + oUv,
+                                                                 W + oMv, dhv_next, 0, g->dA, g->part, NV);
+        k_sum_parts<<<32, 256, 0, st>>>(g->part, nbh, width, 1.f, g->G + oUv);
+        // AV[l] = agg_v(HC[l+1]): dHC[l+1] += agg over constraints with a_v values
+        k_agg<H><<<grid_for(NC * 32, kT), kT, 0, st>>>(g->cptr, g->cidx, g->av_c, g->dA, dhc, m, n, batch, 1);
+        // constraint update: HC[l+1] = relu(Uc HC[l] + Mc AC[l] + bc)
+        k_update_back<H><<<nbh, kT, update_back_smem<H>(), st>>>(dhc, g->HC[l + 1], g->HC[l], g->AC[l], W + oUc,
+                                                                 W + oMc, dhc_next, 0, g->dA, g->part, NC);
+        k_sum_parts<<<32, 256, 0, st>>>(g->part, nbh, width, 1.f, g->G + oUc);
+        // AC[l] = agg_c(HV[l]): dHV[l] += agg over variables with a_c values
+        k_agg<H><<<grid_for(NV * 32, kT), kT, 0, st>>>(g->vptr, g->vidx, g->ac_v, g->dA, dhv_next, n, m, batch, 1);
+        std::swap(dhv, dhv_next);
+        std::swap(dhc, dhc_next);
+    }
+    // input layers
+    k_input_back<H><<<nbh, kT, 0, st>>>(dhv, g->HV[0], g->fv, g->Fv, NV, g->part);
+    k_sum_parts<<<4, 256, 0, st>>>(g->part, nbh, H * g->Fv + H, 1.f, g->G + g->oWv);
+    k_input_back<H><<<nbh, kT, 0, st>>>(dhc, g->HC[0], g->fc, g->Fc, NC, g->part);
+    k_sum_parts<<<4, 256, 0, st>>>(g->part, nbh, H * g->Fc + H, 1.f, g->G + g->oWc);
+    GNN_CK(cudaGetLastError());
+    if (loss) {
+        std::vector<double> lp(2 * nbl + 1);
+        GNN_CK(cudaMemcpyAsync(lp.data(), g->lpart, sizeof(double) * lp.size(), cudaMemcpyDeviceToHost, st));
+        GNN_CK(cudaStreamSynchronize(st));
+        double sx = 0, sy = 0;
+        for (int b = 0; b < nbl; ++b) { sx += lp[b]; sy += lp[nbl + b]; }
+        *loss = (ax * sx / n + ay * sy / m + ao * lp[2 * nbl]) / batch;
+    }
+    return 0;
+}
+
+int upload_inputs(sps_gnn* g, int batch, const float* vf, const float* cf, const float* xt, const float* yt,
+                  const float* lt) {
+    cudaStream_t st = g->st;
+    const size_t nv = (size_t)g->n * batch, nc = (size_t)g->m * batch;
+    GNN_CK(cudaMemcpyAsync(g->fv, vf, sizeof(float) * nv * g->Fv, cudaMemcpyHostToDevice, st));
+    GNN_CK(cudaMemcpyAsync(g->fc, cf, sizeof(float) * nc * g->Fc, cudaMemcpyHostToDevice, st));
+    if (xt) GNN_CK(cudaMemcpyAsync(g->xt, xt, sizeof(float) * nv, cudaMemcpyHostToDevice, st));
+    if (yt) GNN_CK(cudaMemcpyAsync(g->yt, yt, sizeof(float) * nc, cudaMemcpyHostToDevice, st));
+    if (lt) GNN_CK(cudaMemcpyAsync(g->lt, lt, sizeof(float) * batch, cudaMemcpyHostToDevice, st));
+    return 0;
+}
+
+int check_batch(sps_gnn* g, int32_t batch, const float* vf, const float* cf) {
+    if (batch < 1 || batch > g->B) return g->fail(-1, "batch must be in [1, max_batch]");
+    if (!vf || !cf) return g->fail(-1, "null features");
+    return 0;
+}
+
+// Scaled-uniform initialisation (fan-in), deterministic in the seed.
+void init_params(std::vector<float>& p, const sps_gnn* g) {
+    uint64_t s = g->opt.seed * 6364136223846793005ULL + 1442695040888963407ULL;
+    auto uni = [&]() {
+        s ^= s >> 12; s ^= s << 25; s ^= s >> 27;
+        return double((s * 2685821657736338717ULL) >> 11) * (1.0 / 9007199254740992.0) * 2.0 - 1.0;
+    };
+    const int H = g->H;
+    auto fill = [&](int64_t off, int64_t count, double fan_in) {
+        const double a = std::sqrt(3.0 / std::max(1.0, fan_in));
+        for (int64_t t = 0; t < count; ++t) p[off + t] = float(a * uni());
+    };
+    std::fill(p.begin(), p.end(), 0.f);
+    fill(g->oWv, (int64_t)H * g->Fv, g->Fv);
+    fill(g->oWc, (int64_t)H * g->Fc, g->Fc);
+    for (int l = 0; l < g->L; ++l) {
+        const int64_t o = g->layer_off(l);
+        fill(o, 2LL * H * H, 2.0 * H);                       // Uc, Mc
+        fill(o + 2LL * H * H + H, 2LL * H * H, 2.0 * H);     // Uv, Mv
+    }
+    fill(g->oWx, H, H);
+    fill(g->oWy, H, H);
+    fill(g->oWo, 2 * H, 2.0 * H);
+}
+
+template <int H>
+int run_loss_grad(sps_gnn* g, int batch, double* loss) {
+    if (int rc = forward<H>(g, batch)) return rc;
+    return backward<H>(g, batch, loss);
+}
+
+}  // namespace
+
+extern "C" {
+
+int sps_gnn_options_init(sps_gnn_options* o) {
+    if (!o) return -1;
+    std::memset(o, 0, sizeof(*o));
+    o->hidden = 64;
+    o->layers = 3;
+    o->seed = 0;
+    o->lr = 1e-3f;
+    o->beta1 = 0.9f;
+    o->beta2 = 0.999f;
+    o->eps = 1e-8f;
+    o->loss_x = 1.f;
+    o->loss_y = 1.f;
+    o->loss_omega = 0.1f;
+    o->max_batch = 8;
+    o->device = 0;
+    return 0;
+}
+
+int sps_gnn_create(const sps_gnn_graph* gr, const sps_gnn_options* opt_in, sps_gnn** out) {
+    g_gnn_create_error.clear();
+    if (!gr || !out) { g_gnn_create_error = "null graph or output"; return -1; }
+    *out = nullptr;
+    sps_gnn_options opt;
+    if (opt_in) opt = *opt_in; else sps_gnn_options_init(&opt);
+    if (opt.hidden != 32 && opt.hidden != 64) { g_gnn_create_error = "hidden must be 32 or 64"; return -1; }
+    if (opt.layers < 1 || opt.layers > 8 || opt.max_batch < 1) { g_gnn_create_error = "layers in 1..8, max_batch >= 1"; return -1; }
+    if (gr->n_var < 1 || gr->n_con < 1 || gr->f_var < 1 || gr->f_var > kMaxF || gr->f_con < 1 || gr->f_con > kMaxF ||
+        !gr->con_ptr) {
+        g_gnn_create_error = "graph needs n_var, n_con >= 1, feature widths in 1..8 and con_ptr";
+        return -1;
+    }
+    const int m = gr->n_con, n = gr->n_var;
+    if (gr->con_ptr[0] != 0) { g_gnn_create_error = "con_ptr[0] != 0"; return -1; }
+    for (int i = 0; i < m; ++i)
+        if (gr->con_ptr[i + 1] < gr->con_ptr[i]) { g_gnn_create_error = "con_ptr not monotone"; return -1; }
+    const int64_t nnz = gr->con_ptr[m];
+    if (nnz > 0 && (!gr->con_idx || !gr->con_val)) { g_gnn_create_error = "null con_idx / con_val"; return -1; }
+    for (int64_t k = 0; k < nnz; ++k)
+        if (gr->con_idx[k] < 0 || gr->con_idx[k] >= n || !std::isfinite(gr->con_val[k])) {
+            g_gnn_create_error = "edge " + std::to_string(k) + ": variable out of range or non-finite value";
+            return -1;
+        }
+    auto g = new sps_gnn();
+    g->g = *gr;
+    g->opt = opt;
+    g->H = opt.hidden; g->L = opt.layers; g->Fv = gr->f_var; g->Fc = gr->f_con;
+    g->n = n; g->m = m; g->B = opt.max_batch; g->nnz = nnz;
+    const int H = g->H;
+    // parameter offsets
+    int64_t o = 0;
+    g->oWv = o; o += (int64_t)H * g->Fv; g->obv = o; o += H;
+    g->oWc = o; o += (int64_t)H * g->Fc; g->obc = o; o += H;
+    g->oL0 = o; g->per_layer = 4LL * H * H + 2 * H; o += g->per_layer * g->L;
+    g->oWx = o; o += H; g->obx = o; o += 1;
+    g->oWy = o; o += H; g->oby = o; o += 1;
+    g->oWo = o; o += 2 * H; g->obo = o; o += 1;
+    g->np = o;
+    // host graph: degrees, normalised values, CSR by variable
+    std::vector<int32_t> degc(m), degv(n, 0), vptr(n + 1, 0), vidx(nnz);
+    std::vector<float> ac_c(nnz), av_c(nnz), av_v(nnz), ac_v(nnz);
+    for (int i = 0; i < m; ++i) degc[i] = gr->con_ptr[i + 1] - gr->con_ptr[i];
+    for (int64_t k = 0; k < nnz; ++k) degv[gr->con_idx[k]]++;
+    for (int j = 0; j < n; ++j) vptr[j + 1] = vptr[j] + degv[j];
+    std::vector<int32_t> fill(vptr.begin(), vptr.end() - 1);
+    for (int i = 0; i < m; ++i)
+        for (int32_t k = gr->con_ptr[i]; k < gr->con_ptr[i + 1]; ++k) {
+            const int j = gr->con_idx[k];
+            const float a = gr->con_val[k];
+            ac_c[k] = a / float(degc[i]);
+            av_c[k] = a / float(degv[j]);
+            const int32_t q = fill[j]++;
+            vidx[q] = i;
+            av_v[q] = av_c[k];
+            ac_v[q] = ac_c[k];
+        }
+    int rc = 0;
+    {
+        sps_gnn* gg = g;
+        auto setup = [&]() -> int {
+            sps_gnn* g = gg;
+            GNN_CK(cudaSetDevice(opt.device));
+            GNN_CK(cudaStreamCreateWithFlags(&g->st, cudaStreamNonBlocking));
+            if (H == 64) { if (set_smem_attrs<64>()) return g->fail(-2, "shared-memory attribute"); }
+            else if (set_smem_attrs<32>()) return g->fail(-2, "shared-memory attribute");
+            GNN_CK(g->alloc(&g->cptr, m + 1)); GNN_CK(g->alloc(&g->cidx, nnz));
+            GNN_CK(g->alloc(&g->vptr, n + 1)); GNN_CK(g->alloc(&g->vidx, nnz));
+            GNN_CK(g->alloc(&g->ac_c, nnz)); GNN_CK(g->alloc(&g->av_c, nnz));
+            GNN_CK(g->alloc(&g->av_v, nnz)); GNN_CK(g->alloc(&g->ac_v, nnz));
+            auto up = [&](void* d, const void* s, size_t b) {
+                return b ? cudaMemcpyAsync(d, s, b, cudaMemcpyHostToDevice, g->st) : cudaSuccess;
+            };
+            GNN_CK(up(g->cptr, gr->con_ptr, 4 * (size_t)(m + 1))); GNN_CK(up(g->cidx, gr->con_idx, 4 * (size_t)nnz));
+            GNN_CK(up(g->vptr, vptr.data(), 4 * (size_t)(n + 1))); GNN_CK(up(g->vidx, vidx.data(), 4 * (size_t)nnz));
+            GNN_CK(up(g->ac_c, ac_c.data(), 4 * (size_t)nnz)); GNN_CK(up(g->av_c, av_c.data(), 4 * (size_t)nnz));
+            GNN_CK(up(g->av_v, av_v.data(), 4 * (size_t)nnz)); GNN_CK(up(g->ac_v, ac_v.data(), 4 * (size_t)nnz));
+            GNN_CK(g->alloc(&g->P, g->np)); GNN_CK(g->alloc(&g->G, g->np));
+            GNN_CK(g->alloc(&g->M1, g->np)); GNN_CK(g->alloc(&g->M2, g->np));
+            GNN_CK(g->alloc(&g->PB, g->np));
+            const int64_t B = g->B, NV = (int64_t)n * B, NC = (int64_t)m * B;
+            GNN_CK(g->alloc(&g->fv, NV * g->Fv)); GNN_CK(g->alloc(&g->fc, NC * g->Fc));
+            GNN_CK(g->alloc(&g->xt, NV)); GNN_CK(g->alloc(&g->yt, NC)); GNN_CK(g->alloc(&g->lt, B));
+            g->HV.resize(g->L + 1); g->HC.resize(g->L + 1); g->AV.resize(g->L); g->AC.resize(g->L);
+            for (int l = 0; l <= g->L; ++l) { GNN_CK(g->alloc(&g->HV[l], NV * H)); GNN_CK(g->alloc(&g->HC[l], NC * H)); }
+            for (int l = 0; l < g->L; ++l) { GNN_CK(g->alloc(&g->AV[l], NV * H)); GNN_CK(g->alloc(&g->AC[l], NC * H)); }
+            GNN_CK(g->alloc(&g->dHV, NV * H)); GNN_CK(g->alloc(&g->dHV2, NV * H));
+            GNN_CK(g->alloc(&g->dHC, NC * H)); GNN_CK(g->alloc(&g->dHC2, NC * H));
+            GNN_CK(g->alloc(&g->dA, std::max(NV, NC) * H));
+            GNN_CK(g->alloc(&g->x0, NV)); GNN_CK(g->alloc(&g->y0, NC)); GNN_CK(g->alloc(&g->lw, B));
+            GNN_CK(g->alloc(&g->dx0, NV)); GNN_CK(g->alloc(&g->dy0, NC)); GNN_CK(g->alloc(&g->dlw, B));
+            GNN_CK(g->alloc(&g->pool, 2 * H * B));
+            g->nb_dense = 152 * 2;
+            g->nb_loss = 152 * 2;
+            g->nb_pool_c = std::max(1, std::min(64, (m + 31) / 32));
+            g->nb_pool_v = std::max(1, std::min(152, (n + 31) / 32));
+            g->part_floats = (int64_t)g->nb_dense * (2 * H * H + H);
+            GNN_CK(g->alloc(&g->part, g->part_floats));
+            GNN_CK(g->alloc(&g->lpart, 2 * g->nb_loss + 1));
+            GNN_CK(g->alloc(&g->pcp, (int64_t)g->nb_pool_c * H * B));
+            GNN_CK(g->alloc(&g->pvp, (int64_t)g->nb_pool_v * H * B));
+            std::vector<float> p(g->np);
+            init_params(p, g);
+            GNN_CK(up(g->P, p.data(), sizeof(float) * g->np));
+            GNN_CK(cudaMemsetAsync(g->M1, 0, sizeof(float) * g->np, g->st));
+            GNN_CK(cudaMemsetAsync(g->M2, 0, sizeof(float) * g->np, g->st));
+            k_to_bf16<<<grid_for(g->np, 256), 256, 0, g->st>>>(g->P, g->PB, g->np);
+            GNN_CK(cudaGetLastError());
+            GNN_CK(cudaStreamSynchronize(g->st));
+            return 0;
+        };
+        rc = setup();
+    }
+    if (rc) {
+        g_gnn_create_error = g->err;
+        delete g;
+        return rc;
+    }
+    *out = g;
+    return 0;
+}
+
+int sps_gnn_predict(sps_gnn* g, int32_t batch, const float* vf, const float* cf, float* x0, float* y0, float* lw) {
+    if (!g) return -1;
+    if (int rc = check_batch(g, batch, vf, cf)) return rc;
+    GNN_CK(cudaSetDevice(g->opt.device));
+    if (int rc = upload_inputs(g, batch, vf, cf, nullptr, nullptr, nullptr)) return rc;
+    const int rc = g->H == 64 ? forward<64>(g, batch) : forward<32>(g, batch);
+    if (rc) return rc;
+    const size_t nv = (size_t)g->n * batch, nc = (size_t)g->m * batch;
+    if (x0) GNN_CK(cudaMemcpyAsync(x0, g->x0, sizeof(float) * nv, cudaMemcpyDeviceToHost, g->st));
+    if (y0) GNN_CK(cudaMemcpyAsync(y0, g->y0, sizeof(float) * nc, cudaMemcpyDeviceToHost, g->st));
+    if (lw) GNN_CK(cudaMemcpyAsync(lw, g->lw, sizeof(float) * batch, cudaMemcpyDeviceToHost, g->st));
+    GNN_CK(cudaStreamSynchronize(g->st));
+    return 0;
+}
+
+int sps_gnn_loss_grad(sps_gnn* g, int32_t batch, const float* vf, const float* cf, const float* xt, const float* yt,
+                      const float* lt, double* loss, float* grad) {
+    if (!g) return -1;
+    if (int rc = check_batch(g, batch, vf, cf)) return rc;
+    if (!xt || !yt || !lt) return g->fail(-1, "null targets");
+    GNN_CK(cudaSetDevice(g->opt.device));
+    if (int rc = upload_inputs(g, batch, vf, cf, xt, yt, lt)) return rc;
+    const int rc = g->H == 64 ? run_loss_grad<64>(g, batch, loss) : run_loss_grad<32>(g, batch, loss);
+    if (rc) return rc;
+    if (grad) {
+        GNN_CK(cudaMemcpyAsync(grad, g->G, sizeof(float) * g->np, cudaMemcpyDeviceToHost, g->st));
+        GNN_CK(cudaStreamSynchronize(g->st));
+    }
+    return 0;
+}
+
+int sps_gnn_train_step(sps_gnn* g, int32_t batch, const float* vf, const float* cf, const float* xt, const float* yt,
+                       const float* lt, double* loss) {
+    if (!g) return -1;
+    if (int rc = check_batch(g, batch, vf, cf)) return rc;
+    if (!xt || !yt || !lt) return g->fail(-1, "null targets");
+    GNN_CK(cudaSetDevice(g->opt.device));
+    if (int rc = upload_inputs(g, batch, vf, cf, xt, yt, lt)) return rc;
+    const int rc = g->H == 64 ? run_loss_grad<64>(g, batch, loss) : run_loss_grad<32>(g, batch, loss);
+    if (rc) return rc;
+    g->step += 1;
+    const float c1 = 1.f - std::pow(g->opt.beta1, float(g->step)), c2 = 1.f - std::pow(g->opt.beta2, float(g->step));
+    k_adam<<<grid_for(g->np, 256), 256, 0, g->st>>>(g->P, g->G, g->M1, g->M2, g->PB, g->np, g->opt.lr,
+                                                    g->opt.beta1, g->opt.beta2, g->opt.eps, c1, c2);
+    GNN_CK(cudaGetLastError());
+    if (!loss) GNN_CK(cudaStreamSynchronize(g->st));
+    return 0;
+}
+
+int64_t sps_gnn_num_params(const sps_gnn* g) { return g ? g->np : -1; }
+
+int sps_gnn_get_params(sps_gnn* g, float* out) {
+    if (!g || !out) return -1;
+    GNN_CK(cudaSetDevice(g->opt.device));
+    GNN_CK(cudaMemcpyAsync(out, g->P, sizeof(float) * g->np, cudaMemcpyDeviceToHost, g->st));
+    GNN_CK(cudaStreamSynchronize(g->st));
+    return 0;
+}
+
+int sps_gnn_set_params(sps_gnn* g, const float* in) {
+    if (!g || !in) return -1;
+    for (int64_t t = 0; t < g->np; ++t)
+        if (!std::isfinite(in[t])) return g->fail(-1, "non-finite parameter");
+    GNN_CK(cudaSetDevice(g->opt.device));
+    GNN_CK(cudaMemcpyAsync(g->P, in, sizeof(float) * g->np, cudaMemcpyHostToDevice, g->st));
+    GNN_CK(cudaMemsetAsync(g->M1, 0, sizeof(float) * g->np, g->st));
+    GNN_CK(cudaMemsetAsync(g->M2, 0, sizeof(float) * g->np, g->st));
+    k_to_bf16<<<grid_for(g->np, 256), 256, 0, g->st>>>(g->P, g->PB, g->np);
+    GNN_CK(cudaGetLastError());
+    GNN_CK(cudaStreamSynchronize(g->st));
+    g->step = 0;
+    return 0;
+}
+
+const char* sps_gnn_last_error(const sps_gnn* g) { return g ? g->err.c_str() : g_gnn_create_error.c_str(); }
+
+void sps_gnn_destroy(sps_gnn* g) { delete g; }
+
+}  // extern "C"

@@ -15,18 +15,29 @@ from sovereign_solver_gb300 import _native as N, pdhg
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
+HEADERS = ("sps_pdhg.h", "sps_gnn.h")
+
+
 def declared_functions():
-    src = open(os.path.join(ROOT, "include", "sps_pdhg.h")).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(sps_[a-z_]+)\s*\(", src)))
+    names = set()
+    for h in HEADERS:
+        src = open(os.path.join(ROOT, "include", h)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(sps_[a-z_0-9]+)\s*\(", src))
+    return sorted(names)
 
 
 def test_library_exports_every_declared_symbol():
     lib = N.load()
     names = declared_functions()
-    assert len(names) >= 10
+    assert len(names) >= 28
     for nm in names:
         assert hasattr(lib, nm), nm
+
+
+STRUCTS = (("sps_problem_desc", N.ProblemDesc), ("sps_options", N.Options), ("sps_result", N.Result),
+           ("sps_batch_stats", N.BatchStats), ("sps_device_lp", N.DeviceLP), ("sps_gnn_graph", N.GnnGraph),
+           ("sps_gnn_options", N.GnnOptions))
 
 
 def test_struct_layout_matches_header(tmp_path):
@@ -37,20 +48,18 @@ def test_struct_layout_matches_header(tmp_path):
     if cc is None:
         pytest.skip("no C compiler")
     checks = []
-    for cname, py in (("sps_problem_desc", N.ProblemDesc), ("sps_options", N.Options),
-                      ("sps_result", N.Result)):
+    for cname, py in STRUCTS:
         checks.append(f'printf("%s %zu\\n", "{cname}", sizeof({cname}));')
         for fname, _ in py._fields_:
             checks.append(f'printf("%s.%s %zu\\n", "{cname}", "{fname}", offsetof({cname}, {fname}));')
     src = tmp_path / "layout.c"
-    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "sps_pdhg.h"\nint main(void){'
-                   + "".join(checks) + "return 0;}\n")
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "sps_pdhg.h"\n#include "sps_gnn.h"\n'
+                   'int main(void){' + "".join(checks) + "return 0;}\n")
     exe = tmp_path / "layout"
     subprocess.run([cc, f"-I{os.path.join(ROOT, 'include')}", str(src), "-o", str(exe)], check=True)
     got = dict(line.split() for line in subprocess.run([str(exe)], capture_output=True, text=True,
                                                         check=True).stdout.splitlines())
-    for cname, py in (("sps_problem_desc", N.ProblemDesc), ("sps_options", N.Options),
-                      ("sps_result", N.Result)):
+    for cname, py in STRUCTS:
         assert int(got[cname]) == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
