@@ -82,13 +82,16 @@ typedef struct {
                                  2 = one graph with a device-driven while loop (default) */
     int32_t device;           /* CUDA device ordinal */
     int32_t max_blocks;       /* schedule tuning: blocks per matrix-pass launch, 0 = one resident wave */
-    int32_t batch_group;      /* batched solver: lanes per column (4, 8, 16, 32), 0 = autotune */
+    int32_t batch_group;      /* batched solver: lanes per column (1, 2, 4, 8, 16, 32), 0 = autotune */
     int32_t escalate;         /* adaptive FP32 stall handling.  A solve stalls when its best
                                  relative KKT error has not halved for max(2048, k/2) attempts
                                  (k = attempt of the last halving).  1 (default): continue in
                                  FP64 from the best point seen, with the primal weight it had;
                                  2: stop with SPS_STATUS_STALLED; 0: no stall test (FP32 only) */
-    int32_t reserved[4];
+    int32_t warm_fallback;    /* 1 (default): a warm start whose relative KKT error is larger than
+                                 the cold start's (x = clip(0, lb, ub), y = 0) is dropped and the
+                                 solve starts cold; 0: always start from the warm point */
+    int32_t reserved[3];
 } sps_options;
 
 typedef struct {
@@ -109,7 +112,9 @@ typedef struct {
     int32_t returned_average; /* 1 if the returned point is the ergodic average */
     int32_t escalated;        /* 1 if the solve stalled in FP32 and was finished in FP64; the
                                  iteration, restart and time fields then cover both parts */
-    int32_t reserved[4];
+    int32_t warm_start_used;  /* 1 if the solve started from the caller's warm start (0 when none
+                                 was given or the cold-start fallback rejected it) */
+    int32_t reserved[3];
 } sps_result;
 
 typedef struct sps_handle sps_handle;
@@ -125,6 +130,8 @@ int sps_create(const sps_problem_desc *prob, const sps_options *opt, sps_handle 
 
 /* Start the next solve from (x0, y0) in the original space (either may be
  * NULL = zero) with primal weight omega0 (<= 0 = default).  Adaptive mode only.
+ * With sps_options.warm_fallback the solve compares the start point's relative
+ * KKT error with the cold start's and keeps the better (sps_result.warm_start_used).
  * New API surface: the reference always starts from zero (solver/lp/pdhg.py:175-176). */
 int sps_set_warm_start(sps_handle *h, const double *x0, const double *y0, double omega0);
 
@@ -184,6 +191,12 @@ int sps_batch_create(int32_t count, const sps_problem_desc *probs, const sps_opt
 /* Solve every instance: one persistent launch, captured in a CUDA graph on the
  * first call and replayed afterwards; blocking. */
 int sps_batch_solve(sps_batch *b, sps_batch_stats *stats);
+/* Warm starts for the following solves, packed in instance order: x0 (sum of n),
+ * y0 (sum of m_ub + m_eq), omega0 (count; <= 0 = the instance's default), all in
+ * the original space; x0 = y0 = NULL clears them.  With sps_options.warm_fallback
+ * (default) an instance whose warm point has a larger relative KKT error than its
+ * cold start starts cold (sps_result.warm_start_used = 0). */
+int sps_batch_set_warm_starts(sps_batch *b, const double *x0, const double *y0, const double *omega0);
 /* Instance k of the last solve: x (n, clipped to bounds), y (m_ub + m_eq), result.
  * res->solve_ms is the instance's own device time inside the persistent launch
  * (plus its FP64 continuation, if any); setup_ms is the batch's. */

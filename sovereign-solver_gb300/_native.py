@@ -42,7 +42,8 @@ class Options(C.Structure):
         ("mode", C.c_int32), ("precision", C.c_int32), ("max_iters", C.c_int64), ("tol", C.c_double),
         ("check_interval", C.c_int32), ("ruiz_iters", C.c_int32), ("time_limit_s", C.c_double),
         ("graph_mode", C.c_int32), ("device", C.c_int32), ("max_blocks", C.c_int32),
-        ("batch_group", C.c_int32), ("escalate", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("batch_group", C.c_int32), ("escalate", C.c_int32), ("warm_fallback", C.c_int32),
+        ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -61,7 +62,7 @@ class Result(C.Structure):
         ("rel_primal", C.c_double), ("rel_dual", C.c_double), ("rel_gap", C.c_double),
         ("primal_weight", C.c_double), ("step_size", C.c_double), ("setup_ms", C.c_double),
         ("solve_ms", C.c_double), ("kernel_launches", C.c_int64), ("returned_average", C.c_int32),
-        ("escalated", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("escalated", C.c_int32), ("warm_start_used", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 
@@ -127,6 +128,7 @@ def load() -> C.CDLL:
         "sps_batch_create": (C.c_int, [C.c_int32, C.POINTER(ProblemDesc), C.POINTER(Options), C.POINTER(H)]),
         "sps_batch_solve": (C.c_int, [H, C.POINTER(BatchStats)]),
         "sps_batch_get": (C.c_int, [H, C.c_int32, _f64p, _f64p, C.POINTER(Result)]),
+        "sps_batch_set_warm_starts": (C.c_int, [H, _f64p, _f64p, _f64p]),
         "sps_batch_last_error": (C.c_char_p, [H]),
         "sps_batch_destroy": (None, [H]),
         "sps_gnn_options_init": (C.c_int, [C.POINTER(GnnOptions)]),

@@ -32,7 +32,8 @@ class PDHGBatch:
 
     def __init__(self, problems: Sequence, tol: float = 1e-4, max_iters: int = MAX_PDHG_ITERS,
                  batch_group: int = 0, time_limit: float = 0.0, check_interval: int = 0,
-                 graph_mode: int = 2, device: int = 0, ruiz_iters: int = 10, escalate: str = "fp64"):
+                 graph_mode: int = 2, device: int = 0, ruiz_iters: int = 10, escalate: str = "fp64",
+                 warm_fallback: bool = True):
         self.lib = N.load()
         self.problems = list(problems)
         if not self.problems:
@@ -41,7 +42,7 @@ class PDHGBatch:
         arr = (N.ProblemDesc * len(self._descs))(*[d.desc for d in self._descs])
         o = make_options(tol=tol, max_iters=max_iters, time_limit=time_limit,
                          check_interval=check_interval, graph_mode=graph_mode, device=device,
-                         ruiz_iters=ruiz_iters, escalate=escalate)
+                         ruiz_iters=ruiz_iters, escalate=escalate, warm_fallback=warm_fallback)
         o.batch_group = int(batch_group)
         h = C.c_void_p()
         N.check(self.lib.sps_batch_create(len(self._descs), arr, C.byref(o), C.byref(h)), None)
@@ -52,6 +53,27 @@ class PDHGBatch:
         if rc != 0:
             msg = self.lib.sps_batch_last_error(self.h).decode(errors="replace")
             raise RuntimeError(f"{N.ERRORS.get(rc, rc)}: {msg}")
+
+    def set_warm_starts(self, starts) -> None:
+        """Warm starts for the following solves: one (x0, y0, omega0) per problem (omega0
+        <= 0 or None = default), e.g. from ``WarmStartGNN.predict``; None clears them."""
+        if starts is None:
+            self._check(self.lib.sps_batch_set_warm_starts(self.h, None, None, None))
+            return
+        starts = list(starts)
+        if len(starts) != len(self.problems):
+            raise ValueError("one warm start per problem")
+        xs, ys, om = [], [], np.empty(len(starts))
+        for k, (d, st) in enumerate(zip(self._descs, starts)):
+            x0, y0, w0 = (tuple(st) + (None, None, None))[:3]
+            xs.append(np.zeros(d.n) if x0 is None else np.asarray(x0, float).ravel())
+            ys.append(np.zeros(d.m_ub + d.m_eq) if y0 is None else np.asarray(y0, float).ravel())
+            if xs[-1].size != d.n or ys[-1].size != d.m_ub + d.m_eq:
+                raise ValueError(f"warm start {k}: wrong length")
+            om[k] = -1.0 if w0 is None else float(w0)
+        x = np.ascontiguousarray(np.concatenate(xs))
+        y = np.ascontiguousarray(np.concatenate(ys))
+        self._check(self.lib.sps_batch_set_warm_starts(self.h, N.f64p(x), N.f64p(y), N.f64p(om)))
 
     def solve_raw(self) -> N.BatchStats:
         st = N.BatchStats()

@@ -261,6 +261,7 @@ int sps_options_init(sps_options* o) {
     o->device = 0;
     o->max_blocks = 0;
     o->escalate = 1;
+    o->warm_fallback = 1;
     return SPS_OK;
 }
 

@@ -95,13 +95,17 @@ struct ColStepE {
     }
 };
 
+// The check epilogues accumulate their FP64 partials in the calling thread's
+// own shared-memory slots (p[q * kBlock], q < 8 or 10) rather than registers:
+// the check runs once per window and this keeps the step loops' register
+// budget.  slot_sums() adds the slots in thread order.
 struct RowCheckE {
     const float *b, *ys, *ylb, *yc, *yl;
     const double* dr;
     const int8_t* kind;
     float* axa;
     double inv_w;
-    double p[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    double* p;                 // this thread's slots
     struct Pre {};
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int r, const double (&acc)[2], const Pre&) {
@@ -110,12 +114,12 @@ struct RowCheckE {
         for (int q = 0; q < 2; ++q) {
             double res = acc[q] - br;
             if (kind[r]) res = fmax(res, 0.0);
-            p[4 * q + 0] += res * res;
-            p[4 * q + 1] += (res / d) * (res / d);
+            p[(4 * q + 0) * kBlock] += res * res;
+            p[(4 * q + 1) * kBlock] += (res / d) * (res / d);
             const double yv = q == 0 ? avg_at(ys, ylb, inv_w, r) : double(yc[r]);
-            p[4 * q + 2] += br * yv;
+            p[(4 * q + 2) * kBlock] += br * yv;
             const double dd = yv - double(yl[r]);
-            p[4 * q + 3] += dd * dd;
+            p[(4 * q + 3) * kBlock] += dd * dd;
         }
     }
 };
@@ -125,7 +129,7 @@ struct ColCheckE {
     const double* dc;
     float* atya;
     double inv_w;
-    double p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double* p;                 // this thread's slots
     struct Pre {};
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int j, const double (&acc)[2], const Pre&) {
@@ -136,13 +140,13 @@ struct ColCheckE {
             const double rc = cj - acc[q];
             const double lam = (hl && hh) ? rc : hl ? fmax(rc, 0.0) : hh ? fmin(rc, 0.0) : 0.0;
             const double dres = rc - lam;
-            p[5 * q + 0] += dres * dres;
-            p[5 * q + 1] += (dres / d) * (dres / d);
+            p[(5 * q + 0) * kBlock] += dres * dres;
+            p[(5 * q + 1) * kBlock] += (dres / d) * (dres / d);
             const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
-            p[5 * q + 2] += cj * xv;
-            p[5 * q + 3] += (hl ? l * fmax(lam, 0.0) : 0.0) + (hh ? h * fmin(lam, 0.0) : 0.0);
+            p[(5 * q + 2) * kBlock] += cj * xv;
+            p[(5 * q + 3) * kBlock] += (hl ? l * fmax(lam, 0.0) : 0.0) + (hh ? h * fmin(lam, 0.0) : 0.0);
             const double dd = xv - double(xl[j]);
-            p[5 * q + 4] += dd * dd;
+            p[(5 * q + 4) * kBlock] += dd * dd;
         }
     }
 };
@@ -178,22 +182,43 @@ __device__ __forceinline__ View make_view(const Args& A, const Inst& I, int G) {
 }
 
 // KKT check of average and current point, decision, and the restart copies.
-__device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm, const uint64_t* dl) {
+// out[q] = sum over threads (in order) of slots[q * kBlock + t], q < N
+template <int N>
+__device__ __forceinline__ void slot_sums(const double* slots, double* out) {
+    __syncthreads();
+    if (threadIdx.x < N) {
+        double t = 0.0;
+        for (int k = 0; k < kBlock; ++k) t += slots[threadIdx.x * kBlock + k];
+        out[threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+__device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm, double* slots,
+                                const uint64_t* dl) {
     const uint64_t deadline = *dl;
     const bool has_avg = c.w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / c.w_sum : 1.0;
     const int cur = c.cur;
-    RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w};
+    double* mine = slots + threadIdx.x;
+    for (int q = 0; q < 8; ++q) mine[q * kBlock] = 0.0;
+    RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w,
+                 mine};
     group_rows<32, 2, double>(v.rptr, v.ridx, v.rval, v.m,
                               Gather2{has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], inv_w}, er);
-    block_sum<8>(er.p, sm);
-    ColCheckE ec{v.c, v.lo, v.hi, has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], v.xl, v.dc, v.atya, inv_w};
+    slot_sums<8>(slots, sm);                       // sm[0..7]: row partials
+    for (int q = 0; q < 10; ++q) mine[q * kBlock] = 0.0;
+    ColCheckE ec{v.c, v.lo, v.hi, has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], v.xl, v.dc, v.atya,
+                 inv_w, mine};
     group_rows_dyn<2, double>(v.G, v.cptr, v.cidx, v.cval, v.n,
                               Gather2{has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], inv_w}, ec);
-    block_sum<10>(ec.p, sm);
+    slot_sums<10>(slots, sm + 8);                  // sm[8..17]: column partials
     if (threadIdx.x == 0) {
         const bool stop = deadline && global_ns() > deadline;
-        decide_check(c, ec.p, er.p, I.inv_nb, I.inv_nc, stop);
+        double tr[8], tc[10];
+        for (int q = 0; q < 8; ++q) tr[q] = sm[q];
+        for (int q = 0; q < 10; ++q) tc[q] = sm[8 + q];
+        decide_check(c, tc, tr, I.inv_nb, I.inv_nc, stop);
     }
     __syncthreads();
     const int ap = c.apply;
@@ -242,9 +267,12 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     __syncthreads();
 }
 
-__device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
-    const Inst I = A.inst[k];
-    const View v = make_view(A, I, G);
+// Start point of instance k (cold: x = clip(0, lo, hi), y = 0; warm: the caller's
+// point scaled and projected, with its primal weight), its products K x0 and
+// K^T y0, and the init-phase check that records its relative KKT error.
+__device__ void start_point(const Args& A, int k, const Inst& I, const View& v, int G, bool warm, Ctl& c,
+                            double* sm, double* slots) {
+    __syncthreads();
     if (threadIdx.x == 0) {
         c = Ctl{};
         c.status = SPS_STATUS_ITERATION_LIMIT;
@@ -252,24 +280,60 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
         c.max_iters = A.max_iters;
         c.tol = A.tol;
         c.eta = A.a.eta0[k];
-        c.omega = A.a.omega0[k];
+        c.omega = warm && A.wom[k] > 0.0 ? A.wom[k] : A.a.omega0[k];
         c.kkt_last = INFINITY;
         c.stall_on = A.stall_on;
-        c.t_begin = global_ns();
     }
     for (int j = threadIdx.x; j < v.n; j += kBlock) {
-        const float x = fminf(fmaxf(0.f, v.lo[j]), v.hi[j]);
+        const float x0 = warm ? float(A.wx[I.vc + j] / v.dc[j]) : 0.f;
+        const float x = fminf(fmaxf(x0, v.lo[j]), v.hi[j]);
         v.X[0][j] = x;
         v.xl[j] = x;
         v.xs[j] = 0.f;
-        v.ATY[0][j] = 0.f;                      // K^T y0 with y0 = 0
     }
-    for (int i = threadIdx.x; i < v.m; i += kBlock) { v.Y[0][i] = 0.f; v.yl[i] = 0.f; v.ys[i] = 0.f; }
+    for (int i = threadIdx.x; i < v.m; i += kBlock) {
+        float y = warm ? float(A.wy[I.vr + i] / v.dr[i]) : 0.f;
+        if (v.kind[i]) y = fminf(y, 0.f);
+        v.Y[0][i] = y;
+        v.yl[i] = y;
+        v.ys[i] = 0.f;
+    }
     __syncthreads();
-    StoreE st{v.AX[0]};
-    group_rows<32, 1, float>(v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[0]}, st);
+    StoreE sx{v.AX[0]};
+    group_rows<32, 1, float>(v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[0]}, sx);
+    StoreE sy{v.ATY[0]};
+    group_rows_dyn<1, float>(G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[0]}, sy);
     __syncthreads();
-    check_and_apply(v, I, c, sm, A.deadline);
+    check_and_apply(v, I, c, sm, slots, A.deadline);
+}
+
+__device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, double* slots) {
+    const Inst I = A.inst[k];
+    const View v = make_view(A, I, G);
+    const uint64_t t_begin = global_ns();
+    const bool warm = A.warm != 0;
+    bool used = warm;
+    if (warm && A.fallback) {
+        // keep the warm point only if its relative KKT error is not above the cold start's
+        double cold = A.cold_rel[k];
+        if (!(cold >= 0.0)) {
+            start_point(A, k, I, v, G, false, c, sm, slots);
+            cold = c.rel_kkt;
+            if (threadIdx.x == 0) A.cold_rel[k] = cold;
+        }
+        start_point(A, k, I, v, G, true, c, sm, slots);
+        if (!(c.rel_kkt <= cold)) {
+            used = false;
+            start_point(A, k, I, v, G, false, c, sm, slots);
+        }
+    } else {
+        start_point(A, k, I, v, G, warm, c, sm, slots);
+    }
+    if (threadIdx.x == 0) {
+        c.t_begin = t_begin;
+        c.warm_used = used ? 1 : 0;
+    }
+    __syncthreads();
     for (;;) {
         for (int w = 0; w < A.check_interval; ++w) {
             if (c.done || c.iters >= c.max_iters) break;
@@ -304,7 +368,7 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
             __syncthreads();
         }
         if (c.done) break;
-        check_and_apply(v, I, c, sm, A.deadline);
+        check_and_apply(v, I, c, sm, slots, A.deadline);
         if (c.done) break;
     }
     if (threadIdx.x == 0) {
@@ -313,9 +377,10 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm) {
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_batch_solve(Args A, int G) {
+__global__ void __launch_bounds__(kBlock, 2) k_batch_solve(Args A, int G) {
     __shared__ Ctl c;
     __shared__ double sm[kWarps * 10];
+    __shared__ double slots[10 * kBlock];
     __shared__ int s_inst;
     for (;;) {
         if (threadIdx.x == 0) {
@@ -325,7 +390,7 @@ __global__ void __launch_bounds__(kBlock) k_batch_solve(Args A, int G) {
         __syncthreads();
         const int k = s_inst;
         if (k < 0) return;
-        solve_one(A, k, G, c, sm);
+        solve_one(A, k, G, c, sm, slots);
         __syncthreads();
     }
 }
@@ -474,8 +539,11 @@ struct sps_batch {
     std::vector<int8_t> escalated;
     std::vector<double> esc_ms;             // wall time of each instance's FP64 continuation
     cudaGraphExec_t gexec = nullptr;
-    int32_t gexec_G = -1;
+    int32_t gexec_G = -1, gexec_warm = -1;
     uint64_t gexec_tl = 0;
+    // warm starts (original space, packed like the vectors) and the cold-start error cache
+    double *d_wx = nullptr, *d_wy = nullptr, *d_wom = nullptr, *d_cold_rel = nullptr;
+    int32_t warm = 0;
     uint64_t* d_deadline = nullptr;
     double setup_ms = 0.0, solve_ms = 0.0;
     bool solved = false;
@@ -759,6 +827,8 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         SPB_CK(cudaMemsetAsync(b->d_deadline, 0, sizeof(uint64_t), b->st));
         SPB_CK(b->alloc(&b->d_xo, vc));
         SPB_CK(b->alloc(&b->d_yo, vr));
+        SPB_CK(b->alloc(&b->d_cold_rel, count));
+        SPB_CK(cudaMemsetAsync(b->d_cold_rel, 0xFF, sizeof(double) * count, b->st));   // NaN = unknown
         float *d_xb = nullptr, *d_yb = nullptr;
         if (opt.escalate != 0) { SPB_CK(b->alloc(&d_xb, vc)); SPB_CK(b->alloc(&d_yb, vr)); }
         double *t_rv, *t_cv, *t_c, *t_lo, *t_hi, *t_b;
@@ -806,14 +876,16 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         b->setup_ms = ms;
     }
     // ---- lanes per column: given, or timed on a sample of the batch
-    if (opt.batch_group == 4 || opt.batch_group == 8 || opt.batch_group == 16 || opt.batch_group == 32) {
+    const int g_opt = opt.batch_group;
+    if (g_opt == 1 || g_opt == 2 || g_opt == 4 || g_opt == 8 || g_opt == 16 || g_opt == 32) {
         b->G = opt.batch_group;
     } else {
         sps_batch* bb = bp;
         const int32_t sample = std::min<int32_t>(count, 2 * bb->blocks);
         double best = 1e300;
-        for (int G : {4, 8, 16, 32}) {
-            sps::batch::Args A{bb->d_inst, bb->d_order, sample, 64, 128, 0.0, bb->d_deadline, bb->arr, bb->d_out,
+        for (int G : {1, 2, 4, 8, 16, 32}) {
+            // 32 attempts and one check per candidate on the sample (largest instances first)
+            sps::batch::Args A{bb->d_inst, bb->d_order, sample, 32, 32, 0.0, bb->d_deadline, bb->arr, bb->d_out,
                                bb->d_counter, 0};
             cudaMemsetAsync(bb->d_counter, 0, sizeof(uint32_t), bb->st);
             cudaEventRecord(bb->e0, bb->st);
@@ -838,7 +910,8 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     const int64_t W = b->opt.check_interval > 0 ? b->opt.check_interval : 64;
     const uint64_t tl = b->opt.time_limit_s > 0 ? (uint64_t)(b->opt.time_limit_s * 1e9) : 0;
     sps::batch::Args A{b->d_inst, b->d_order, b->count, (int32_t)W, b->opt.max_iters, b->opt.tol, b->d_deadline,
-                       b->arr, b->d_out, b->d_counter, b->opt.escalate != 0 ? 1 : 0};
+                       b->arr, b->d_out, b->d_counter, b->opt.escalate != 0 ? 1 : 0, b->warm,
+                       b->opt.warm_fallback ? 1 : 0, b->d_wx, b->d_wy, b->d_wom, b->d_cold_rel};
     auto enqueue = [&](cudaStream_t s) {
         cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
         sps::batch::k_set_deadline<<<1, 32, 0, s>>>(b->d_deadline, tl);
@@ -848,7 +921,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     if (b->opt.graph_mode != 0) {
         // one graph (counter reset, deadline, persistent solve), built once per
         // schedule and time limit and replayed by later solves
-        if (!b->gexec || b->gexec_G != b->G || b->gexec_tl != tl) {
+        if (!b->gexec || b->gexec_G != b->G || b->gexec_tl != tl || b->gexec_warm != b->warm) {
             if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
             cudaGraph_t g;
             cudaStream_t cap;
@@ -866,6 +939,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
             SPB_CK(e);
             b->gexec_G = b->G;
             b->gexec_tl = tl;
+            b->gexec_warm = b->warm;
         }
         SPB_CK(cudaGraphLaunch(b->gexec, b->st));
     } else {
@@ -917,6 +991,39 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     return SPS_OK;
 }
 
+extern "C" int sps_batch_set_warm_starts(sps_batch* b, const double* x0, const double* y0, const double* omega0) {
+    if (!b) return SPS_ERR_INVALID;
+    if (!x0 && !y0) {
+        b->warm = 0;
+        return SPS_OK;
+    }
+    if (b->opt.mode != SPS_MODE_ADAPTIVE) return b->fail(SPS_ERR_STATE, "warm starts need the adaptive mode");
+    SPB_CK(cudaSetDevice(b->opt.device));
+    if (!b->d_wx) {
+        SPB_CK(b->alloc(&b->d_wx, b->sum_n));
+        SPB_CK(b->alloc(&b->d_wy, b->sum_m));
+        SPB_CK(b->alloc(&b->d_wom, b->count));
+    }
+    auto finite = [](const double* v, int64_t len) {
+        for (int64_t t = 0; t < len; ++t)
+            if (!std::isfinite(v[t])) return false;
+        return true;
+    };
+    if ((x0 && !finite(x0, b->sum_n)) || (y0 && !finite(y0, b->sum_m)))
+        return b->fail(SPS_ERR_INVALID, "non-finite warm start");
+    std::vector<double> om(b->count, -1.0);
+    if (omega0)
+        for (int32_t k = 0; k < b->count; ++k) om[k] = std::isfinite(omega0[k]) ? omega0[k] : -1.0;
+    if (x0) SPB_CK(cudaMemcpyAsync(b->d_wx, x0, sizeof(double) * b->sum_n, cudaMemcpyHostToDevice, b->st));
+    else SPB_CK(cudaMemsetAsync(b->d_wx, 0, sizeof(double) * b->sum_n, b->st));
+    if (y0) SPB_CK(cudaMemcpyAsync(b->d_wy, y0, sizeof(double) * b->sum_m, cudaMemcpyHostToDevice, b->st));
+    else SPB_CK(cudaMemsetAsync(b->d_wy, 0, sizeof(double) * b->sum_m, b->st));
+    SPB_CK(cudaMemcpyAsync(b->d_wom, om.data(), sizeof(double) * b->count, cudaMemcpyHostToDevice, b->st));
+    SPB_CK(cudaStreamSynchronize(b->st));
+    b->warm = 1;
+    return SPS_OK;
+}
+
 extern "C" int sps_batch_get(sps_batch* b, int32_t k, double* x, double* y, sps_result* res) {
     if (!b || k < 0 || k >= b->count) return SPS_ERR_INVALID;
     if (!b->solved) return b->fail(SPS_ERR_STATE, "call sps_batch_solve first");
@@ -949,6 +1056,7 @@ extern "C" int sps_batch_get(sps_batch* b, int32_t k, double* x, double* y, sps_
         res->kernel_launches = 1;
         res->returned_average = c.choice;
         res->escalated = b->escalated[k];
+        res->warm_start_used = c.warm_used;
     }
     return SPS_OK;
 }

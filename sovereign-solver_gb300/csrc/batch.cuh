@@ -5,7 +5,7 @@
 // to back (offsets inside an instance are local, 0-based); column vectors and
 // row vectors likewise.  One block of 256 threads owns one instance at a time
 // and runs the whole adaptive PDHG loop on it with block barriers only: rows
-// one warp each, columns `G` lanes each (G autotuned), FP32 iterates, FP64
+// one warp each, columns `G` lanes each (G in 1..32, autotuned), FP32 iterates, FP64
 // block reductions, the same step/restart/termination decisions as the
 // single-LP kernels (decide.cuh) on a shared-memory control block.
 // Instances are handed out largest first from an atomic counter.
@@ -48,6 +48,9 @@ struct Args {
     Ctl* out;                 // per instance final state
     uint32_t* counter;
     int32_t stall_on;         // stall test on (FP64 continuation on the host)
+    int32_t warm, fallback;   // warm starts set / cold-start fallback on
+    const double *wx, *wy, *wom;   // warm starts (original space, packed like the vectors), omega0
+    double* cold_rel;         // per instance: relative KKT error of the cold start (< 0 = unknown)
 };
 
 // ---------------------------------------------------------------------------
@@ -92,6 +95,8 @@ template <int NV, class Acc, class Gather, class Epi>
 __device__ __forceinline__ void group_rows_dyn(int G, const int32_t* ptr, const int32_t* idx, const float* val,
                                                int count, const Gather& g, Epi& e) {
     switch (G) {
+        case 1: group_rows<1, NV, Acc>(ptr, idx, val, count, g, e); break;
+        case 2: group_rows<2, NV, Acc>(ptr, idx, val, count, g, e); break;
         case 4: group_rows<4, NV, Acc>(ptr, idx, val, count, g, e); break;
         case 8: group_rows<8, NV, Acc>(ptr, idx, val, count, g, e); break;
         case 16: group_rows<16, NV, Acc>(ptr, idx, val, count, g, e); break;

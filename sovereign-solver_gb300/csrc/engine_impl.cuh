@@ -86,6 +86,8 @@ struct Engine : EngineBase {
     double *d_xout = nullptr, *d_yout = nullptr, *d_wx = nullptr, *d_wy = nullptr;
     bool have_warm_x = false, have_warm_y = false;
     double warm_omega = 0.0;
+    bool warm_used = false;
+    double cold_rel = -1.0;      // relative KKT error of the cold start point (cached)
     double eta0 = 1.0, omega0 = 1.0;
     Args<V> args{};
     cudaGraphExec_t win_exec = nullptr, loop_exec = nullptr;
@@ -720,7 +722,7 @@ struct Engine : EngineBase {
         c0.max_iters = opt.max_iters;
         c0.tol = opt.tol;
         c0.eta = eta0;
-        c0.omega = (adaptive && warm_omega > 0) ? warm_omega : omega0;
+        c0.omega = omega0;
         c0.kkt_last = INFINITY;
         c0.stall_on = stall_test() ? 1 : 0;
         *h_ctl = c0;
@@ -730,16 +732,50 @@ struct Engine : EngineBase {
         SPS_CK(cudaEventRecord(ev0, st));
         SPS_CK(cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
         const int gr = args.rows.total_blocks, gc = args.cols.total_blocks;
+        const bool warm = adaptive && (have_warm_x || have_warm_y);
+        warm_used = warm;
         if (adaptive) {
-            k_ad_start<V><<<args.apply_blocks, kBlock, 0, st>>>(args, have_warm_x ? d_wx : nullptr,
-                                                               have_warm_y ? d_wy : nullptr, d_perm_col,
-                                                               d_perm_row, d_rkind, tl_ns);
-            spmv_rows<V><<<gr, kBlock, 0, st>>>(args, args.X[0], args.AX[0]);
-            spmv_cols<V><<<gc, kBlock, 0, st>>>(args, args.Y[0], args.ATY[0]);
-            ad_row_check<V><<<gr, kBlock, 0, st>>>(args);
-            ad_col_check<V><<<gc, kBlock, 0, st>>>(args);
-            ad_apply<V><<<args.apply_blocks, kBlock, 0, st>>>(args);
-            launches += 6;
+            // start-up: the start point, its products, its KKT check (init phase) and the
+            // first candidate; with the fallback the warm point's relative KKT error is
+            // compared with the cold start's (cached per problem) and the better one kept
+            auto start = [&](bool use_warm) -> int {
+                Ctl c = c0;
+                if (use_warm && warm_omega > 0) c.omega = warm_omega;
+                *h_ctl = c;
+                SPS_CK(cudaMemcpyAsync(d_ctl, h_ctl, sizeof(Ctl), cudaMemcpyHostToDevice, st));
+                k_ad_start<V><<<args.apply_blocks, kBlock, 0, st>>>(args, use_warm && have_warm_x ? d_wx : nullptr,
+                                                                   use_warm && have_warm_y ? d_wy : nullptr,
+                                                                   d_perm_col, d_perm_row, d_rkind, tl_ns);
+                spmv_rows<V><<<gr, kBlock, 0, st>>>(args, args.X[0], args.AX[0]);
+                spmv_cols<V><<<gc, kBlock, 0, st>>>(args, args.Y[0], args.ATY[0]);
+                ad_row_check<V><<<gr, kBlock, 0, st>>>(args);
+                ad_col_check<V><<<gc, kBlock, 0, st>>>(args);
+                ad_apply<V><<<args.apply_blocks, kBlock, 0, st>>>(args);
+                launches += 6;
+                SPS_CK(cudaGetLastError());
+                return SPS_OK;
+            };
+            auto start_error = [&](double* rel) -> int {
+                SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+                SPS_CK(cudaStreamSynchronize(st));
+                *rel = h_ctl->rel_kkt;
+                return SPS_OK;
+            };
+            if (warm && opt.warm_fallback) {
+                if (!(cold_rel >= 0.0)) {
+                    if (int rc = start(false)) return rc;
+                    if (int rc = start_error(&cold_rel)) return rc;
+                }
+                double warm_rel = 0.0;
+                if (int rc = start(true)) return rc;
+                if (int rc = start_error(&warm_rel)) return rc;
+                if (!(warm_rel <= cold_rel)) {
+                    warm_used = false;
+                    if (int rc = start(false)) return rc;
+                }
+            } else if (int rc = start(warm)) {
+                return rc;
+            }
         } else {
             k_rf_start<V><<<args.apply_blocks, kBlock, 0, st>>>(args, tl_ns);
             rf_row_check<V><<<gr, kBlock, 0, st>>>(args, 1);
@@ -787,6 +823,7 @@ struct Engine : EngineBase {
         res->solve_ms = ms;
         res->kernel_launches = launches;
         res->returned_average = h_ctl->choice;
+        res->warm_start_used = warm_used ? 1 : 0;
         double obj = 0;
         for (int j = 0; j < n_user; ++j) obj += c_user[j] * x_sol[j];
         res->objective = obj;

@@ -5,13 +5,17 @@ message-passing net over the constraint matrix shared by every instance of a
 family (one sparsity pattern; per-instance c and b), trained on PDHG solutions
 by the library's own forward / backward / Adam kernels.  ``predict`` gives a
 warm start (x0, y0, omega0) for ``PDHGEngine.warm_start`` or
-``PDHGBatch(..., warm_starts=...)``; those solves fall back to a cold start
+``PDHGBatch.set_warm_starts``; those solves fall back to a cold start
 when the prediction is worse than zero (KKT of the start point), and the usual
 relative-KKT test judges every answer.
 
-Features (per instance, scaled by fixed family scales):
-  variable j:   [c_j / c_scale, 1]
-  constraint i: [b_i / b_scale, 1 if '<=' row else 0, 1]
+Features (per instance, scaled by fixed family scales; cmin_i = min of c over
+the columns of row i):
+  variable j:   [c_j, mean over its '<=' rows of (c_j - cmin_i),
+                 mean over its '=' rows of (c_j - cmin_i), 1]      (costs / c_scale)
+  constraint i: [b_i / b_scale, 1 if '<=' row else 0, cmin_i / c_scale, 1]
+The cost gaps tell each variable how far it is from the cheapest column of its
+rows, which mean aggregation alone cannot compute.
 Targets: x* / x_scale, y* / y_scale, log omega* (omega in the engine's scaled space).
 """
 
@@ -25,7 +29,7 @@ import scipy.sparse as sp
 
 from . import _native as N
 
-FV, FC = 2, 3
+FV, FC = 4, 4
 
 
 def stacked_rows(problem) -> sp.csr_matrix:
@@ -60,6 +64,14 @@ class WarmStartGNN:
         self.scales = dict(scales)
         self._kind = np.zeros(self.m, np.float32)
         self._kind[: self.m_ub] = 1.0
+        deg = np.diff(self._ptr)
+        self._row = np.repeat(np.arange(self.m), deg)
+        self._nonempty = deg > 0
+        self._starts = self._ptr[:-1][self._nonempty]
+        le = self._kind[self._row] > 0
+        self._w_le, self._w_eq = le.astype(float), (~le).astype(float)
+        self._cnt_le = np.maximum(np.bincount(self._idx, weights=self._w_le, minlength=self.n), 1)
+        self._cnt_eq = np.maximum(np.bincount(self._idx, weights=self._w_eq, minlength=self.n), 1)
         gr = N.GnnGraph(self.n, self.m, N.i32p(self._ptr), N.i32p(self._idx), N.f32p(self._val), FV, FC)
         o = N.GnnOptions()
         self.lib.sps_gnn_options_init(C.byref(o))
@@ -75,14 +87,23 @@ class WarmStartGNN:
 
     # ---------------------------------------------------------------- data
     def features_from(self, c, b):
-        """(var features n x 2, constraint features m x 3) from one instance's c and b."""
+        """(var features n x 4, constraint features m x 4) from one instance's c and b."""
+        c = np.asarray(c, float) / self.scales["c"]
+        ce = c[self._idx]
+        cmin = np.zeros(self.m)
+        if self._starts.size:
+            cmin[self._nonempty] = np.minimum.reduceat(ce, self._starts)
+        d = ce - cmin[self._row]
         fv = np.empty((self.n, FV), np.float32)
-        fv[:, 0] = np.asarray(c, float) / self.scales["c"]
-        fv[:, 1] = 1.0
+        fv[:, 0] = c
+        fv[:, 1] = np.bincount(self._idx, weights=d * self._w_le, minlength=self.n) / self._cnt_le
+        fv[:, 2] = np.bincount(self._idx, weights=d * self._w_eq, minlength=self.n) / self._cnt_eq
+        fv[:, 3] = 1.0
         fc = np.empty((self.m, FC), np.float32)
         fc[:, 0] = np.asarray(b, float) / self.scales["b"]
         fc[:, 1] = self._kind
-        fc[:, 2] = 1.0
+        fc[:, 2] = cmin
+        fc[:, 3] = 1.0
         return fv, fc
 
     def features(self, problem):

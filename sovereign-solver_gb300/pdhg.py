@@ -90,10 +90,11 @@ class _Desc:
 
 def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, tol=PDHG_TOL,
                  check_interval=0, ruiz_iters=10, time_limit=0.0, graph_mode=2, device=0,
-                 max_blocks=0, escalate="fp64") -> N.Options:
+                 max_blocks=0, escalate="fp64", warm_fallback=True) -> N.Options:
     """Options for ``sps_create``.  ``escalate`` (adaptive FP32): "fp64" continues a
     stalled solve in FP64 from its best point, "stop" ends it with status
-    "stalled", "off" keeps iterating in FP32."""
+    "stalled", "off" keeps iterating in FP32.  ``warm_fallback``: start cold when
+    a warm start's relative KKT error is above the cold start's."""
     if mode not in N.MODES:
         raise ValueError(f"Unknown mode {mode!r}. Choose 'adaptive' or 'reference'.")
     if precision not in N.PRECISIONS:
@@ -108,6 +109,7 @@ def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, to
     o.time_limit_s, o.graph_mode, o.device = float(time_limit), int(graph_mode), int(device)
     o.max_blocks = int(max_blocks)
     o.escalate = N.ESCALATE[escalate]
+    o.warm_fallback = 1 if warm_fallback else 0
     return o
 
 
@@ -187,7 +189,7 @@ def to_result(problem, r: N.Result, x, y, mode, precision) -> SolveResult:
         "primal_weight": float(r.primal_weight), "step_size": float(r.step_size),
         "setup_ms": float(r.setup_ms), "solve_ms": float(r.solve_ms),
         "kernel_launches": int(r.kernel_launches), "returned_average": bool(r.returned_average),
-        "escalated": bool(r.escalated),
+        "escalated": bool(r.escalated), "warm_start_used": bool(r.warm_start_used),
     }
     msg = f"{mode}/{precision} PDHG on GPU: rel_kkt={r.rel_kkt:.3e}"
     return SolveResult(status, x, obj, int(r.iterations), message=msg, y=y,

@@ -24,8 +24,8 @@ def _template(n=300, m=40, m_ub=15, seed=0):
 
 def _data(net, B, seed=1):
     rng = np.random.default_rng(seed)
-    fvs = [rng.standard_normal((net.n, 2)).astype(np.float32) for _ in range(B)]
-    fcs = [rng.standard_normal((net.m, 3)).astype(np.float32) for _ in range(B)]
+    fvs = [rng.standard_normal((net.n, 4)).astype(np.float32) for _ in range(B)]
+    fcs = [rng.standard_normal((net.m, 4)).astype(np.float32) for _ in range(B)]
     xts = [rng.random(net.n).astype(np.float32) for _ in range(B)]
     yts = [rng.standard_normal(net.m).astype(np.float32) for _ in range(B)]
     lts = rng.standard_normal(B).astype(np.float32)
@@ -39,7 +39,7 @@ def test_gradients_match_oracle(hidden):
         fvs, fcs, xts, yts, lts = _data(net, 3)
         loss, g = net.loss_grad(fvs, fcs, xts, yts, lts)
         params = net.params()
-        lay = gnn_ref.Layout(hidden, 3, 2, 3)
+        lay = gnn_ref.Layout(hidden, 3, 4, 4)
         assert lay.size == net.num_params
         ref_loss, ref_g = gnn_ref.loss_grad(params, lay, net._ptr, net._idx, net._val, fvs, fcs, xts, yts,
                                             list(lts), 1.0, 1.0, 0.1, bf16=True)
@@ -56,7 +56,7 @@ def test_forward_matches_oracle():
     with WarmStartGNN(p, seed=5, max_batch=2) as net:
         fvs, fcs, *_ = _data(net, 2, seed=6)
         X, Y, Lw = net.predict_features(fvs, fcs)
-        lay = gnn_ref.Layout(64, 3, 2, 3)
+        lay = gnn_ref.Layout(64, 3, 4, 4)
         params = net.params()
         for s in range(2):
             x, y, lw = gnn_ref.predict(params, lay, net._ptr, net._idx, net._val, fvs[s], fcs[s])
