@@ -397,6 +397,146 @@ def run_batch(args, rank, world):
     return line
 
 
+WEIGHTS = os.path.join(ROOT, "sovereign-solver_gb300", "data", "warmstart_transport_200x400.npz")
+TEST_SEED0 = 10_000_000          # held-out seeds (training used 0 .. 19 999)
+
+
+def run_warmstart(args, rank, world):
+    """Learned warm start on the 200 x 400 transportation family: ``--batch``
+    held-out seeds (per GPU).  One step = GNN inference (device features) +
+    warm starts + one batched solve of every seed, batch resident; value =
+    solves/s.  Reported beside it: the same batch solved cold, and cold
+    single-instance PDHG (create + solve + read-back per LP) on a sample.
+    e2e = sps_batch_create + inference + warm starts + solve + read-back of
+    every instance from host arrays."""
+    import ctypes as C
+    import sovereign_solver_gb300 as sps
+    from sovereign_solver_gb300 import _native as N
+    from sovereign_solver_gb300.gnn import WarmStartGNN
+    from sovereign_solver_gb300.warmstart import transport_instances
+    from sovereign_solver_gb300.workloads import TransportFamily
+
+    fam = TransportFamily()
+    template = fam.problem(0)
+    seeds = np.arange(TEST_SEED0 + rank * args.batch, TEST_SEED0 + (rank + 1) * args.batch)
+    probs = transport_instances(fam, template, seeds)
+    net = WarmStartGNN.load(WEIGHTS, template, max_batch=16, device=args.device)
+    hbm, peak_kind = peaks()
+    b = sps.PDHGBatch(probs, tol=args.tol, max_iters=args.max_iters, device=args.device)
+    # cold batched (resident)
+    b.set_warm_starts(None)
+    for _ in range(max(1, args.warmup // 2)):
+        b.solve_raw()
+    t_cold = []
+    for _ in range(max(1, args.steps // 2)):
+        st = b.solve_raw()
+        t_cold.append(st.solve_ms / 1e3)
+    cold = [b.result(k) for k in range(len(probs))]
+    # warm batched (resident): inference + warm starts + solve
+    def warm_step():
+        t0 = time.perf_counter()
+        starts = net.predict(probs)
+        t1 = time.perf_counter()
+        b.set_warm_starts(starts)
+        st = b.solve_raw()
+        return t1 - t0, st.solve_ms / 1e3, time.perf_counter() - t0
+    for _ in range(args.warmup):
+        warm_step()
+    barrier(world)
+    steps = []
+    with ClockSampler(args.device) as clk:
+        for _ in range(args.steps):
+            steps.append(warm_step())
+    warm = [b.result(k) for k in range(len(probs))]
+    b.close()
+    # cold single-instance PDHG on a sample (create + solve + read-back)
+    single = []
+    for p in probs[:args.single_sample]:
+        t0 = time.perf_counter()
+        with sps.PDHGEngine(p, tol=args.tol, max_iters=args.max_iters, device=args.device) as eng:
+            r = eng.solve()
+        single.append((time.perf_counter() - t0, r.iterations, r.status == "optimal"))
+    # end to end through the C ABI from host arrays (create, inference, warm starts, solve, read-back)
+    from sovereign_solver_gb300 import pdhg
+    descs = [pdhg._Desc(p) for p in probs]
+    arr = (N.ProblemDesc * len(descs))(*[d.desc for d in descs])
+    lib = N.load()
+    opts = pdhg.make_options(tol=args.tol, max_iters=args.max_iters, device=args.device)
+    xs = [np.empty(p.n_vars) for p in probs]
+    ys = [np.empty(p.n_ineq + p.n_eq) for p in probs]
+    e2e_s = []
+    for _ in range(max(1, args.e2e_steps)):
+        t0 = time.perf_counter()
+        h = C.c_void_p()
+        N.check(lib.sps_batch_create(len(descs), arr, C.byref(opts), C.byref(h)), None)
+        starts = net.predict(probs)
+        wx = np.concatenate([s_[0] for s_ in starts])
+        wy = np.concatenate([s_[1] for s_ in starts])
+        wo = np.array([s_[2] for s_ in starts])
+        rc = lib.sps_batch_set_warm_starts(h, N.f64p(wx), N.f64p(wy), N.f64p(wo))
+        sst = N.BatchStats()
+        rc = rc or lib.sps_batch_solve(h, C.byref(sst))
+        rr = N.Result()
+        for k in range(len(descs)):
+            rc = rc or lib.sps_batch_get(h, k, N.f64p(xs[k]), N.f64p(ys[k]), C.byref(rr))
+        lib.sps_batch_destroy(h)
+        if rc:
+            raise RuntimeError(f"warm-start e2e failed: {rc}")
+        e2e_s.append(time.perf_counter() - t0)
+    net.close()
+
+    per_rank = {"t": sum(s_[2] for s_ in steps), "e2e": sum(e2e_s) / len(e2e_s), "n": len(probs)}
+    gathered = gather(world, per_rank)
+    if rank != 0:
+        return None
+    t_max = max(g["t"] for g in gathered)
+    total = sum(g["n"] for g in gathered)
+    ci = np.array([r.iterations for r in cold])
+    wi = np.array([r.iterations for r in warm])
+    nnz = probs[0].A_ub.nnz + probs[0].A_eq.nnz
+    n_, m_ = probs[0].n_vars, probs[0].n_ineq + probs[0].n_eq
+    per_it = 16 * nnz + 4 * (m_ + 1) + 4 * n_ + 20 * m_ + 4 * (n_ + 1) + 4 * m_ + 28 * n_ + 16 * m_
+    solve_s = np.mean([s_[1] for s_ in steps])
+    achieved = float(wi.sum()) * per_it / solve_s / 1e9
+    fwd_launches = 9 + 4 * net.layers
+    line = {
+        "metric": METRIC,
+        "value": total * args.steps / t_max, "unit": "solves/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t_max * 1e3 / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": (f"learned warm start: transportation family 200x400 (n=80k, m=600, nnz=160k), "
+                                f"{args.batch} held-out seeds per GPU, network trained on seeds 0..19999"),
+                   "tol_rel_kkt": args.tol, "mode": "GNN inference + warm-started batched PDHG (cold fallback on)",
+                   "precision": "fp32 iterates, fp64 checks; GNN bf16 weights, fp32 accumulation",
+                   "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)"},
+        "warm_iters_median": float(np.median(wi)), "cold_iters_median": float(np.median(ci)),
+        "warm_iters_mean": float(wi.mean()), "cold_iters_mean": float(ci.mean()),
+        "warm_used": int(sum(r.stats["warm_start_used"] for r in warm)),
+        "warm_optimal": int(sum(r.status == "optimal" for r in warm)),
+        "cold_optimal": int(sum(r.status == "optimal" for r in cold)),
+        "max_rel_kkt_warm": float(max(r.rel_kkt for r in warm)),
+        "gnn_inference_s_per_solve": float(np.mean([s_[0] for s_ in steps])) / len(probs),
+        "warm_batched_s_per_solve": t_max / args.steps / total * world,
+        "cold_batched_s_per_solve": float(np.mean(t_cold)) / len(probs),
+        "cold_single_s_per_solve": float(np.mean([s_[0] for s_ in single])),
+        "cold_single_iters_median": float(np.median([s_[1] for s_ in single])),
+        "cold_single_sample": len(single),
+        "gpu_launches": args.steps * (3 + fwd_launches * ((len(probs) + 15) // 16)),
+        "e2e": {"value": total / max(g["e2e"] for g in gathered), "unit": "solves/s",
+                "sec_per_batch": max(g["e2e"] for g in gathered),
+                "h2d_bytes_per_step": int(sum(problem_bytes(p) for p in probs)),
+                "d2h_bytes_per_step": int(sum(8 * (p.n_vars + p.n_ineq + p.n_eq) for p in probs))},
+        "roofline": {"bound": "hbm", "kernel": "k_batch_solve (persistent, warm-started)",
+                     "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_kind": peak_kind, "algorithmic_bytes": float(wi.sum()) * per_it, "traffic": None},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+    return line
+
+
 def cpu_baseline(p, args):
     s = reference_sample(p, args.cpu_budget)
     ref_iters = load_reference_iterations(args.config)
@@ -480,8 +620,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", type=int, default=1,
                     help="0: planted 200x500; 1: transportation 1000x2000 (default); 2: power-law 1Mx2M; "
-                         "3: batched planted LPs (--batch of them)")
-    ap.add_argument("--batch", type=int, default=4096)
+                         "3: batched planted LPs (--batch of them); 4: learned warm start on the "
+                         "transportation family (--batch held-out seeds)")
+    ap.add_argument("--batch", type=int, default=None,
+                    help="instances per GPU: config 3 default 4096, config 4 default 1000")
+    ap.add_argument("--single-sample", type=int, default=32)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=TOL)
     ap.add_argument("--max-iters", type=int, default=100000)
@@ -497,7 +640,11 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank, world)
     elif args.config == 3:
+        args.batch = args.batch or 4096
         run_batch(args, rank, world)
+    elif args.config == 4:
+        args.batch = args.batch or 1000
+        run_warmstart(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

@@ -6,7 +6,7 @@
  * of a parametric LP family (one sparsity pattern, per-instance c / b).  No
  * counterpart in the reference: it always starts PDHG from zero
  * (solver/lp/pdhg.py:175-176); the prediction is consumed by
- * sps_set_warm_start / sps_batch_set_warm_start, whose cold-start fallback
+ * sps_set_warm_start / sps_batch_set_warm_starts, whose cold-start fallback
  * keeps a bad prediction from slowing a solve down.
  *
  * Network (hidden width H, L layers; variable nodes j, constraint nodes i,
@@ -40,7 +40,8 @@ typedef struct {
     const int32_t *con_ptr;        /* CSR by constraint: n_con + 1 offsets */
     const int32_t *con_idx;        /*   variable of each edge */
     const float   *con_val;        /*   A_ij of each edge */
-    int32_t f_var, f_con;          /* input feature widths (1..8) */
+    int32_t f_var, f_con;          /* input feature widths (1..8); 1 and 1 with lp_features */
+    const int8_t  *con_kind;       /* 1 = '<=' row, 0 = '=' row (NULL = all '='); used by lp_features */
 } sps_gnn_graph;
 
 typedef struct {
@@ -51,7 +52,13 @@ typedef struct {
     float loss_x, loss_y, loss_omega;   /* loss weights */
     int32_t max_batch;             /* instances per call */
     int32_t device;
-    int32_t reserved[6];
+    int32_t lp_features;           /* 1: the inputs are an LP's scaled costs (var_feat, one per
+                                      variable) and right-hand sides (con_feat, one per row); the
+                                      device expands them to the network's features
+                                      var [c_j, gap_le_j, gap_eq_j, 1], con [b_i, kind_i, cmin_i, 1]
+                                      with cmin_i = min of c over row i and gap_le_j / gap_eq_j the
+                                      mean of c_j - cmin_i over the '<=' / '=' rows of column j */
+    int32_t reserved[5];
 } sps_gnn_options;
 
 typedef struct sps_gnn sps_gnn;

@@ -79,7 +79,7 @@ class GnnGraph(C.Structure):
     _fields_ = [
         ("n_var", C.c_int32), ("n_con", C.c_int32),
         ("con_ptr", _i32p), ("con_idx", _i32p), ("con_val", C.POINTER(C.c_float)),
-        ("f_var", C.c_int32), ("f_con", C.c_int32),
+        ("f_var", C.c_int32), ("f_con", C.c_int32), ("con_kind", C.POINTER(C.c_int8)),
     ]
 
 
@@ -88,7 +88,8 @@ class GnnOptions(C.Structure):
         ("hidden", C.c_int32), ("layers", C.c_int32), ("seed", C.c_uint64),
         ("lr", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("eps", C.c_float),
         ("loss_x", C.c_float), ("loss_y", C.c_float), ("loss_omega", C.c_float),
-        ("max_batch", C.c_int32), ("device", C.c_int32), ("reserved", C.c_int32 * 6),
+        ("max_batch", C.c_int32), ("device", C.c_int32), ("lp_features", C.c_int32),
+        ("reserved", C.c_int32 * 5),
     ]
 
 

@@ -427,6 +427,61 @@ __global__ void k_to_bf16(const float* __restrict__ p, __nv_bfloat16* __restrict
         pb[t] = __float2bfloat16_rn(p[t]);
 }
 
+// ---- LP features (lp_features): constraint side, one warp per (instance, row) --------
+// cmin = min of c over the row's columns (0 for an empty row); fc = [b, kind, cmin, 1]
+__global__ void __launch_bounds__(kT) k_lp_con_features(const int32_t* __restrict__ ptr,
+                                                         const int32_t* __restrict__ idx,
+                                                         const int8_t* __restrict__ kind,
+                                                         const float* __restrict__ c, const float* __restrict__ b,
+                                                         int n, int m, int batch, float* __restrict__ fc,
+                                                         float* __restrict__ cmin) {
+    const int lane = threadIdx.x & 31;
+    const int64_t rows = (int64_t)m * batch;
+    for (int64_t w = (blockIdx.x * (int64_t)kT + threadIdx.x) >> 5; w < rows; w += ((int64_t)gridDim.x * kT) >> 5) {
+        const int64_t s = w / m;
+        const int r = int(w % m);
+        const float* cs = c + s * (int64_t)n;
+        float v = INFINITY;
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) v = fminf(v, cs[idx[k]]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0) {
+            const float cm = ptr[r + 1] > ptr[r] ? v : 0.f;
+            cmin[w] = cm;
+            fc[w * 4 + 0] = b[w];
+            fc[w * 4 + 1] = float(kind[r]);
+            fc[w * 4 + 2] = cm;
+            fc[w * 4 + 3] = 1.f;
+        }
+    }
+}
+
+// variable side, one thread per (instance, column): fv = [c, mean gap over '<=' rows,
+// mean gap over '=' rows, 1] with gap = c - cmin(row)
+__global__ void __launch_bounds__(kT) k_lp_var_features(const int32_t* __restrict__ ptr,
+                                                        const int32_t* __restrict__ idx,
+                                                        const int8_t* __restrict__ kind,
+                                                        const float* __restrict__ c, const float* __restrict__ cmin,
+                                                        int n, int m, int batch, float* __restrict__ fv) {
+    const int64_t total = (int64_t)n * batch;
+    for (int64_t t = blockIdx.x * (int64_t)kT + threadIdx.x; t < total; t += (int64_t)gridDim.x * kT) {
+        const int64_t s = t / n;
+        const int j = int(t % n);
+        const float cj = c[t];
+        float sle = 0.f, seq = 0.f;
+        int nle = 0, neq = 0;
+        for (int k = ptr[j]; k < ptr[j + 1]; ++k) {
+            const int r = idx[k];
+            const float d = cj - cmin[s * m + r];
+            if (kind[r]) { sle += d; ++nle; } else { seq += d; ++neq; }
+        }
+        fv[t * 4 + 0] = cj;
+        fv[t * 4 + 1] = sle / float(nle > 0 ? nle : 1);
+        fv[t * 4 + 2] = seq / float(neq > 0 ? neq : 1);
+        fv[t * 4 + 3] = 1.f;
+    }
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -436,6 +491,9 @@ struct sps_gnn {
     sps_gnn_graph g{};
     sps_gnn_options opt{};
     int H = 64, L = 3, Fv = 1, Fc = 1, n = 0, m = 0, B = 1;
+    int lpf = 0;                 // lp_features: inputs are scaled c and b, expanded on the device
+    float *craw = nullptr, *braw = nullptr, *cmin = nullptr;
+    int8_t* kind = nullptr;
     int64_t nnz = 0, np = 0;
     cudaStream_t st = nullptr;
     std::vector<void*> dev;
@@ -610,8 +668,18 @@ int upload_inputs(sps_gnn* g, int batch, const float* vf, const float* cf, const
                   const float* lt) {
     cudaStream_t st = g->st;
     const size_t nv = (size_t)g->n * batch, nc = (size_t)g->m * batch;
-    GNN_CK(cudaMemcpyAsync(g->fv, vf, sizeof(float) * nv * g->Fv, cudaMemcpyHostToDevice, st));
-    GNN_CK(cudaMemcpyAsync(g->fc, cf, sizeof(float) * nc * g->Fc, cudaMemcpyHostToDevice, st));
+    if (g->lpf) {
+        GNN_CK(cudaMemcpyAsync(g->craw, vf, sizeof(float) * nv, cudaMemcpyHostToDevice, st));
+        GNN_CK(cudaMemcpyAsync(g->braw, cf, sizeof(float) * nc, cudaMemcpyHostToDevice, st));
+        k_lp_con_features<<<grid_for((int64_t)nc * 32, kT), kT, 0, st>>>(g->cptr, g->cidx, g->kind, g->craw, g->braw,
+                                                                       g->n, g->m, batch, g->fc, g->cmin);
+        k_lp_var_features<<<grid_for((int64_t)nv, kT), kT, 0, st>>>(g->vptr, g->vidx, g->kind, g->craw, g->cmin,
+                                                                  g->n, g->m, batch, g->fv);
+        GNN_CK(cudaGetLastError());
+    } else {
+        GNN_CK(cudaMemcpyAsync(g->fv, vf, sizeof(float) * nv * g->Fv, cudaMemcpyHostToDevice, st));
+        GNN_CK(cudaMemcpyAsync(g->fc, cf, sizeof(float) * nc * g->Fc, cudaMemcpyHostToDevice, st));
+    }
     if (xt) GNN_CK(cudaMemcpyAsync(g->xt, xt, sizeof(float) * nv, cudaMemcpyHostToDevice, st));
     if (yt) GNN_CK(cudaMemcpyAsync(g->yt, yt, sizeof(float) * nc, cudaMemcpyHostToDevice, st));
     if (lt) GNN_CK(cudaMemcpyAsync(g->lt, lt, sizeof(float) * batch, cudaMemcpyHostToDevice, st));
@@ -701,10 +769,17 @@ int sps_gnn_create(const sps_gnn_graph* gr, const sps_gnn_options* opt_in, sps_g
             g_gnn_create_error = "edge " + std::to_string(k) + ": variable out of range or non-finite value";
             return -1;
         }
+    if (opt.lp_features && (gr->f_var != 1 || gr->f_con != 1)) {
+        g_gnn_create_error = "lp_features takes one input per variable (c) and per row (b): f_var = f_con = 1";
+        return -1;
+    }
     auto g = new sps_gnn();
     g->g = *gr;
     g->opt = opt;
-    g->H = opt.hidden; g->L = opt.layers; g->Fv = gr->f_var; g->Fc = gr->f_con;
+    g->lpf = opt.lp_features ? 1 : 0;
+    g->H = opt.hidden; g->L = opt.layers;
+    g->Fv = g->lpf ? 4 : gr->f_var;
+    g->Fc = g->lpf ? 4 : gr->f_con;
     g->n = n; g->m = m; g->B = opt.max_batch; g->nnz = nnz;
     const int H = g->H;
     // parameter offsets
@@ -719,6 +794,7 @@ int sps_gnn_create(const sps_gnn_graph* gr, const sps_gnn_options* opt_in, sps_g
     // host graph: degrees, normalised values, CSR by variable
     std::vector<int32_t> degc(m), degv(n, 0), vptr(n + 1, 0), vidx(nnz);
     std::vector<float> ac_c(nnz), av_c(nnz), av_v(nnz), ac_v(nnz);
+    std::vector<int8_t> kd(m, 0);
     for (int i = 0; i < m; ++i) degc[i] = gr->con_ptr[i + 1] - gr->con_ptr[i];
     for (int64_t k = 0; k < nnz; ++k) degv[gr->con_idx[k]]++;
     for (int j = 0; j < n; ++j) vptr[j + 1] = vptr[j] + degv[j];
@@ -759,6 +835,13 @@ int sps_gnn_create(const sps_gnn_graph* gr, const sps_gnn_options* opt_in, sps_g
             GNN_CK(g->alloc(&g->PB, g->np));
             const int64_t B = g->B, NV = (int64_t)n * B, NC = (int64_t)m * B;
             GNN_CK(g->alloc(&g->fv, NV * g->Fv)); GNN_CK(g->alloc(&g->fc, NC * g->Fc));
+            if (g->lpf) {
+                GNN_CK(g->alloc(&g->craw, NV)); GNN_CK(g->alloc(&g->braw, NC)); GNN_CK(g->alloc(&g->cmin, NC));
+                GNN_CK(g->alloc(&g->kind, m));
+                if (gr->con_kind)
+                    for (int i = 0; i < m; ++i) kd[i] = gr->con_kind[i] ? 1 : 0;
+                GNN_CK(up(g->kind, kd.data(), (size_t)m));
+            }
             GNN_CK(g->alloc(&g->xt, NV)); GNN_CK(g->alloc(&g->yt, NC)); GNN_CK(g->alloc(&g->lt, B));
             g->HV.resize(g->L + 1); g->HC.resize(g->L + 1); g->AV.resize(g->L); g->AC.resize(g->L);
             for (int l = 0; l <= g->L; ++l) { GNN_CK(g->alloc(&g->HV[l], NV * H)); GNN_CK(g->alloc(&g->HC[l], NC * H)); }

@@ -15,7 +15,10 @@ the columns of row i):
                  mean over its '=' rows of (c_j - cmin_i), 1]      (costs / c_scale)
   constraint i: [b_i / b_scale, 1 if '<=' row else 0, cmin_i / c_scale, 1]
 The cost gaps tell each variable how far it is from the cheapest column of its
-rows, which mean aggregation alone cannot compute.
+rows, which mean aggregation alone cannot compute.  With ``lp_features``
+(default) the network takes only the scaled c and b and the device builds these
+features (``k_lp_con_features`` / ``k_lp_var_features``); ``host_features`` is
+the same construction in NumPy (the tests compare the two).
 Targets: x* / x_scale, y* / y_scale, log omega* (omega in the engine's scaled space).
 """
 
@@ -45,7 +48,8 @@ class WarmStartGNN:
     """A warm-start predictor for the family of ``template`` (same K pattern)."""
 
     def __init__(self, template, hidden: int = 64, layers: int = 3, seed: int = 0, lr: float = 1e-3,
-                 max_batch: int = 8, device: int = 0, loss_weights=(1.0, 1.0, 0.1), scales: dict | None = None):
+                 max_batch: int = 8, device: int = 0, loss_weights=(1.0, 1.0, 0.1), scales: dict | None = None,
+                 lp_features: bool = True):
         self.lib = N.load()
         K = stacked_rows(template)
         K.sort_indices()
@@ -72,12 +76,17 @@ class WarmStartGNN:
         self._w_le, self._w_eq = le.astype(float), (~le).astype(float)
         self._cnt_le = np.maximum(np.bincount(self._idx, weights=self._w_le, minlength=self.n), 1)
         self._cnt_eq = np.maximum(np.bincount(self._idx, weights=self._w_eq, minlength=self.n), 1)
-        gr = N.GnnGraph(self.n, self.m, N.i32p(self._ptr), N.i32p(self._idx), N.f32p(self._val), FV, FC)
+        self.lp_features = bool(lp_features)
+        self._kind8 = np.ascontiguousarray(self._kind.astype(np.int8))
+        fin_v, fin_c = (1, 1) if self.lp_features else (FV, FC)
+        gr = N.GnnGraph(self.n, self.m, N.i32p(self._ptr), N.i32p(self._idx), N.f32p(self._val), fin_v, fin_c,
+                        self._kind8.ctypes.data_as(C.POINTER(C.c_int8)))
         o = N.GnnOptions()
         self.lib.sps_gnn_options_init(C.byref(o))
         o.hidden, o.layers, o.seed, o.lr = hidden, layers, seed, lr
         o.loss_x, o.loss_y, o.loss_omega = loss_weights
         o.max_batch, o.device = max_batch, device
+        o.lp_features = 1 if self.lp_features else 0
         h = C.c_void_p()
         rc = self.lib.sps_gnn_create(C.byref(gr), C.byref(o), C.byref(h))
         if rc != 0:
@@ -87,6 +96,14 @@ class WarmStartGNN:
 
     # ---------------------------------------------------------------- data
     def features_from(self, c, b):
+        """The network's inputs for one instance's c and b: scaled (c, b) as columns with
+        ``lp_features``, else the expanded features of ``host_features``."""
+        if self.lp_features:
+            return (np.asarray(c, float) / self.scales["c"]).astype(np.float32)[:, None], \
+                   (np.asarray(b, float) / self.scales["b"]).astype(np.float32)[:, None]
+        return self.host_features(c, b)
+
+    def host_features(self, c, b):
         """(var features n x 4, constraint features m x 4) from one instance's c and b."""
         c = np.asarray(c, float) / self.scales["c"]
         ce = c[self._idx]
@@ -177,7 +194,8 @@ class WarmStartGNN:
     # ---------------------------------------------------------------- persistence
     def save(self, path: str) -> None:
         np.savez(path, params=self.params(), hidden=self.hidden, layers=self.layers, n=self.n, m=self.m,
-                 nnz=self.nnz, scales=np.array([self.scales[k] for k in ("c", "b", "x", "y")]))
+                 nnz=self.nnz, scales=np.array([self.scales[k] for k in ("c", "b", "x", "y")]),
+                 lp_features=int(self.lp_features))
 
     @classmethod
     def load(cls, path: str, template, **kw) -> "WarmStartGNN":

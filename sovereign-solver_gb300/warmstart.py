@@ -3,7 +3,7 @@
 Pipeline (every step on the GPU through this package):
   1. ``solve_family`` solves the training seeds cold with the batched solver
      (tolerance 1e-4) and keeps each solution (x sparse, y, the final primal
-     weight) plus the instance's scaled costs (FP16) as features;
+     weight) plus the instance's scaled costs (FP16) and right-hand sides;
   2. ``train`` fits ``WarmStartGNN`` on them with its own forward / backward /
      Adam kernels (minibatches of ``net.max_batch`` instances);
   3. ``evaluate`` compares, on held-out seeds, cold single-instance PDHG with the
@@ -29,7 +29,7 @@ if __package__ in (None, ""):
     __package__ = "sovereign_solver_gb300"
 
 from .batch import PDHGBatch
-from .gnn import FC, FV, WarmStartGNN
+from .gnn import WarmStartGNN
 from .pdhg import PDHGEngine
 from .problem import Problem
 from .workloads import TransportFamily
@@ -53,8 +53,8 @@ def transport_instances(fam: TransportFamily, template: Problem, seeds):
 @dataclass
 class FamilyData:
     seeds: np.ndarray
-    vfeat: np.ndarray               # (k, n, FV - 1) FP16 variable features (the constant column dropped)
-    cfeat: np.ndarray               # (k, m, FC - 1) FP32 constraint features
+    c: np.ndarray                   # (k, n) FP16: c / c_scale
+    b: np.ndarray                   # (k, m) FP32: b / b_scale
     x_ptr: np.ndarray               # sparse x* (CSR over instances)
     x_idx: np.ndarray
     x_val: np.ndarray               # FP32, original units
@@ -77,8 +77,8 @@ def solve_family(net: WarmStartGNN, fam: TransportFamily, template: Problem, see
     """Cold batched solves of ``seeds``; solutions and features for training."""
     seeds = np.asarray(seeds)
     k, n, m = len(seeds), net.n, net.m
-    vfeat = np.empty((k, n, FV - 1), np.float16)
-    cfeat = np.empty((k, m, FC - 1), np.float32)
+    cs = np.empty((k, n), np.float16)
+    bs = np.empty((k, m), np.float32)
     y = np.empty((k, m), np.float32)
     omega = np.empty(k)
     its = np.empty(k, np.int64)
@@ -95,9 +95,8 @@ def solve_family(net: WarmStartGNN, fam: TransportFamily, template: Problem, see
         t_solve += time.perf_counter() - t
         for q, (p, r) in enumerate(zip(probs, res)):
             i = s0 + q
-            fv, fc = net.features(p)
-            vfeat[i] = fv[:, :-1]
-            cfeat[i] = fc[:, :-1]
+            cs[i] = p.c / net.scales["c"]
+            bs[i] = np.concatenate([p.b_ub, p.b_eq]) / net.scales["b"]
             y[i] = r.y
             omega[i] = r.stats["primal_weight"]
             its[i] = r.iterations
@@ -109,19 +108,14 @@ def solve_family(net: WarmStartGNN, fam: TransportFamily, template: Problem, see
         if log:
             log(f"solved {min(k, s0 + chunk)}/{k} seeds ({t_solve:.1f}s in solves; "
                 f"median {np.median(its[:s0 + len(sl)]):.0f} iterations)")
-    return FamilyData(seeds, vfeat, cfeat, np.asarray(xp, np.int64), np.concatenate(xi) if xi else np.zeros(0, np.int32),
+    return FamilyData(seeds, cs, bs, np.asarray(xp, np.int64), np.concatenate(xi) if xi else np.zeros(0, np.int32),
                       np.concatenate(xv) if xv else np.zeros(0, np.float32), y, omega, its, opt, t_solve)
 
 
 def _batch_arrays(net: WarmStartGNN, data: FamilyData, rows):
     fvs, fcs, xts, yts, lts = [], [], [], [], []
     for i in rows:
-        fv = np.empty((net.n, FV), np.float32)
-        fv[:, :-1] = data.vfeat[i]
-        fv[:, -1] = 1.0
-        fc = np.empty((net.m, FC), np.float32)
-        fc[:, :-1] = data.cfeat[i]
-        fc[:, -1] = 1.0
+        fv, fc = net.features_from(data.c[i].astype(float) * net.scales["c"], data.b[i].astype(float) * net.scales["b"])
         xt, yt, lt = net.targets(data.x_dense(i, net.n), data.y[i], data.omega[i])
         fvs.append(fv); fcs.append(fc); xts.append(xt); yts.append(yt); lts.append(lt)
     return fvs, fcs, xts, yts, np.asarray(lts, np.float32)

@@ -35,7 +35,7 @@ def _data(net, B, seed=1):
 @pytest.mark.parametrize("hidden", [64, 32])
 def test_gradients_match_oracle(hidden):
     p = _template()
-    with WarmStartGNN(p, hidden=hidden, layers=3, seed=3, max_batch=4) as net:
+    with WarmStartGNN(p, hidden=hidden, layers=3, seed=3, max_batch=4, lp_features=False) as net:
         fvs, fcs, xts, yts, lts = _data(net, 3)
         loss, g = net.loss_grad(fvs, fcs, xts, yts, lts)
         params = net.params()
@@ -53,7 +53,7 @@ def test_gradients_match_oracle(hidden):
 
 def test_forward_matches_oracle():
     p = _template(seed=4)
-    with WarmStartGNN(p, seed=5, max_batch=2) as net:
+    with WarmStartGNN(p, seed=5, max_batch=2, lp_features=False) as net:
         fvs, fcs, *_ = _data(net, 2, seed=6)
         X, Y, Lw = net.predict_features(fvs, fcs)
         lay = gnn_ref.Layout(64, 3, 4, 4)
@@ -69,7 +69,7 @@ def test_training_lowers_loss_and_is_reproducible():
     p = _template(seed=7)
     runs = []
     for _ in range(2):
-        with WarmStartGNN(p, seed=11, lr=3e-3, max_batch=4) as net:
+        with WarmStartGNN(p, seed=11, lr=3e-3, max_batch=4, lp_features=False) as net:
             fvs, fcs, xts, yts, lts = _data(net, 4, seed=8)
             losses = [net.train_step(fvs, fcs, xts, yts, lts) for _ in range(150)]
             runs.append((losses, net.params()))
@@ -81,7 +81,7 @@ def test_training_lowers_loss_and_is_reproducible():
 
 def test_batch_limit_and_bad_params():
     p = _template()
-    with WarmStartGNN(p, max_batch=2) as net:
+    with WarmStartGNN(p, max_batch=2, lp_features=False) as net:
         fvs, fcs, xts, yts, lts = _data(net, 3)
         with pytest.raises(RuntimeError):
             net.train_step(fvs, fcs, xts, yts, lts)
@@ -89,3 +89,22 @@ def test_batch_limit_and_bad_params():
         bad[0] = np.nan
         with pytest.raises(RuntimeError):
             net.set_params(bad)
+
+
+def test_device_lp_features_match_host_features():
+    """lp_features: the device expansion of (c, b) gives the predictions of the NumPy features."""
+    p = _template(seed=9)
+    rng = np.random.default_rng(10)
+    cs = [rng.random(p.n_vars) + 0.1 for _ in range(3)]
+    bs = [rng.random(p.n_ineq + p.n_eq) + 0.5 for _ in range(3)]
+    with WarmStartGNN(p, seed=12, max_batch=4, lp_features=True) as dev, \
+            WarmStartGNN(p, seed=12, max_batch=4, lp_features=False, scales=dev.scales) as host:
+        np.testing.assert_array_equal(dev.params(), host.params())
+        fd = [dev.features_from(c, b) for c, b in zip(cs, bs)]
+        assert fd[0][0].shape == (p.n_vars, 1) and fd[0][1].shape == (p.n_ineq + p.n_eq, 1)
+        fh = [host.host_features(c, b) for c, b in zip(cs, bs)]
+        Xd, Yd, Ld = dev.predict_features([f[0] for f in fd], [f[1] for f in fd])
+        Xh, Yh, Lh = host.predict_features([f[0] for f in fh], [f[1] for f in fh])
+    np.testing.assert_allclose(Xd, Xh, rtol=1e-4, atol=1e-5 * np.abs(Xh).max())
+    np.testing.assert_allclose(Yd, Yh, rtol=1e-4, atol=1e-5 * np.abs(Yh).max())
+    np.testing.assert_allclose(Ld, Lh, rtol=1e-4, atol=1e-5)
