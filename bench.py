@@ -297,6 +297,38 @@ def run_ours(args, rank, world):
     return line
 
 
+def _ref_solve_one(k):
+    """Worker (spawned, one OpenMP thread): the reference algorithm on batched instance k."""
+    os.environ["OMP_NUM_THREADS"] = "1"
+    import sovereign_solver_gb300.workloads as wl
+    from oracle import pdhg_ref_c
+    p = wl.batch_planted_lp(k)[0]
+    t0 = time.perf_counter()
+    r = pdhg_ref_c.solve(p, max_iters=100000, tol=1e-4)
+    return k, r.status, r.iterations, time.perf_counter() - t0
+
+
+def batch_cpu_baseline(args):
+    """Reference algorithm (C restatement of solver/lp/pdhg.py, one thread per
+    process) on every 128th instance of the batch (32 LPs), one spawned process
+    per host core; solves/s = 32 / wall time."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    ks = list(range(0, 4096, 128))
+    procs = max(1, min(16, os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    with ProcessPoolExecutor(procs, mp_context=mp.get_context("spawn")) as ex:
+        out = list(ex.map(_ref_solve_one, ks))
+    wall = time.perf_counter() - t0
+    per = [o[3] for o in out]
+    return {"value": len(ks) / wall, "unit": "solves/s", "cores": procs, "kind": "port",
+            "sample": (f"reference algorithm (C restatement of solver/lp/pdhg.py) to 1e-4 on instances "
+                       f"0, 128, ..., 3968 of the batch ({len(ks)} LPs), {procs} single-threaded processes, "
+                       f"{wall:.1f} s wall; per-LP {np.median(per):.2f} s median, "
+                       f"{sum(o[1] == 'optimal' for o in out)}/{len(ks)} optimal"),
+            "serial_s_per_solve": float(np.mean(per))}
+
+
 def run_batch(args, rank, world):
     """Batched workload: ``--batch`` LPs of the config-0 construction with m
     log-uniform in [50, 5000], n = m * U[1.5, 3], 10-50 nonzeros per column,
@@ -393,6 +425,8 @@ def run_batch(args, rank, world):
                      "peak_kind": peak_kind, "algorithmic_bytes": alg, "traffic": None},
         "clocks": clk.summary(),
     }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = batch_cpu_baseline(args)
     print(json.dumps(line), flush=True)
     return line
 
@@ -533,13 +567,15 @@ def run_warmstart(args, rank, world):
                      "peak_kind": peak_kind, "algorithmic_bytes": float(wi.sum()) * per_it, "traffic": None},
         "clocks": clk.summary(),
     }
+    if args.cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(probs[0], args, ref_key=f"4:{TEST_SEED0}")
     print(json.dumps(line), flush=True)
     return line
 
 
-def cpu_baseline(p, args):
+def cpu_baseline(p, args, ref_key=None):
     s = reference_sample(p, args.cpu_budget)
-    ref_iters = load_reference_iterations(args.config)
+    ref_iters = load_reference_iterations(ref_key or args.config)
     out = {"unit": "solves/s", "cores": s["threads"], "kind": "port",
            "s_per_iter": s["s_per_iter"],
            "sample": (f"{s['iters']} iterations of the reference algorithm (C+OpenMP restatement of "

@@ -182,11 +182,13 @@ typedef struct {
     int32_t blocks;             /* persistent blocks */
     int32_t escalated;          /* instances that stalled in FP32 and were finished in FP64 by the
                                    single-LP engine after the persistent launch (in solve_ms) */
-    int32_t reserved[4];
+    int32_t lanes_per_row;      /* row-pass schedule (4, 8, 16, 32 lanes per row; timed) */
+    int32_t reserved[3];
 } sps_batch_stats;
 
 /* Pack `count` problems, upload and scale them (one block per instance) and pick
- * the schedule (opt->batch_group, or timed on a sample when 0). */
+ * the schedule: lanes per column (opt->batch_group, or timed on a sample when 0),
+ * then lanes per row (timed). */
 int sps_batch_create(int32_t count, const sps_problem_desc *probs, const sps_options *opt, sps_batch **out);
 /* Solve every instance: one persistent launch, captured in a CUDA graph on the
  * first call and replayed afterwards; blocking. */

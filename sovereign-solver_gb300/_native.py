@@ -51,7 +51,7 @@ class BatchStats(C.Structure):
     _fields_ = [
         ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("total_iterations", C.c_int64),
         ("optimal", C.c_int32), ("lanes_per_column", C.c_int32), ("blocks", C.c_int32),
-        ("escalated", C.c_int32), ("reserved", C.c_int32 * 4),
+        ("escalated", C.c_int32), ("lanes_per_row", C.c_int32), ("reserved", C.c_int32 * 3),
     ]
 
 

@@ -24,8 +24,9 @@ from .result import SolveResult
 class PDHGBatch:
     """A batch of problems resident on the GPU.
 
-    ``batch_group`` picks the lanes per column of the column pass (4, 8, 16,
-    32); 0 lets the library time the candidates on a sample of the batch.
+    ``batch_group`` picks the lanes per column of the column pass (1, 2, 4, 8,
+    16, 32); 0 lets the library time the candidates on a sample of the batch.
+    The lanes per row of the row pass (4, 8, 16, 32) are always timed.
     ``escalate``: "fp64" (FP64 continuation of stalled instances), "stop"
     (status "stalled") or "off" (FP32 to the iteration limit).
     """

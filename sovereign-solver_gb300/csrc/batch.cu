@@ -152,7 +152,7 @@ struct ColCheckE {
 };
 
 struct View {                 // one instance's arrays
-    int n, m, G;
+    int n, m, G, Gr;              // lanes per column, lanes per row
     const int32_t *rptr, *ridx, *cptr, *cidx;
     const float *rval, *cval;
     const int8_t* kind;
@@ -166,7 +166,7 @@ struct View {                 // one instance's arrays
 __device__ __forceinline__ View make_view(const Args& A, const Inst& I, int G) {
     const Arrays& a = A.a;
     View v;
-    v.n = I.n; v.m = I.m; v.G = G;
+    v.n = I.n; v.m = I.m; v.G = G & 0xFF; v.Gr = G >> 8 ? G >> 8 : 32;
     v.rptr = a.rptr + I.rp; v.ridx = a.ridx + I.re; v.rval = a.rval + I.re;
     v.cptr = a.cptr + I.cp; v.cidx = a.cidx + I.ce; v.cval = a.cval + I.ce;
     v.kind = a.kind + I.vr;
@@ -204,7 +204,7 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     for (int q = 0; q < 8; ++q) mine[q * kBlock] = 0.0;
     RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w,
                  mine};
-    group_rows<32, 2, double>(v.rptr, v.ridx, v.rval, v.m,
+    group_rows_r<2, double>(v.Gr, v.rptr, v.ridx, v.rval, v.m,
                               Gather2{has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], inv_w}, er);
     slot_sums<8>(slots, sm);                       // sm[0..7]: row partials
     for (int q = 0; q < 10; ++q) mine[q * kBlock] = 0.0;
@@ -300,9 +300,9 @@ __device__ void start_point(const Args& A, int k, const Inst& I, const View& v, 
     }
     __syncthreads();
     StoreE sx{v.AX[0]};
-    group_rows<32, 1, float>(v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[0]}, sx);
+    group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[0]}, sx);
     StoreE sy{v.ATY[0]};
-    group_rows_dyn<1, float>(G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[0]}, sy);
+    group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[0]}, sy);
     __syncthreads();
     check_and_apply(v, I, c, sm, slots, A.deadline);
 }
@@ -339,7 +339,7 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             if (c.done || c.iters >= c.max_iters) break;
             int cur = c.cur;
             RowStepE er{v.b, v.AX[cur], v.Y[cur], v.kind, v.AX[1 - cur], v.Y[1 - cur], float(c.eta * c.omega)};
-            group_rows<32, 1, float>(v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur]}, er);
+            group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur]}, er);
             double t2[2] = {double(er.dy2), double(er.inter)};
             block_sum<2>(t2, sm);
             if (threadIdx.x == 0) decide_step(c, t2[0], t2[1]);
@@ -350,7 +350,7 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             float dx2;
             if (c.accepted) {
                 ColStepE ec{v.X[cur], v.c, v.lo, v.hi, v.xl, v.ATY[cur], v.X[1 - cur], v.xs, tau, wgt};
-                group_rows_dyn<1, float>(G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur]}, ec);
+                group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur]}, ec);
                 dx2 = ec.dx2;
                 for (int i = threadIdx.x; i < v.m; i += kBlock) v.ys[i] += wgt * (v.Y[cur][i] - v.yl[i]);
             } else {
@@ -516,7 +516,7 @@ using sps::batch::Inst;
 struct sps_batch {
     int32_t count = 0;
     sps_options opt{};
-    int32_t G = 8, blocks = 0;
+    int32_t G = 8, Gr = 32, blocks = 0;      // lanes per column / per row, persistent blocks
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<Inst> inst;
@@ -876,29 +876,48 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         b->setup_ms = ms;
     }
     // ---- lanes per column: given, or timed on a sample of the batch
-    const int g_opt = opt.batch_group;
-    if (g_opt == 1 || g_opt == 2 || g_opt == 4 || g_opt == 8 || g_opt == 16 || g_opt == 32) {
-        b->G = opt.batch_group;
-    } else {
+    // schedule: lanes per column given (batch_group) or timed; lanes per row timed
+    // second with the chosen column schedule (32 attempts and one check per
+    // candidate on a sample of the largest instances)
+    {
         sps_batch* bb = bp;
         const int32_t sample = std::min<int32_t>(count, 2 * bb->blocks);
-        double best = 1e300;
-        for (int G : {1, 2, 4, 8, 16, 32}) {
-            // 32 attempts and one check per candidate on the sample (largest instances first)
+        auto time_one = [&](int sched, float* ms) -> bool {
             sps::batch::Args A{bb->d_inst, bb->d_order, sample, 32, 32, 0.0, bb->d_deadline, bb->arr, bb->d_out,
                                bb->d_counter, 0};
             cudaMemsetAsync(bb->d_counter, 0, sizeof(uint32_t), bb->st);
             cudaEventRecord(bb->e0, bb->st);
-            sps::batch::k_batch_solve<<<std::min(bb->blocks, sample), sps::kBlock, 0, bb->st>>>(A, G);
+            sps::batch::k_batch_solve<<<std::min(bb->blocks, sample), sps::kBlock, 0, bb->st>>>(A, sched);
             cudaEventRecord(bb->e1, bb->st);
-            if (cudaStreamSynchronize(bb->st) != cudaSuccess) {
+            if (cudaStreamSynchronize(bb->st) != cudaSuccess) return false;
+            cudaEventElapsedTime(ms, bb->e0, bb->e1);
+            return true;
+        };
+        const int g_opt = opt.batch_group;
+        int gc = 0, gr = 32;
+        double best = 1e300;
+        float ms = 0.f;
+        if (g_opt == 1 || g_opt == 2 || g_opt == 4 || g_opt == 8 || g_opt == 16 || g_opt == 32) {
+            gc = g_opt;
+        } else {
+            for (int G : {1, 2, 4, 8, 16, 32}) {
+                if (!time_one(sps::batch::pack_schedule(G, 32), &ms)) {
+                    sps::set_create_error(std::string("autotune: ") + cudaGetErrorString(cudaGetLastError()));
+                    return SPS_ERR_CUDA;
+                }
+                if (ms < best) { best = ms; gc = G; }
+            }
+        }
+        best = 1e300;
+        for (int R : {4, 8, 16, 32}) {
+            if (!time_one(sps::batch::pack_schedule(gc, R), &ms)) {
                 sps::set_create_error(std::string("autotune: ") + cudaGetErrorString(cudaGetLastError()));
                 return SPS_ERR_CUDA;
             }
-            float ms = 0;
-            cudaEventElapsedTime(&ms, bb->e0, bb->e1);
-            if (ms < best) { best = ms; bb->G = G; }
+            if (ms < best) { best = ms; gr = R; }
         }
+        bb->G = gc;
+        bb->Gr = gr;
     }
     *out = b.release();
     return SPS_OK;
@@ -915,13 +934,14 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     auto enqueue = [&](cudaStream_t s) {
         cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
         sps::batch::k_set_deadline<<<1, 32, 0, s>>>(b->d_deadline, tl);
-        sps::batch::k_batch_solve<<<b->blocks, sps::kBlock, 0, s>>>(A, b->G);
+        sps::batch::k_batch_solve<<<b->blocks, sps::kBlock, 0, s>>>(A, sps::batch::pack_schedule(b->G, b->Gr));
     };
     SPB_CK(cudaEventRecord(b->e0, b->st));
     if (b->opt.graph_mode != 0) {
         // one graph (counter reset, deadline, persistent solve), built once per
         // schedule and time limit and replayed by later solves
-        if (!b->gexec || b->gexec_G != b->G || b->gexec_tl != tl || b->gexec_warm != b->warm) {
+        const int sched = sps::batch::pack_schedule(b->G, b->Gr);
+        if (!b->gexec || b->gexec_G != sched || b->gexec_tl != tl || b->gexec_warm != b->warm) {
             if (b->gexec) { cudaGraphExecDestroy(b->gexec); b->gexec = nullptr; }
             cudaGraph_t g;
             cudaStream_t cap;
@@ -937,7 +957,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
             }
             cudaStreamDestroy(cap);
             SPB_CK(e);
-            b->gexec_G = b->G;
+            b->gexec_G = sched;
             b->gexec_tl = tl;
             b->gexec_warm = b->warm;
         }
@@ -981,6 +1001,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
         stats->setup_ms = b->setup_ms;
         stats->solve_ms = b->solve_ms;
         stats->lanes_per_column = b->G;
+        stats->lanes_per_row = b->Gr;
         stats->blocks = b->blocks;
         stats->escalated = n_esc;
         for (const Ctl& c : b->out) {

@@ -104,5 +104,20 @@ __device__ __forceinline__ void group_rows_dyn(int G, const int32_t* ptr, const 
     }
 }
 
+// Row passes: G lanes per row in {4, 8, 16, 32} (several rows per warp in flight).
+template <int NV, class Acc, class Gather, class Epi>
+__device__ __forceinline__ void group_rows_r(int G, const int32_t* ptr, const int32_t* idx, const float* val,
+                                             int count, const Gather& g, Epi& e) {
+    switch (G) {
+        case 4: group_rows<4, NV, Acc>(ptr, idx, val, count, g, e); break;
+        case 8: group_rows<8, NV, Acc>(ptr, idx, val, count, g, e); break;
+        case 16: group_rows<16, NV, Acc>(ptr, idx, val, count, g, e); break;
+        default: group_rows<32, NV, Acc>(ptr, idx, val, count, g, e); break;
+    }
+}
+
+// Schedule of a launch: lanes per column (low byte) and per row (next byte).
+__host__ __device__ constexpr int pack_schedule(int gc, int gr) { return gc | (gr << 8); }
+
 }  // namespace batch
 }  // namespace sps

@@ -8,6 +8,7 @@ exact with the reference on every golden vector) to a relative KKT tolerance of
 the reference's time per solve with these counts.
 
     python tests/golden/make_reference_iterations.py      # writes reference_iterations.json
+    python tests/golden/make_reference_iterations.py 3    # only the batched workload's sample
 """
 
 import json
@@ -25,12 +26,23 @@ CASES = {
     "0": lambda: wl.planted_lp(seed=0)[0],
     "1": lambda: wl.transportation_lp(1000, 2000, seed=0)[0],
 }
+# batched workload: every 128th instance of the 4096 (32 instances)
+for _k in range(0, 4096, 128):
+    CASES[f"3:{_k}"] = (lambda k: lambda: wl.batch_planted_lp(k)[0])(_k)
+# learned warm start: the first 8 held-out seeds of the transportation family
+_FAM = []
+for _s in range(8):
+    CASES[f"4:{10_000_000 + _s}"] = (lambda s: lambda: (_FAM or _FAM.append(wl.TransportFamily()) or _FAM)[0].problem(s))(
+        10_000_000 + _s)
 
 
 def main():
     out = {}
     path = os.path.join(HERE, "reference_iterations.json")
-    for key in sys.argv[1:] or sorted(CASES):
+    keys = sys.argv[1:] or sorted(CASES)
+    if keys == ["3"] or keys == ["4"]:
+        keys = sorted(k for k in CASES if k.startswith(keys[0] + ":"))
+    for key in keys:
         p = CASES[key]()
         t0 = time.perf_counter()
         r = pdhg_ref_c.solve(p, max_iters=100000, tol=1e-4)
