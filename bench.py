@@ -136,6 +136,12 @@ def problem_bytes(p) -> int:
     return tot + 8 * (3 * p.n_vars + p.n_ineq + p.n_eq)
 
 
+# dram__bytes_read.sum + dram__bytes_write.sum per launch of the iteration kernels,
+# from one ncu capture of the default workload (transportation LP 1000 x 2000,
+# seed 0, FP32 adaptive; --graph-mode 0 so the kernels are separate launches).
+MEASURED_TRAFFIC = {1: {"row": 40.19e6 + 0.01e6, "col": 64.34e6 + 2.31e6}}
+
+
 def iteration_bytes(p) -> dict:
     """Algorithmic HBM bytes per launch of the two fused iteration kernels (FP32).
 
@@ -251,12 +257,11 @@ def run_ours(args, rank, world):
     for a in pinned:
         lib.sps_unpin_host(a.ctypes.data)
 
-    per_rank = {"ms": sum(ms), "e2e_s": sum(e2e_s), "e2e_steps": len(e2e_s)}
+    per_rank = {"ms": sum(ms), "e2e_s": sum(e2e_s), "e2e_steps": len(e2e_s), "n": 1}
     gathered = gather(world, per_rank)
     if rank != 0:
         return None
-    t_max = max(g["ms"] for g in gathered) / 1e3
-    value = world * args.steps / t_max
+    value, t_max = job_throughput(gathered, "n", "ms", args.steps, 1e-3)
     e2e_t = max(g["e2e_s"] / g["e2e_steps"] for g in gathered)
     ib = iteration_bytes(p)
     dom = "col" if kt[1] >= kt[0] else "row"
@@ -286,7 +291,8 @@ def run_ours(args, rank, world):
         "kernel_ms": {"row_pass": kt[0], "col_pass": kt[1], "accept_rate": kt[2]},
         "roofline": {"bound": "hbm", "kernel": f"ad_{dom}_step (fused {'CSC' if dom == 'col' else 'CSR'} SpMV + update)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_kind": peak_kind, "algorithmic_bytes": ib[dom], "traffic": None,
+                     "peak_kind": peak_kind, "algorithmic_bytes": ib[dom],
+                     "traffic": MEASURED_TRAFFIC.get(args.config, {}).get(dom) if args.seed == 0 else None,
                      "other_pass_gbs": (ib["row" if dom == "col" else "col"] /
                                         ((kt[0] if dom == "col" else kt[1]) / 1e3) / 1e9)},
         "clocks": clk.summary(),
@@ -341,7 +347,7 @@ def run_batch(args, rank, world):
     from sovereign_solver_gb300 import _native as N, pdhg
 
     t = time.perf_counter()
-    probs, stars = make_batch(args.batch, first=rank * args.batch)
+    probs, stars = make_batch(args.batch, first=instance_range(rank, args.batch)[0])
     log(f"generated {len(probs)} instances in {time.perf_counter() - t:.1f}s")
     nnz = [p.A_eq.nnz + p.A_ub.nnz for p in probs]
     hbm, peak_kind = peaks()
@@ -395,9 +401,8 @@ def run_batch(args, rank, world):
     gathered = gather(world, per_rank)
     if rank != 0:
         return None
-    t_max = max(g["ms"] for g in gathered) / 1e3
+    value, t_max = job_throughput(gathered, "n", "ms", args.steps, 1e-3)
     total = sum(g["n"] for g in gathered)
-    value = total * args.steps / t_max
     e2e_t = max(g["e2e_s"] for g in gathered)
     achieved = alg / (t_max / args.steps) / 1e9
     line = {
@@ -452,7 +457,7 @@ def run_warmstart(args, rank, world):
 
     fam = TransportFamily()
     template = fam.problem(0)
-    seeds = np.arange(TEST_SEED0 + rank * args.batch, TEST_SEED0 + (rank + 1) * args.batch)
+    seeds = np.arange(*instance_range(rank, args.batch, TEST_SEED0))
     probs = transport_instances(fam, template, seeds)
     net = WarmStartGNN.load(WEIGHTS, template, max_batch=16, device=args.device)
     hbm, peak_kind = peaks()
@@ -523,7 +528,7 @@ def run_warmstart(args, rank, world):
     gathered = gather(world, per_rank)
     if rank != 0:
         return None
-    t_max = max(g["t"] for g in gathered)
+    value, t_max = job_throughput(gathered, "n", "t", args.steps)
     total = sum(g["n"] for g in gathered)
     ci = np.array([r.iterations for r in cold])
     wi = np.array([r.iterations for r in warm])
@@ -535,7 +540,7 @@ def run_warmstart(args, rank, world):
     fwd_launches = 9 + 4 * net.layers
     line = {
         "metric": METRIC,
-        "value": total * args.steps / t_max, "unit": "solves/s",
+        "value": value, "unit": "solves/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -624,6 +629,19 @@ def run_reference(args, rank, world):
 
 
 # --------------------------------------------------------------------------- distributed plumbing
+def instance_range(rank: int, per_rank: int, first: int = 0):
+    """Instances of rank r (weak scaling: every rank its own disjoint block)."""
+    return first + rank * per_rank, first + (rank + 1) * per_rank
+
+
+def job_throughput(gathered, units_key: str, time_key: str, steps: int, time_scale: float = 1.0):
+    """Whole-job rate: all ranks' units per step / the slowest rank's time per step.
+    Returns (units per second, slowest rank's total time in seconds)."""
+    t_max = max(g[time_key] for g in gathered) * time_scale
+    total = sum(g[units_key] for g in gathered)
+    return total * steps / t_max, t_max
+
+
 def init_dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
