@@ -342,6 +342,7 @@ struct Engine : EngineBase {
         int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx, *d_rsoff, *d_csoff, *d_rseg, *d_rsegk, *d_cseg, *d_csegk;
         V *d_rval, *d_cval, *d_c, *d_b, *d_lo = nullptr, *d_hi = nullptr, *d_tau = nullptr, *d_sigma = nullptr;
         double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa, *d_segpart, *d_rowpart_r, *d_rowpart_c;
+        double *d_idr = nullptr, *d_idc = nullptr;
         uint32_t* d_tickets;
         V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
         V *xs, *ys, *xl = nullptr, *yl = nullptr, *AXa = nullptr, *ATYa = nullptr, *xbar = nullptr;
@@ -390,6 +391,7 @@ struct Engine : EngineBase {
             add(&ATY0, sizeof(V) * n); add(&ATY1, sizeof(V) * n);
             add(&xl, sizeof(V) * n); add(&yl, sizeof(V) * m);
             add(&AXa, sizeof(V) * m); add(&ATYa, sizeof(V) * n);
+            add(&d_idr, sizeof(double) * m); add(&d_idc, sizeof(double) * n);
             if (stall_test()) { add(&xb, sizeof(V) * n); add(&yb, sizeof(V) * m); }
         } else {
             add(&xbar, sizeof(V) * n);
@@ -471,8 +473,8 @@ struct Engine : EngineBase {
             SPS_CK(cudaStreamSynchronize(st));
         }
         auto stats = [&]() {
-            k_abs_stats<<<warp_grid_m, kBlock, 0, st>>>(t_ptr, t_idx, t_rval, d_dr, d_dc, rmax, rsum, m);
-            k_abs_stats<<<warp_grid_n, kBlock, 0, st>>>(t_cptr, t_cidx, t_cval, d_dc, d_dr, cmax, csum, n);
+            launch_abs_stats(t_ptr, t_idx, t_rval, d_dr, d_dc, rmax, rsum, m, nnz, kSms * 16, st);
+            launch_abs_stats(t_cptr, t_cidx, t_cval, d_dc, d_dr, cmax, csum, n, nnz, kSms * 16, st);
         };
         if (adaptive) {
             const int ruiz = opt.ruiz_iters >= 0 ? opt.ruiz_iters : 10;
@@ -523,6 +525,7 @@ struct Engine : EngineBase {
             SPS_CK(cudaMemcpyAsync(t_b, bi.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
             k_scale_vectors<V><<<grid_for(std::max(n, m)), kBlock, 0, st>>>(t_c, t_l, t_u, t_b, d_dc, d_dr, d_c,
                                                                            d_lo, d_hi, d_b, n, m);
+            if (d_idc) k_reciprocals<<<grid_for(std::max(n, m)), kBlock, 0, st>>>(d_dc, d_dr, d_idc, d_idr, n, m);
             SPS_CK(cudaGetLastError());
             SPS_CK(cudaStreamSynchronize(st));
             cudaFree(t_c);
@@ -561,6 +564,7 @@ struct Engine : EngineBase {
         a.uniform_bounds = uniform;
         a.lo_u = V(L0); a.hi_u = V(U0);
         a.dr = d_dr; a.dc = d_dc;
+        a.idr = d_idr; a.idc = d_idc;
         a.tau = d_tau; a.sigma = d_sigma;
         if (adaptive) {
             a.inv_nb = 1.0 / (1.0 + std::sqrt(nb2));

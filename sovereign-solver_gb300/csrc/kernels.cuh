@@ -36,6 +36,7 @@ struct Args {
     V lo_u, hi_u;
     int32_t uniform_bounds;
     const double* dr; const double* dc;
+    const double* idr; const double* idc;    // adaptive: 1 / dr, 1 / dc (the checks multiply)
     const V* tau; const V* sigma;
     double inv_nb, inv_nc;     // normalisers of the reported relative error
     V* X[2]; V* Y[2]; V* AX[2]; V* ATY[2];
@@ -243,14 +244,14 @@ struct AdRowCheckEpi {
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int r, int kind, const double (&acc)[2], const Pre&) {
-        const double br = double(a->b[r]), dr = a->dr[r];
+        const double br = double(a->b[r]), idr = a->idr[r];
         axa[r] = V(acc[0]);
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             double res = acc[q] - br;
             if (kind) res = fmax(res, 0.0);
             p[4 * q + 0] += res * res;
-            const double ro = res / dr;
+            const double ro = res * idr;
             p[4 * q + 1] += ro * ro;
             const double yv = q == 0 ? avg_at(ys, ylb, inv_w, r) : double(yc[r]);
             p[4 * q + 2] += br * yv;
@@ -290,7 +291,7 @@ struct AdColCheckEpi {
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int j, int, const double (&acc)[2], const Pre&) {
-        const double cj = double(a->c[j]), dc = a->dc[j];
+        const double cj = double(a->c[j]), idc = a->idc[j];
         const double lo = double(lo_at(*a, j)), hi = double(hi_at(*a, j));
         const bool hl = isfinite(lo), hh = isfinite(hi);
         atya[j] = V(acc[0]);
@@ -300,7 +301,7 @@ struct AdColCheckEpi {
             const double lam = (hl && hh) ? rc : hl ? fmax(rc, 0.0) : hh ? fmin(rc, 0.0) : 0.0;
             const double dres = rc - lam;
             p[5 * q + 0] += dres * dres;
-            const double dor = dres / dc;
+            const double dor = dres * idc;
             p[5 * q + 1] += dor * dor;
             const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
             p[5 * q + 2] += cj * xv;

@@ -77,20 +77,24 @@ static __global__ void k_sort_columns(const int32_t* __restrict__ cptr, int32_t*
 }
 
 // Per-row (or per-column) max |s| and sum |s| of the scaled matrix
-// s_ij = d_own[i] * v_ij * d_other[j].  One warp per row.
+// s_ij = d_own[i] * v_ij * d_other[j].  G lanes per row (G = 1..32, chosen
+// from the mean row length so short rows do not leave most of a warp idle).
+template <int G>
 static __global__ void k_abs_stats(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                            const double* __restrict__ val, const double* __restrict__ d_own,
-                            const double* __restrict__ d_other, double* __restrict__ vmax,
-                            double* __restrict__ vsum, int32_t rows) {
-    const int lane = threadIdx.x & 31;
-    for (int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < rows; r += (gridDim.x * blockDim.x) >> 5) {
+                                   const double* __restrict__ val, const double* __restrict__ d_own,
+                                   const double* __restrict__ d_other, double* __restrict__ vmax,
+                                   double* __restrict__ vsum, int32_t rows) {
+    const int lane = threadIdx.x & (G - 1);
+    const int64_t groups = ((int64_t)gridDim.x * blockDim.x) / G;
+    for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G; r < rows; r += groups) {
         double mx = 0.0, sm = 0.0;
-        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += 32) {
+        for (int k = ptr[r] + lane; k < ptr[r + 1]; k += G) {
             const double a = fabs(val[k] * d_other[idx[k]]);
             mx = fmax(mx, a);
             sm += a;
         }
-        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
             mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
             sm += __shfl_xor_sync(0xffffffffu, sm, o);
         }
@@ -98,6 +102,31 @@ static __global__ void k_abs_stats(const int32_t* __restrict__ ptr, const int32_
             vmax[r] = mx * d_own[r];
             vsum[r] = sm * d_own[r];
         }
+    }
+}
+
+// Lanes per row for the statistics pass: the power of two at or above the mean
+// row length, at most 32.
+static inline int stats_lanes(int64_t nnz, int64_t rows) {
+    const int64_t avg = rows > 0 ? (nnz + rows - 1) / rows : 1;
+    int g = 1;
+    while (g < 32 && g < avg) g <<= 1;
+    return g;
+}
+
+static inline void launch_abs_stats(const int32_t* ptr, const int32_t* idx, const double* val, const double* d_own,
+                                    const double* d_other, double* vmax, double* vsum, int32_t rows, int64_t nnz,
+                                    int max_blocks, cudaStream_t st) {
+    const int g = stats_lanes(nnz, rows);
+    const int64_t threads = (int64_t)rows * g;
+    const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((threads + 255) / 256, max_blocks));
+    switch (g) {
+        case 1: k_abs_stats<1><<<blocks, 256, 0, st>>>(ptr, idx, val, d_own, d_other, vmax, vsum, rows); break;
+        case 2: k_abs_stats<2><<<blocks, 256, 0, st>>>(ptr, idx, val, d_own, d_other, vmax, vsum, rows); break;
+        case 4: k_abs_stats<4><<<blocks, 256, 0, st>>>(ptr, idx, val, d_own, d_other, vmax, vsum, rows); break;
+        case 8: k_abs_stats<8><<<blocks, 256, 0, st>>>(ptr, idx, val, d_own, d_other, vmax, vsum, rows); break;
+        case 16: k_abs_stats<16><<<blocks, 256, 0, st>>>(ptr, idx, val, d_own, d_other, vmax, vsum, rows); break;
+        default: k_abs_stats<32><<<blocks, 256, 0, st>>>(ptr, idx, val, d_own, d_other, vmax, vsum, rows); break;
     }
 }
 
@@ -173,6 +202,14 @@ __global__ void k_scale_vectors(const double* __restrict__ c, const double* __re
         }
     }
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) bs[i] = V(b[i] * dr[i]);
+}
+
+// Reciprocal scale factors (FP64) for the adaptive checks, which multiply by them.
+__global__ static void k_reciprocals(const double* __restrict__ dc, const double* __restrict__ dr,
+                                     double* __restrict__ idc, double* __restrict__ idr, int32_t n, int32_t m) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) idc[j] = 1.0 / dc[j];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) idr[i] = 1.0 / dr[i];
 }
 
 // Reference diagonal steps (solver/lp/pdhg.py:139-147): 0.999 / max(sum|a|, 1e-4).
