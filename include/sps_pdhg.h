@@ -91,7 +91,11 @@ typedef struct {
     int32_t warm_fallback;    /* 1 (default): a warm start whose relative KKT error is larger than
                                  the cold start's (x = clip(0, lb, ub), y = 0) is dropped and the
                                  solve starts cold; 0: always start from the warm point */
-    int32_t reserved[3];
+    int32_t batch_team;       /* batched solver: blocks (one thread-block cluster) per large
+                                 instance, 1..8; 0 = 2; 1 = one block per instance */
+    int32_t batch_team_nnz;   /* batched solver: instances with at least this many nonzeros are
+                                 large; 0 = 65536 */
+    int32_t reserved[1];
 } sps_options;
 
 typedef struct {
@@ -183,7 +187,8 @@ typedef struct {
     int32_t escalated;          /* instances that stalled in FP32 and were finished in FP64 by the
                                    single-LP engine after the persistent launch (in solve_ms) */
     int32_t lanes_per_row;      /* row-pass schedule (4, 8, 16, 32 lanes per row; timed) */
-    int32_t reserved[3];
+    int32_t team;               /* blocks per large instance in the launch (1 = no clusters) */
+    int32_t reserved[2];
 } sps_batch_stats;
 
 /* Pack `count` problems, upload and scale them (one block per instance) and pick

@@ -27,6 +27,9 @@ class PDHGBatch:
     ``batch_group`` picks the lanes per column of the column pass (1, 2, 4, 8,
     16, 32); 0 lets the library time the candidates on a sample of the batch.
     The lanes per row of the row pass (4, 8, 16, 32) are always timed.
+    ``batch_team``: blocks (a thread-block cluster) per large instance, 0 = 2,
+    1 = one block per instance; ``batch_team_nnz``: nonzeros from which an
+    instance is large (0 = 65 536).
     ``escalate``: "fp64" (FP64 continuation of stalled instances), "stop"
     (status "stalled") or "off" (FP32 to the iteration limit).
     """
@@ -34,7 +37,7 @@ class PDHGBatch:
     def __init__(self, problems: Sequence, tol: float = 1e-4, max_iters: int = MAX_PDHG_ITERS,
                  batch_group: int = 0, time_limit: float = 0.0, check_interval: int = 0,
                  graph_mode: int = 2, device: int = 0, ruiz_iters: int = 10, escalate: str = "fp64",
-                 warm_fallback: bool = True):
+                 warm_fallback: bool = True, batch_team: int = 0, batch_team_nnz: int = 0):
         self.lib = N.load()
         self.problems = list(problems)
         if not self.problems:
@@ -45,6 +48,8 @@ class PDHGBatch:
                          check_interval=check_interval, graph_mode=graph_mode, device=device,
                          ruiz_iters=ruiz_iters, escalate=escalate, warm_fallback=warm_fallback)
         o.batch_group = int(batch_group)
+        o.batch_team = int(batch_team)
+        o.batch_team_nnz = int(batch_team_nnz)
         h = C.c_void_p()
         N.check(self.lib.sps_batch_create(len(self._descs), arr, C.byref(o), C.byref(h)), None)
         self.h = h

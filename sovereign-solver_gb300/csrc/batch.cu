@@ -27,25 +27,32 @@ namespace sps {
 void set_create_error(const std::string& msg);
 namespace batch {
 
+// Gathers of iterate vectors.  In team mode (coh) the vector is written by
+// other SMs during the launch, so it is read through L2 (__ldcg); a block on
+// its own reads what it wrote itself and keeps the read-only path.
 struct Gather1 {
     const float* x;
-    __device__ __forceinline__ float operator()(int, int j) const { return __ldg(x + j); }
+    bool coh;
+    __device__ __forceinline__ float operator()(int, int j) const { return coh ? __ldcg(x + j) : __ldg(x + j); }
 };
 
 // Point 0 of a check is the average, kept as an offset from the restart point
 // (x_last + x_sum / w_sum, x_sum = sum of w_k (x_k - x_last)) so that FP32 sums
 // stay accurate near convergence; l = null when there is no average yet and
 // point 0 aliases the current iterate.
-__device__ __forceinline__ double avg_at(const float* s, const float* l, double inv_w, int j) {
-    const double v = double(__ldg(s + j)) * inv_w;
-    return l ? v + double(__ldg(l + j)) : v;
+__device__ __forceinline__ float ld_vec(const float* p, bool coh) { return coh ? __ldcg(p) : __ldg(p); }
+
+__device__ __forceinline__ double avg_at(const float* s, const float* l, double inv_w, int j, bool coh = false) {
+    const double v = double(ld_vec(s + j, coh)) * inv_w;
+    return l ? v + double(ld_vec(l + j, coh)) : v;
 }
 
 struct Gather2 {
     const float *s, *l, *x;
     double inv_w;
+    bool coh;
     __device__ __forceinline__ double operator()(int q, int j) const {
-        return q == 0 ? avg_at(s, l, inv_w, j) : double(__ldg(x + j));
+        return q == 0 ? avg_at(s, l, inv_w, j, coh) : double(ld_vec(x + j, coh));
     }
 };
 
@@ -194,8 +201,19 @@ __device__ __forceinline__ void slot_sums(const double* slots, double* out) {
     __syncthreads();
 }
 
-__device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm, double* slots,
-                                const uint64_t* dl) {
+// Element loops of a team.  A block owns exactly the rows (columns) its warps
+// visit in the row (column) passes: chunks of CH = kWarps * (32 / lanes)
+// consecutive elements, every size-th chunk from chunk `rank` on, so every
+// per-row and per-column array is read and written by one block only (the
+// gathers are the only reads across blocks).  The block's threads walk its
+// owned elements densely; on its own (size 1) this is the identity.
+#define TEAM_OWNED(var, count, CH)                                                                \
+    for (int o_ = threadIdx.x, var; (var = (T.rank + (o_ / (CH)) * T.size) * (CH) + o_ % (CH)) < (count); \
+         o_ += kBlock)
+
+__device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm, double* slots, const uint64_t* dl,
+                                const Team& T) {
+    const int chc = kWarps * (32 / v.G), chr = kWarps * (32 / v.Gr);
     const uint64_t deadline = *dl;
     const bool has_avg = c.w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / c.w_sum : 1.0;
@@ -205,30 +223,38 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w,
                  mine};
     group_rows_r<2, double>(v.Gr, v.rptr, v.ridx, v.rval, v.m,
-                              Gather2{has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], inv_w}, er);
+                            Gather2{has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], inv_w, T.size > 1}, er,
+                            T.rank, T.size);
     slot_sums<8>(slots, sm);                       // sm[0..7]: row partials
     for (int q = 0; q < 10; ++q) mine[q * kBlock] = 0.0;
     ColCheckE ec{v.c, v.lo, v.hi, has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], v.xl, v.dc, v.atya,
                  inv_w, mine};
     group_rows_dyn<2, double>(v.G, v.cptr, v.cidx, v.cval, v.n,
-                              Gather2{has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], inv_w}, ec);
+                              Gather2{has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], inv_w, T.size > 1}, ec,
+                              T.rank, T.size);
     slot_sums<10>(slots, sm + 8);                  // sm[8..17]: column partials
+    // team totals of the 18 partials and of the deadline test (any block past it stops all)
+    double tt[19];
     if (threadIdx.x == 0) {
-        const bool stop = deadline && global_ns() > deadline;
+        for (int q = 0; q < 18; ++q) tt[q] = sm[q];
+        tt[18] = (deadline && global_ns() > deadline) ? 1.0 : 0.0;
+    }
+    if (!team_total<19>(tt, T)) return false;
+    if (threadIdx.x == 0) {
         double tr[8], tc[10];
-        for (int q = 0; q < 8; ++q) tr[q] = sm[q];
-        for (int q = 0; q < 10; ++q) tc[q] = sm[8 + q];
-        decide_check(c, tc, tr, I.inv_nb, I.inv_nc, stop);
+        for (int q = 0; q < 8; ++q) tr[q] = tt[q];
+        for (int q = 0; q < 10; ++q) tc[q] = tt[8 + q];
+        decide_check(c, tc, tr, I.inv_nb, I.inv_nc, tt[18] > 0.0);
     }
     __syncthreads();
     const int ap = c.apply;
-    if (ap == 0) return;
+    if (ap == 0) return true;
     const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !c.done;
     const bool save = (ap & AP_SAVE_BEST) && v.xb, save_avg = ap & AP_SAVE_AVG;
     const double iw = c.w_sum > 0.0 ? 1.0 / c.w_sum : 0.0;
     const float tau = float(c.eta / c.omega);
     float dx2 = 0.f;
-    for (int j = threadIdx.x; j < v.n; j += kBlock) {
+    TEAM_OWNED(j, v.n, chc) {
         if (save) v.xb[j] = save_avg ? float(double(v.xl[j]) + double(v.xs[j]) * iw) : v.X[cur][j];
         float xv;
         if (load) {
@@ -245,7 +271,7 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
             dx2 += (x2 - xv) * (x2 - xv);
         }
     }
-    for (int i = threadIdx.x; i < v.m; i += kBlock) {
+    TEAM_OWNED(i, v.m, chr) {
         if (save) v.yb[i] = save_avg ? float(double(v.yl[i]) + double(v.ys[i]) * iw) : v.Y[cur][i];
         float yv;
         if (load) {
@@ -259,20 +285,23 @@ __device__ void check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     }
     double t[1] = {double(dx2)};
     block_sum<1>(t, sm);
+    if (!team_total<1>(t, T)) return false;
     if (threadIdx.x == 0) {
         if (cand) c.dx2 = t[0];
         if (rst) c.w_sum = 0.0;
         c.apply = 0;
     }
     __syncthreads();
+    return true;
 }
 
 // Start point of instance k (cold: x = clip(0, lo, hi), y = 0; warm: the caller's
 // point scaled and projected, with its primal weight), its products K x0 and
 // K^T y0, and the init-phase check that records its relative KKT error.
-__device__ void start_point(const Args& A, int k, const Inst& I, const View& v, int G, bool warm, Ctl& c,
-                            double* sm, double* slots) {
-    __syncthreads();
+__device__ bool start_point(const Args& A, int k, const Inst& I, const View& v, bool warm, Ctl& c, double* sm,
+                            double* slots, const Team& T) {
+    const int chc = kWarps * (32 / v.G), chr = kWarps * (32 / v.Gr);
+    if (!team_barrier(T)) return false;
     if (threadIdx.x == 0) {
         c = Ctl{};
         c.status = SPS_STATUS_ITERATION_LIMIT;
@@ -284,32 +313,35 @@ __device__ void start_point(const Args& A, int k, const Inst& I, const View& v, 
         c.kkt_last = INFINITY;
         c.stall_on = A.stall_on;
     }
-    for (int j = threadIdx.x; j < v.n; j += kBlock) {
+    TEAM_OWNED(j, v.n, chc) {
         const float x0 = warm ? float(A.wx[I.vc + j] / v.dc[j]) : 0.f;
         const float x = fminf(fmaxf(x0, v.lo[j]), v.hi[j]);
         v.X[0][j] = x;
         v.xl[j] = x;
         v.xs[j] = 0.f;
     }
-    for (int i = threadIdx.x; i < v.m; i += kBlock) {
+    TEAM_OWNED(i, v.m, chr) {
         float y = warm ? float(A.wy[I.vr + i] / v.dr[i]) : 0.f;
         if (v.kind[i]) y = fminf(y, 0.f);
         v.Y[0][i] = y;
         v.yl[i] = y;
         v.ys[i] = 0.f;
     }
-    __syncthreads();
+    if (!team_barrier(T)) return false;
     StoreE sx{v.AX[0]};
-    group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[0]}, sx);
+    group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[0], T.size > 1}, sx, T.rank, T.size);
     StoreE sy{v.ATY[0]};
-    group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[0]}, sy);
-    __syncthreads();
-    check_and_apply(v, I, c, sm, slots, A.deadline);
+    group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[0], T.size > 1}, sy, T.rank, T.size);
+    if (!team_barrier(T)) return false;
+    return check_and_apply(v, I, c, sm, slots, A.deadline, T);
 }
 
-__device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, double* slots) {
+// The whole solve of instance k by this block (T.size == 1) or by the team of
+// blocks of a cluster.  Returns false when a team barrier timed out.
+__device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, double* slots, const Team& T) {
     const Inst I = A.inst[k];
     const View v = make_view(A, I, G);
+    const int chc = kWarps * (32 / v.G), chr = kWarps * (32 / v.Gr);
     const uint64_t t_begin = global_ns();
     const bool warm = A.warm != 0;
     bool used = warm;
@@ -317,17 +349,17 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
         // keep the warm point only if its relative KKT error is not above the cold start's
         double cold = A.cold_rel[k];
         if (!(cold >= 0.0)) {
-            start_point(A, k, I, v, G, false, c, sm, slots);
+            if (!start_point(A, k, I, v, false, c, sm, slots, T)) return false;
             cold = c.rel_kkt;
-            if (threadIdx.x == 0) A.cold_rel[k] = cold;
+            if (threadIdx.x == 0 && T.rank == 0) A.cold_rel[k] = cold;
         }
-        start_point(A, k, I, v, G, true, c, sm, slots);
+        if (!start_point(A, k, I, v, true, c, sm, slots, T)) return false;
         if (!(c.rel_kkt <= cold)) {
             used = false;
-            start_point(A, k, I, v, G, false, c, sm, slots);
+            if (!start_point(A, k, I, v, false, c, sm, slots, T)) return false;
         }
     } else {
-        start_point(A, k, I, v, G, warm, c, sm, slots);
+        if (!start_point(A, k, I, v, warm, c, sm, slots, T)) return false;
     }
     if (threadIdx.x == 0) {
         c.t_begin = t_begin;
@@ -339,9 +371,10 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             if (c.done || c.iters >= c.max_iters) break;
             int cur = c.cur;
             RowStepE er{v.b, v.AX[cur], v.Y[cur], v.kind, v.AX[1 - cur], v.Y[1 - cur], float(c.eta * c.omega)};
-            group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur]}, er);
+            group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur], T.size > 1}, er, T.rank, T.size);
             double t2[2] = {double(er.dy2), double(er.inter)};
             block_sum<2>(t2, sm);
+            if (!team_total<2>(t2, T)) return false;
             if (threadIdx.x == 0) decide_step(c, t2[0], t2[1]);
             __syncthreads();
             if (c.done) break;
@@ -350,12 +383,12 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             float dx2;
             if (c.accepted) {
                 ColStepE ec{v.X[cur], v.c, v.lo, v.hi, v.xl, v.ATY[cur], v.X[1 - cur], v.xs, tau, wgt};
-                group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur]}, ec);
+                group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur], T.size > 1}, ec, T.rank, T.size);
                 dx2 = ec.dx2;
-                for (int i = threadIdx.x; i < v.m; i += kBlock) v.ys[i] += wgt * (v.Y[cur][i] - v.yl[i]);
+                TEAM_OWNED(i, v.m, chr) v.ys[i] += wgt * (v.Y[cur][i] - v.yl[i]);
             } else {
                 dx2 = 0.f;
-                for (int j = threadIdx.x; j < v.n; j += kBlock) {
+                TEAM_OWNED(j, v.n, chc) {
                     const float xj = v.X[cur][j];
                     const float x2 = fminf(fmaxf(xj - tau * (v.c[j] - v.ATY[cur][j]), v.lo[j]), v.hi[j]);
                     v.X[1 - cur][j] = x2;
@@ -364,35 +397,90 @@ __device__ void solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             }
             double t1[1] = {double(dx2)};
             block_sum<1>(t1, sm);
+            if (!team_total<1>(t1, T)) return false;
             if (threadIdx.x == 0) { c.dx2 = t1[0]; c.apply = 0; }
             __syncthreads();
         }
         if (c.done) break;
-        check_and_apply(v, I, c, sm, slots, A.deadline);
+        if (!check_and_apply(v, I, c, sm, slots, A.deadline, T)) return false;
         if (c.done) break;
     }
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && T.rank == 0) {
         c.t_end = global_ns();
         A.out[k] = c;
     }
+    return true;
 }
 
+// Persistent solver.  Instances are handed out largest first from an atomic
+// counter.  With A.team > 1 the launch is made of clusters of A.team blocks:
+// while the next instance has at least A.team_nnz nonzeros the cluster's rank
+// 0 takes it for the whole cluster (every block reads the index from rank 0's
+// shared memory between two team barriers) and the team solves it; from the
+// first smaller instance on, every block takes its own instances.
 __global__ void __launch_bounds__(kBlock, 2) k_batch_solve(Args A, int G) {
     __shared__ Ctl c;
     __shared__ double sm[kWarps * 10];
     __shared__ double slots[10 * kBlock];
-    __shared__ int s_inst;
+    __shared__ double xch[2 * kXch];
+    __shared__ uint32_t counter;
+    __shared__ int s_inst, s_err;
+    uint32_t gen = 0;
+    int phase = 0;
+    const int C = A.team > 1 ? A.team : 1;
+    int rank = 0;
+    if (threadIdx.x == 0) { counter = 0u; s_err = 0; }
+    if (C > 1) {
+        uint32_t r;
+        asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+        rank = (int)r;
+        // every block of the cluster initialises its counter before any block arrives at a team barrier
+        asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+    }
+    __syncthreads();
+    const Team team{C, rank, &counter, &gen, xch, &phase, &s_err};
+    const Team solo{1, 0, &counter, &gen, xch, &phase, &s_err};
+    bool together = C > 1;
     for (;;) {
-        if (threadIdx.x == 0) {
-            const uint32_t q = atomicAdd(A.counter, 1u);
-            s_inst = q < (uint32_t)A.count ? A.order[q] : -1;
+        int k;
+        if (together) {
+            if (threadIdx.x == 0 && rank == 0) {
+                const uint32_t q = atomicAdd(A.counter, 1u);
+                s_inst = q < (uint32_t)A.count ? A.order[q] : -1;
+            }
+            if (!team_barrier(team)) break;
+            if (threadIdx.x == 0) {
+                int r0;
+                asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(r0) : "r"(cluster_addr(&s_inst, 0)) : "memory");
+                sm[0] = double(r0);
+            }
+            __syncthreads();
+            k = int(sm[0]);
+            if (!team_barrier(team)) break;       // rank 0 may overwrite s_inst only after every block read it
+            if (k < 0) break;
+            if (A.inst[k].nnz >= A.team_nnz) {
+                if (!solve_one(A, k, G, c, sm, slots, team)) break;
+                continue;
+            }
+            together = false;                      // smaller instances: one block each from now on
+            if (rank != 0) continue;
+        } else {
+            if (threadIdx.x == 0) {
+                const uint32_t q = atomicAdd(A.counter, 1u);
+                s_inst = q < (uint32_t)A.count ? A.order[q] : -1;
+            }
+            __syncthreads();
+            k = s_inst;
+            if (k < 0) break;
         }
-        __syncthreads();
-        const int k = s_inst;
-        if (k < 0) return;
-        solve_one(A, k, G, c, sm, slots);
+        solve_one(A, k, G, c, sm, slots, solo);
         __syncthreads();
     }
+    if (threadIdx.x == 0 && s_err) atomicExch(A.team_error, 1);
+    // every block reaches this point once (all loops above are bounded): no block
+    // leaves while a peer may still read its shared memory (the barrier counter,
+    // the exchange buffers, the instance index)
+    if (C > 1) asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
 }
 
 // ---------------------------------------------------------------------------
@@ -517,6 +605,9 @@ struct sps_batch {
     int32_t count = 0;
     sps_options opt{};
     int32_t G = 8, Gr = 32, blocks = 0;      // lanes per column / per row, persistent blocks
+    int32_t team = 1;                         // cluster size of the solve launch
+    int32_t team_nnz = 65536;                 // instances at least this large are solved by a team
+    int32_t* d_team_error = nullptr;
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<Inst> inst;
@@ -614,7 +705,7 @@ bool check_instance(const sps_problem_desc& d, std::string& why) {
 // single-LP engine solves it in FP64, warm-started from the best point of the
 // FP32 stall test (in xo / yo) with the primal weight it had there, within the
 // iterations and time left; its result replaces the instance's.
-int continue_fp64(sps_batch* b, int32_t k, double used_s) {
+int continue_fp64(sps_batch* b, int32_t k, double used_s, std::string* why) {
     const Inst& I = b->inst[k];
     Ctl& c = b->out[k];
     if (b->opt.time_limit_s > 0 && used_s >= b->opt.time_limit_s) {
@@ -647,7 +738,10 @@ int continue_fp64(sps_batch* b, int32_t k, double used_s) {
     o.time_limit_s = b->opt.time_limit_s > 0 ? b->opt.time_limit_s - used_s : 0.0;
     sps_handle* h = nullptr;
     int rc = sps_create(&d, &o, &h);
-    if (rc != SPS_OK) return b->fail(rc, "instance " + std::to_string(k) + " FP64 continuation: " + sps_last_error(nullptr));
+    if (rc != SPS_OK) {
+        *why = "instance " + std::to_string(k) + " FP64 continuation: " + sps_last_error(nullptr);
+        return rc;
+    }
     sps_result r;
     double* x = b->xo.data() + I.vc;
     double* y = b->yo.data() + I.vr;
@@ -655,9 +749,9 @@ int continue_fp64(sps_batch* b, int32_t k, double used_s) {
     if (rc == SPS_OK) rc = sps_solve(h, &r);
     if (rc == SPS_OK) rc = sps_get_solution(h, x, y);
     if (rc != SPS_OK) {
-        const std::string why = sps_last_error(h);
+        *why = "instance " + std::to_string(k) + " FP64 continuation: " + sps_last_error(h);
         sps_destroy(h);
-        return b->fail(rc, "instance " + std::to_string(k) + " FP64 continuation: " + why);
+        return rc;
     }
     sps_destroy(h);
     c.status = r.status;
@@ -705,6 +799,7 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         I.m = d.m_ub + d.m_eq;
         I.m_ub = d.m_ub;
         const int64_t nz = (int64_t)(d.m_ub ? d.ub_indptr[d.m_ub] : 0) + (d.m_eq ? d.eq_indptr[d.m_eq] : 0);
+        I.nnz = (int32_t)std::min<int64_t>(nz, INT32_MAX);
         I.rp = rp; I.re = re; I.cp = cp; I.ce = re; I.vc = vc; I.vr = vr;
         rp += I.m + 1; cp += I.n + 1; re += nz; vc += I.n; vr += I.m;
     }
@@ -794,6 +889,8 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
     b->order.resize(count);
     std::iota(b->order.begin(), b->order.end(), 0);
     std::stable_sort(b->order.begin(), b->order.end(), [&](int32_t a, int32_t c) { return work[a] > work[c]; });
+    // large instances (solved by a team of blocks when clusters are available)
+    b->team_nnz = opt.batch_team_nnz > 0 ? opt.batch_team_nnz : sps::batch::kTeamNnz;
 
     // ---- device
     sps_batch* bp = b.get();
@@ -828,6 +925,7 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         SPB_CK(b->alloc(&b->d_xo, vc));
         SPB_CK(b->alloc(&b->d_yo, vr));
         SPB_CK(b->alloc(&b->d_cold_rel, count));
+        SPB_CK(b->alloc(&b->d_team_error, 1));
         SPB_CK(cudaMemsetAsync(b->d_cold_rel, 0xFF, sizeof(double) * count, b->st));   // NaN = unknown
         float *d_xb = nullptr, *d_yb = nullptr;
         if (opt.escalate != 0) { SPB_CK(b->alloc(&d_xb, vc)); SPB_CK(b->alloc(&d_yb, vr)); }
@@ -869,6 +967,26 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         SPB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sps::batch::k_batch_solve, sps::kBlock, 0));
         SPB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         b->blocks = std::max(1, std::min(count, nb * sms));
+        // clusters for the large instances: used when such a launch can be scheduled
+        const int want = opt.batch_team > 0 ? std::min(opt.batch_team, 8) : 2;
+        if (want > 1 && b->blocks >= want) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = want;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3((b->blocks / want) * want);
+            cfg.blockDim = dim3(sps::kBlock);
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            int ncl = 0;
+            if (cudaOccupancyMaxActiveClusters(&ncl, sps::batch::k_batch_solve, &cfg) == cudaSuccess && ncl > 0) {
+                b->team = want;
+                b->blocks = (b->blocks / want) * want;
+            }
+            cudaGetLastError();
+        }
         SPB_CK(cudaEventRecord(b->e1, b->st));
         SPB_CK(cudaStreamSynchronize(b->st));
         float ms = 0;
@@ -881,16 +999,27 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
     // candidate on a sample of the largest instances)
     {
         sps_batch* bb = bp;
+        // A sample spread over the whole size range (every stride-th instance of the
+        // largest-first order); a candidate's cost is the SUM of its instances' device
+        // times for 32 attempts and one check each (throughput, not the sample's
+        // makespan, which only reflects its largest instance).
         const int32_t sample = std::min<int32_t>(count, 2 * bb->blocks);
-        auto time_one = [&](int sched, float* ms) -> bool {
-            sps::batch::Args A{bb->d_inst, bb->d_order, sample, 32, 32, 0.0, bb->d_deadline, bb->arr, bb->d_out,
+        std::vector<int32_t> pick(sample);
+        for (int32_t q = 0; q < sample; ++q) pick[q] = bb->order[(int64_t)q * count / sample];
+        int32_t* d_pick = nullptr;
+        SPB_CK(bb->alloc(&d_pick, sample));
+        SPB_CK(cudaMemcpyAsync(d_pick, pick.data(), sizeof(int32_t) * sample, cudaMemcpyHostToDevice, bb->st));
+        std::vector<Ctl> outs(count);
+        auto time_one = [&](int sched, float* cost) -> bool {
+            sps::batch::Args A{bb->d_inst, d_pick, sample, 32, 32, 0.0, bb->d_deadline, bb->arr, bb->d_out,
                                bb->d_counter, 0};
             cudaMemsetAsync(bb->d_counter, 0, sizeof(uint32_t), bb->st);
-            cudaEventRecord(bb->e0, bb->st);
             sps::batch::k_batch_solve<<<std::min(bb->blocks, sample), sps::kBlock, 0, bb->st>>>(A, sched);
-            cudaEventRecord(bb->e1, bb->st);
+            cudaMemcpyAsync(outs.data(), bb->d_out, sizeof(Ctl) * count, cudaMemcpyDeviceToHost, bb->st);
             if (cudaStreamSynchronize(bb->st) != cudaSuccess) return false;
-            cudaEventElapsedTime(ms, bb->e0, bb->e1);
+            double tot = 0.0;
+            for (int32_t q = 0; q < sample; ++q) tot += 1e-6 * double(outs[pick[q]].t_end - outs[pick[q]].t_begin);
+            *cost = float(tot);
             return true;
         };
         const int g_opt = opt.batch_group;
@@ -930,11 +1059,29 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     const uint64_t tl = b->opt.time_limit_s > 0 ? (uint64_t)(b->opt.time_limit_s * 1e9) : 0;
     sps::batch::Args A{b->d_inst, b->d_order, b->count, (int32_t)W, b->opt.max_iters, b->opt.tol, b->d_deadline,
                        b->arr, b->d_out, b->d_counter, b->opt.escalate != 0 ? 1 : 0, b->warm,
-                       b->opt.warm_fallback ? 1 : 0, b->d_wx, b->d_wy, b->d_wom, b->d_cold_rel};
+                       b->opt.warm_fallback ? 1 : 0, b->d_wx, b->d_wy, b->d_wom, b->d_cold_rel,
+                       b->team, b->team_nnz, b->d_team_error};
     auto enqueue = [&](cudaStream_t s) {
         cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
         sps::batch::k_set_deadline<<<1, 32, 0, s>>>(b->d_deadline, tl);
-        sps::batch::k_batch_solve<<<b->blocks, sps::kBlock, 0, s>>>(A, sps::batch::pack_schedule(b->G, b->Gr));
+        cudaMemsetAsync(b->d_team_error, 0, sizeof(int32_t), s);
+        const int sched = sps::batch::pack_schedule(b->G, b->Gr);
+        if (b->team > 1) {
+            cudaLaunchConfig_t cfg = {};
+            cudaLaunchAttribute attr[1];
+            attr[0].id = cudaLaunchAttributeClusterDimension;
+            attr[0].val.clusterDim.x = b->team;
+            attr[0].val.clusterDim.y = 1;
+            attr[0].val.clusterDim.z = 1;
+            cfg.gridDim = dim3(b->blocks);
+            cfg.blockDim = dim3(sps::kBlock);
+            cfg.stream = s;
+            cfg.attrs = attr;
+            cfg.numAttrs = 1;
+            cudaLaunchKernelEx(&cfg, sps::batch::k_batch_solve, A, sched);
+        } else {
+            sps::batch::k_batch_solve<<<b->blocks, sps::kBlock, 0, s>>>(A, sched);
+        }
     };
     SPB_CK(cudaEventRecord(b->e0, b->st));
     if (b->opt.graph_mode != 0) {
@@ -978,20 +1125,40 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     SPB_CK(cudaStreamSynchronize(b->st));
     float ms = 0;
     cudaEventElapsedTime(&ms, b->e0, b->e1);
+    int32_t team_err = 0;
+    SPB_CK(cudaMemcpy(&team_err, b->d_team_error, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    if (team_err) return b->fail(SPS_ERR_CUDA, "a team barrier of the batched solve timed out");
     b->escalated.assign(b->count, 0);
     b->esc_ms.assign(b->count, 0.0);
     int32_t n_esc = 0;
     double esc_ms = 0.0;
     if (b->opt.escalate == 1) {
+        // FP64 continuations of the stalled instances, several at once: each has its
+        // own engine and stream, so their small kernels overlap on the GPU
         const auto t0 = std::chrono::steady_clock::now();
-        for (int32_t k = 0; k < b->count; ++k) {
-            if (b->out[k].status != SPS_STATUS_STALLED) continue;
-            const auto t1 = std::chrono::steady_clock::now();
-            const double used = ms * 1e-3 + std::chrono::duration<double>(t1 - t0).count();
-            if (int rc = continue_fp64(b, k, used)) return rc;
-            b->esc_ms[k] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
-            ++n_esc;
-        }
+        std::vector<int32_t> todo;
+        for (int32_t k = 0; k < b->count; ++k)
+            if (b->out[k].status == SPS_STATUS_STALLED) todo.push_back(k);
+        std::vector<int> rcs(todo.size(), SPS_OK);
+        std::vector<std::string> whys(todo.size());
+        std::atomic<size_t> next{0};
+        auto work = [&]() {
+            for (size_t i; (i = next.fetch_add(1)) < todo.size();) {
+                const int32_t k = todo[i];
+                const auto t1 = std::chrono::steady_clock::now();
+                const double used = ms * 1e-3 + std::chrono::duration<double>(t1 - t0).count();
+                rcs[i] = continue_fp64(b, k, used, &whys[i]);
+                b->esc_ms[k] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
+            }
+        };
+        const int nt = (int)std::min<size_t>(todo.size(), 8);
+        std::vector<std::thread> pool;
+        for (int t = 1; t < nt; ++t) pool.emplace_back(work);
+        if (!todo.empty()) work();
+        for (auto& th : pool) th.join();
+        for (size_t i = 0; i < todo.size(); ++i)
+            if (rcs[i] != SPS_OK) return b->fail(rcs[i], whys[i]);
+        n_esc = (int32_t)todo.size();
         esc_ms = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     b->solve_ms = ms + esc_ms;
@@ -1002,6 +1169,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
         stats->solve_ms = b->solve_ms;
         stats->lanes_per_column = b->G;
         stats->lanes_per_row = b->Gr;
+        stats->team = b->team;
         stats->blocks = b->blocks;
         stats->escalated = n_esc;
         for (const Ctl& c : b->out) {

@@ -17,7 +17,7 @@ namespace sps {
 namespace batch {
 
 struct Inst {                 // per-instance descriptor
-    int32_t n, m, m_ub, pad;
+    int32_t n, m, m_ub, nnz;
     int64_t rp, re;           // row-offset base (m + 1 entries), row-entry base
     int64_t cp, ce;           // column-offset base (n + 1 entries), column-entry base
     int64_t vc, vr;           // column-vector base, row-vector base
@@ -51,17 +51,106 @@ struct Args {
     int32_t warm, fallback;   // warm starts set / cold-start fallback on
     const double *wx, *wy, *wom;   // warm starts (original space, packed like the vectors), omega0
     double* cold_rel;         // per instance: relative KKT error of the cold start (< 0 = unknown)
+    int32_t team;             // cluster size of the launch (1 = one block per instance)
+    int32_t team_nnz;         // instances with at least this many nonzeros are solved by a whole cluster
+    int32_t* team_error;      // set when a team barrier gave up waiting
 };
+
+// ---------------------------------------------------------------------------
+// Teams: the blocks of one thread-block cluster solving one large instance.
+// Rows and columns are split over the team's warps; every reduction is each
+// block's partial published in its shared memory and summed by every block in
+// rank order, so all blocks take the same decisions without a broadcast.
+// The team barrier is a counter in rank 0's shared memory (release-add,
+// acquire-poll at cluster scope) with a bounded wait: a block that waits
+// longer than kTeamSpin polls (about a second) records an error and leaves.
+constexpr int kXch = 24;                  // doubles per exchange buffer
+constexpr int32_t kTeamNnz = 65536;       // smallest size solved by a team
+constexpr uint32_t kTeamSpin = 1u << 21;
+
+__device__ __forceinline__ uint32_t cluster_addr(const void* p, uint32_t rank) {
+    uint32_t a = (uint32_t)__cvta_generic_to_shared(p), r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void cluster_add_release(uint32_t addr, uint32_t v) {
+    asm volatile("red.release.cluster.shared::cluster.add.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_load_acquire(uint32_t addr) {
+    uint32_t v;
+    asm volatile("ld.acquire.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ double cluster_load_f64(uint32_t addr) {
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(addr) : "memory");
+    return v;
+}
+
+struct Team {
+    int size, rank;           // blocks on the instance, this block's cluster rank
+    uint32_t* counter;        // barrier counter (this block's copy; rank 0's is the one used)
+    uint32_t* gen;            // barriers passed (this block)
+    double* xch;              // 2 x kXch exchange buffers (this block)
+    int* phase;               // which exchange buffer is next
+    int* err;                 // 1 once a barrier timed out
+};
+
+// All threads: barrier over the team with global-memory ordering.  Returns false
+// (for every thread of the block) when the wait timed out.
+__device__ __forceinline__ bool team_barrier(const Team& T) {
+    if (T.size <= 1) {
+        __syncthreads();
+        return true;
+    }
+    __threadfence();          // every thread's writes are ordered before the block's arrival
+    __syncthreads();
+    if (threadIdx.x == 0 && !*T.err) {
+        const uint32_t target = (*T.gen + 1) * (uint32_t)T.size;
+        const uint32_t a = cluster_addr(T.counter, 0);
+        cluster_add_release(a, 1u);
+        uint32_t it = 0;
+        while (cluster_load_acquire(a) < target) {
+            if (++it > kTeamSpin) { *T.err = 1; break; }
+            __nanosleep(64);
+        }
+        *T.gen += 1;
+    }
+    __syncthreads();
+    return !*T.err;
+}
+
+// Thread 0 holds a block total in t; afterwards thread 0 holds the team total
+// (blocks added in rank order).  Returns false on a barrier timeout.
+template <int N>
+__device__ __forceinline__ bool team_total(double (&t)[N], const Team& T) {
+    static_assert(N <= kXch, "exchange buffer too small");
+    if (T.size <= 1) return true;
+    double* buf = T.xch + (*T.phase & 1) * kXch;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < N; ++q) buf[q] = t[q];
+    if (!team_barrier(T)) return false;
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < N; ++q) t[q] = 0.0;
+        for (int r = 0; r < T.size; ++r) {
+            const uint32_t a = cluster_addr(buf, (uint32_t)r);
+            for (int q = 0; q < N; ++q) t[q] += cluster_load_f64(a + 8u * q);
+        }
+    }
+    *T.phase += 1;            // every thread keeps the same count
+    return true;
+}
 
 // ---------------------------------------------------------------------------
 // Group traversal inside one block: G lanes per row, rows [0, count).
 // g(q, j) gathers, e.pre(r) / e(r, acc, pre) as in the single-LP visitors.
 template <int G, int NV, class Acc, class Gather, class Epi>
 __device__ __forceinline__ void group_rows(const int32_t* __restrict__ ptr, const int32_t* __restrict__ idx,
-                                           const float* __restrict__ val, int count, const Gather& g, Epi& e) {
+                                           const float* __restrict__ val, int count, const Gather& g, Epi& e,
+                                           int trank = 0, int tsize = 1) {
     constexpr int per_warp = 32 / G;
     const int warp = threadIdx.x >> 5, wl = threadIdx.x & 31, lane = wl & (G - 1);
-    for (int base = warp * per_warp; base < count; base += kWarps * per_warp) {
+    for (int base = (trank * kWarps + warp) * per_warp; base < count; base += tsize * kWarps * per_warp) {
         const int r = base + wl / G;
         const bool valid = r < count;
         typename Epi::Pre pre;
@@ -93,26 +182,26 @@ __device__ __forceinline__ void group_rows(const int32_t* __restrict__ ptr, cons
 
 template <int NV, class Acc, class Gather, class Epi>
 __device__ __forceinline__ void group_rows_dyn(int G, const int32_t* ptr, const int32_t* idx, const float* val,
-                                               int count, const Gather& g, Epi& e) {
+                                               int count, const Gather& g, Epi& e, int tr = 0, int ts = 1) {
     switch (G) {
-        case 1: group_rows<1, NV, Acc>(ptr, idx, val, count, g, e); break;
-        case 2: group_rows<2, NV, Acc>(ptr, idx, val, count, g, e); break;
-        case 4: group_rows<4, NV, Acc>(ptr, idx, val, count, g, e); break;
-        case 8: group_rows<8, NV, Acc>(ptr, idx, val, count, g, e); break;
-        case 16: group_rows<16, NV, Acc>(ptr, idx, val, count, g, e); break;
-        default: group_rows<32, NV, Acc>(ptr, idx, val, count, g, e); break;
+        case 1: group_rows<1, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        case 2: group_rows<2, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        case 4: group_rows<4, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        case 8: group_rows<8, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        case 16: group_rows<16, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        default: group_rows<32, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
     }
 }
 
 // Row passes: G lanes per row in {4, 8, 16, 32} (several rows per warp in flight).
 template <int NV, class Acc, class Gather, class Epi>
 __device__ __forceinline__ void group_rows_r(int G, const int32_t* ptr, const int32_t* idx, const float* val,
-                                             int count, const Gather& g, Epi& e) {
+                                             int count, const Gather& g, Epi& e, int tr = 0, int ts = 1) {
     switch (G) {
-        case 4: group_rows<4, NV, Acc>(ptr, idx, val, count, g, e); break;
-        case 8: group_rows<8, NV, Acc>(ptr, idx, val, count, g, e); break;
-        case 16: group_rows<16, NV, Acc>(ptr, idx, val, count, g, e); break;
-        default: group_rows<32, NV, Acc>(ptr, idx, val, count, g, e); break;
+        case 4: group_rows<4, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        case 8: group_rows<8, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        case 16: group_rows<16, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
+        default: group_rows<32, NV, Acc>(ptr, idx, val, count, g, e, tr, ts); break;
     }
 }
 

@@ -101,7 +101,8 @@ struct Engine : EngineBase {
     ~Engine() override {
         if (win_exec) cudaGraphExecDestroy(win_exec);
         if (loop_exec) cudaGraphExecDestroy(loop_exec);
-        if (arena) cudaFree(arena);
+        if (arena) cudaFreeAsync(arena, st);
+        if (st) cudaStreamSynchronize(st);
         if (h_ctl) cudaFreeHost(h_ctl);
         if (h_abort) cudaFreeHost(h_abort);
         if (ev0) cudaEventDestroy(ev0);
@@ -283,11 +284,11 @@ struct Engine : EngineBase {
         // ---- staging upload and validation
         int32_t *s_ptr, *s_idx, *s_colcount, *s_err;
         double* s_val;
-        SPS_CK(cudaMalloc(&s_ptr, sizeof(int32_t) * (m + 1)));
-        SPS_CK(cudaMalloc(&s_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
-        SPS_CK(cudaMalloc(&s_val, sizeof(double) * std::max<int64_t>(nnz, 1)));
-        SPS_CK(cudaMalloc(&s_colcount, sizeof(int32_t) * (n + 1)));
-        SPS_CK(cudaMalloc(&s_err, sizeof(int32_t)));
+        SPS_CK(cudaMallocAsync(&s_ptr, sizeof(int32_t) * (m + 1), st));
+        SPS_CK(cudaMallocAsync(&s_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(cudaMallocAsync(&s_val, sizeof(double) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(cudaMallocAsync(&s_colcount, sizeof(int32_t) * (n + 1), st));
+        SPS_CK(cudaMallocAsync(&s_err, sizeof(int32_t), st));
         SPS_CK(cudaMemcpyAsync(s_ptr, hp.ptr.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
         {
             int64_t off = 0;
@@ -308,7 +309,7 @@ struct Engine : EngineBase {
         SPS_CK(cudaMemcpyAsync(&herr, s_err, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
         SPS_CK(cudaStreamSynchronize(st));
         if (herr) {
-            cudaFree(s_ptr); cudaFree(s_idx); cudaFree(s_val); cudaFree(s_colcount); cudaFree(s_err);
+            cudaFreeAsync(s_ptr, st); cudaFreeAsync(s_idx, st); cudaFreeAsync(s_val, st); cudaFreeAsync(s_colcount, st); cudaFreeAsync(s_err, st);
             return fail(SPS_ERR_INVALID, (herr & SE_INDEX) ? "column index out of range [0, n)"
                                                            : "non-finite constraint matrix value");
         }
@@ -320,7 +321,7 @@ struct Engine : EngineBase {
         make_plan(clen, nullptr, cp, block_cap);
         const std::vector<int32_t>& perm_col = cp.perm;
         if (rp.total > INT32_MAX || cp.total > INT32_MAX) {
-            cudaFree(s_ptr); cudaFree(s_idx); cudaFree(s_val); cudaFree(s_colcount); cudaFree(s_err);
+            cudaFreeAsync(s_ptr, st); cudaFreeAsync(s_idx, st); cudaFreeAsync(s_val, st); cudaFreeAsync(s_colcount, st); cudaFreeAsync(s_err, st);
             return fail(SPS_ERR_INVALID, "padded matrix layout exceeds 2^31-1 entries");
         }
         std::vector<int32_t> inv_col(n);
@@ -405,7 +406,7 @@ struct Engine : EngineBase {
         add(&d_wy, sizeof(double) * m);
         size_t total = 0;
         for (auto& p : plan) total += p.second;
-        SPS_CK(cudaMalloc(&arena, total));
+        SPS_CK(cudaMallocAsync(&arena, total, st));
         {
             size_t off = 0;
             for (auto& p : plan) { *p.first = arena + off; off += p.second; }
@@ -415,15 +416,15 @@ struct Engine : EngineBase {
         // ---- internal CSR and CSC temporaries (FP64 values)
         int32_t *t_inv_col, *t_fill, *t_ptr, *t_idx, *t_cptr, *t_cidx;
         double *t_rval, *t_cval, *t_stat;
-        SPS_CK(cudaMalloc(&t_inv_col, sizeof(int32_t) * n));
-        SPS_CK(cudaMalloc(&t_fill, sizeof(int32_t) * n));
-        SPS_CK(cudaMalloc(&t_ptr, sizeof(int32_t) * (m + 1)));
-        SPS_CK(cudaMalloc(&t_cptr, sizeof(int32_t) * (n + 1)));
-        SPS_CK(cudaMalloc(&t_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
-        SPS_CK(cudaMalloc(&t_cidx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
-        SPS_CK(cudaMalloc(&t_rval, sizeof(double) * std::max<int64_t>(nnz, 1)));
-        SPS_CK(cudaMalloc(&t_cval, sizeof(double) * std::max<int64_t>(nnz, 1)));
-        SPS_CK(cudaMalloc(&t_stat, sizeof(double) * 2 * (size_t)(n + m)));
+        SPS_CK(cudaMallocAsync(&t_inv_col, sizeof(int32_t) * n, st));
+        SPS_CK(cudaMallocAsync(&t_fill, sizeof(int32_t) * n, st));
+        SPS_CK(cudaMallocAsync(&t_ptr, sizeof(int32_t) * (m + 1), st));
+        SPS_CK(cudaMallocAsync(&t_cptr, sizeof(int32_t) * (n + 1), st));
+        SPS_CK(cudaMallocAsync(&t_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(cudaMallocAsync(&t_cidx, sizeof(int32_t) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(cudaMallocAsync(&t_rval, sizeof(double) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(cudaMallocAsync(&t_cval, sizeof(double) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(cudaMallocAsync(&t_stat, sizeof(double) * 2 * (size_t)(n + m), st));
         SPS_CK(cudaMemcpyAsync(d_perm_row, perm_row.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
         SPS_CK(cudaMemcpyAsync(d_perm_col, perm_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
         SPS_CK(cudaMemcpyAsync(t_inv_col, inv_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
@@ -445,7 +446,7 @@ struct Engine : EngineBase {
             SPS_CK(cudaGetLastError());
         }
         SPS_CK(cudaStreamSynchronize(st));
-        cudaFree(s_ptr); cudaFree(s_idx); cudaFree(s_val); cudaFree(s_colcount); cudaFree(s_err);
+        cudaFreeAsync(s_ptr, st); cudaFreeAsync(s_idx, st); cudaFreeAsync(s_val, st); cudaFreeAsync(s_colcount, st); cudaFreeAsync(s_err, st);
         // columns too long for the device insertion sort: order on the host
         for (int j = 0; j < n; ++j) {
             const int64_t len = cptr[j + 1] - cptr[j];
@@ -492,10 +493,10 @@ struct Engine : EngineBase {
         }
         // scaled values in the iterate precision
         SPS_CK(cudaStreamSynchronize(st));
-        cudaFree(t_stat);
+        cudaFreeAsync(t_stat, st);
         V *t_rvV, *t_cvV;
-        SPS_CK(cudaMalloc(&t_rvV, sizeof(V) * std::max<int64_t>(nnz, 1)));
-        SPS_CK(cudaMalloc(&t_cvV, sizeof(V) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(cudaMallocAsync(&t_rvV, sizeof(V) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(cudaMallocAsync(&t_cvV, sizeof(V) * std::max<int64_t>(nnz, 1), st));
         k_finish_values<V><<<warp_grid_m, kBlock, 0, st>>>(t_ptr, t_idx, t_rval, d_dr, d_dc, t_rvV, m);
         k_finish_values<V><<<warp_grid_n, kBlock, 0, st>>>(t_cptr, t_cidx, t_cval, d_dc, d_dr, t_cvV, n);
         SPS_CK(cudaGetLastError());
@@ -517,7 +518,7 @@ struct Engine : EngineBase {
             for (int j = 0; j < n; ++j) { const int o = perm_col[j]; ci[j] = hp.c[o]; li[j] = hp.lb[o]; ui[j] = hp.ub[o]; }
             for (int r = 0; r < m; ++r) bi[r] = hp.rhs[perm_row[r]];
             double *t_c, *t_l, *t_u, *t_b;
-            SPS_CK(cudaMalloc(&t_c, sizeof(double) * (3 * (size_t)n + m)));
+            SPS_CK(cudaMallocAsync(&t_c, sizeof(double) * (3 * (size_t)n + m), st));
             t_l = t_c + n; t_u = t_l + n; t_b = t_u + n;
             SPS_CK(cudaMemcpyAsync(t_c, ci.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
             SPS_CK(cudaMemcpyAsync(t_l, li.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
@@ -528,21 +529,21 @@ struct Engine : EngineBase {
             if (d_idc) k_reciprocals<<<grid_for(std::max(n, m)), kBlock, 0, st>>>(d_dc, d_dr, d_idc, d_idr, n, m);
             SPS_CK(cudaGetLastError());
             SPS_CK(cudaStreamSynchronize(st));
-            cudaFree(t_c);
+            cudaFreeAsync(t_c, st);
         }
-        cudaFree(t_inv_col); cudaFree(t_fill); cudaFree(t_ptr); cudaFree(t_cptr); cudaFree(t_idx);
-        cudaFree(t_cidx); cudaFree(t_rval); cudaFree(t_cval); cudaFree(t_rvV); cudaFree(t_cvV);
+        cudaFreeAsync(t_inv_col, st); cudaFreeAsync(t_fill, st); cudaFreeAsync(t_ptr, st); cudaFreeAsync(t_cptr, st); cudaFreeAsync(t_idx, st);
+        cudaFreeAsync(t_cidx, st); cudaFreeAsync(t_rval, st); cudaFreeAsync(t_cval, st); cudaFreeAsync(t_rvV, st); cudaFreeAsync(t_cvV, st);
 
         // ---- start-up constants: eta0 = 1 / max|K~|, omega0 = ||c~|| / ||b~||
         {
             const int g = kSms * 2;
             double* t_n;
-            SPS_CK(cudaMalloc(&t_n, sizeof(double) * 3 * g));
+            SPS_CK(cudaMallocAsync(&t_n, sizeof(double) * 3 * g, st));
             k_norms<V><<<g, kBlock, 0, st>>>(d_rval, rp.total, d_c, n, d_b, m, t_n);
             std::vector<double> hn(3 * g);
             SPS_CK(cudaMemcpyAsync(hn.data(), t_n, sizeof(double) * 3 * g, cudaMemcpyDeviceToHost, st));
             SPS_CK(cudaStreamSynchronize(st));
-            cudaFree(t_n);
+            cudaFreeAsync(t_n, st);
             double mx = 0, sc = 0, sb = 0;
             for (int q = 0; q < g; ++q) { mx = std::max(mx, hn[3 * q]); sc += hn[3 * q + 1]; sb += hn[3 * q + 2]; }
             eta0 = mx > 0 ? 1.0 / mx : 1.0;

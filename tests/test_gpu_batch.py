@@ -67,3 +67,33 @@ def test_batch_iteration_limit():
     res = sps.solve_lp_pdhg_batch(probs[:5], tol=1e-12, max_iters=128)
     for r in res:
         assert r.status == "iteration_limit" and r.iterations == 128
+
+
+def _large_batch():
+    """Planted instances of the batched workload with at least 65 536 nonzeros
+    (solved by a cluster of blocks) mixed with small ones (one block each)."""
+    probs = []
+    for k in range(200):
+        p, info = wl.batch_planted_lp(k)
+        if p.A_eq.nnz >= 65536 and sum(q.A_eq.nnz >= 65536 for q in probs) < 6:
+            probs.append(p)
+    probs += [wl.batch_planted_lp(k, m_range=(20, 300))[0] for k in range(10)]
+    return probs
+
+
+def test_team_solves_large_instances():
+    probs = _large_batch()
+    assert sum(p.A_eq.nnz >= 65536 for p in probs) >= 4
+    with sps.PDHGBatch(probs, tol=TOL, batch_team=4) as b:
+        team = b.solve()
+        assert b.stats.team == 4
+        again = b.solve()                     # graph replay: same bits
+    with sps.PDHGBatch(probs, tol=TOL, batch_team=1) as b:
+        solo = b.solve()
+        assert b.stats.team == 1
+    for p, t, a, s in zip(probs, team, again, solo):
+        assert t.status == "optimal" and s.status == "optimal", p.name
+        assert kkt.box_rel_kkt(p, t.x, t.y)["err"] < 1.5 * TOL, p.name
+        assert t.iterations == a.iterations
+        np.testing.assert_array_equal(t.x, a.x)
+        assert abs(t.objective - s.objective) <= 50 * TOL * (1 + abs(s.objective))
