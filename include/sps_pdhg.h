@@ -94,7 +94,7 @@ typedef struct {
     int32_t batch_team;       /* batched solver: blocks (one thread-block cluster) per large
                                  instance, 1..8; 0 = 2; 1 = one block per instance */
     int32_t batch_team_nnz;   /* batched solver: instances with at least this many nonzeros are
-                                 large; 0 = 65536 */
+                                 large; 0 = the larger of 65536 and twice the median instance */
     int32_t reserved[1];
 } sps_options;
 

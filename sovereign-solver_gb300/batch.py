@@ -29,7 +29,7 @@ class PDHGBatch:
     The lanes per row of the row pass (4, 8, 16, 32) are always timed.
     ``batch_team``: blocks (a thread-block cluster) per large instance, 0 = 2,
     1 = one block per instance; ``batch_team_nnz``: nonzeros from which an
-    instance is large (0 = 65 536).
+    instance is large (0 = the larger of 65 536 and twice the median instance).
     ``escalate``: "fp64" (FP64 continuation of stalled instances), "stop"
     (status "stalled") or "off" (FP32 to the iteration limit).
     """

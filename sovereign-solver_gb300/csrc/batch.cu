@@ -890,7 +890,15 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
     std::iota(b->order.begin(), b->order.end(), 0);
     std::stable_sort(b->order.begin(), b->order.end(), [&](int32_t a, int32_t c) { return work[a] > work[c]; });
     // large instances (solved by a team of blocks when clusters are available)
-    b->team_nnz = opt.batch_team_nnz > 0 ? opt.batch_team_nnz : sps::batch::kTeamNnz;
+    // large = at least 65536 nonzeros and twice the median instance: teams shorten the
+    // tail of uneven batches; in batches of similar sizes they would only halve
+    // the number of instances in flight
+    if (opt.batch_team_nnz > 0) {
+        b->team_nnz = opt.batch_team_nnz;
+    } else {
+        const int32_t med = b->inst[b->order[count / 2]].nnz;
+        b->team_nnz = (int32_t)std::max<int64_t>(sps::batch::kTeamNnz, 2LL * med);
+    }
 
     // ---- device
     sps_batch* bp = b.get();

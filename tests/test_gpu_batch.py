@@ -97,3 +97,34 @@ def test_team_solves_large_instances():
         assert t.iterations == a.iterations
         np.testing.assert_array_equal(t.x, a.x)
         assert abs(t.objective - s.objective) <= 50 * TOL * (1 + abs(s.objective))
+
+
+def test_batch_edge_cases():
+    """An instance with no rows, one with an empty column, beside a normal one."""
+    import scipy.sparse as sp
+    no_rows = sps.Problem(c=np.array([1.0, -1.0, 0.5]), A_ub=sp.csr_matrix((0, 3)), b_ub=np.zeros(0),
+                          A_eq=sp.csr_matrix((0, 3)), b_eq=np.zeros(0), lb=np.zeros(3),
+                          ub=np.array([1.0, 2.0, 3.0]), integer_mask=np.zeros(3, bool), name="no_rows")
+    A = sp.csr_matrix(np.array([[1.0, 1.0, 0.0], [1.0, -1.0, 0.0]]))
+    empty_col = sps.Problem(c=np.array([1.0, 2.0, 3.0]), A_ub=sp.csr_matrix((0, 3)), b_ub=np.zeros(0),
+                            A_eq=A, b_eq=np.array([2.0, 0.0]), lb=np.zeros(3), ub=np.full(3, np.inf),
+                            integer_mask=np.zeros(3, bool), name="empty_column")
+    normal = wl.batch_planted_lp(3, m_range=(50, 200))[0]
+    probs = [no_rows, empty_col, normal]
+    with sps.PDHGBatch(probs, tol=TOL) as b:
+        res = b.solve()
+    for p, r in zip(probs, res):
+        assert r.status == "optimal", (p.name, r.status)
+        assert kkt.box_rel_kkt(p, r.x, r.y)["err"] < 1.5 * TOL, p.name
+    np.testing.assert_allclose(res[0].x[:2], [0.0, 2.0], atol=1e-6)
+    assert abs(res[0].objective - (-2.0)) < 1e-5
+    np.testing.assert_allclose(res[1].x, [1.0, 1.0, 0.0], atol=2e-3)
+
+
+def test_batch_time_limit():
+    """A time limit far below the solve time stops the launch: statuses time_limit, no error."""
+    probs = [wl.batch_planted_lp(k)[0] for k in range(64)]
+    with sps.PDHGBatch(probs, tol=1e-8, time_limit=0.05, escalate="off") as b:
+        res = b.solve()
+        assert b.stats.solve_ms < 5000
+    assert sum(r.status == "time_limit" for r in res) >= 32
