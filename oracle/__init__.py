@@ -18,7 +18,9 @@ Contents
                box-form relative KKT the GPU engine reports.
 ``pdlp_ref``   FP64 restatement of the GPU engine's adaptive ("PDLP") mode, for
                step-by-step comparison on small problems.
-``simplex``    FP64 bounded revised simplex, the objective oracle.
+``simplex``    FP64 bounded revised simplex (two phases, dense LU), the objective
+               oracle; matches the reference simplex on every golden problem.
+``gnn_ref``    FP64 restatement of the warm-start network (forward, backward).
 ``pdhg_ref.c`` C + OpenMP restatement of ``pdhg_ref`` used as the timed CPU
                baseline (all host threads).
 """
