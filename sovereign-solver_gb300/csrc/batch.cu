@@ -418,7 +418,7 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
 // 0 takes it for the whole cluster (every block reads the index from rank 0's
 // shared memory between two team barriers) and the team solves it; from the
 // first smaller instance on, every block takes its own instances.
-__global__ void __launch_bounds__(kBlock, 2) k_batch_solve(Args A, int G) {
+__global__ void __launch_bounds__(kBlock, 4) k_batch_solve(Args A, int G) {
     __shared__ Ctl c;
     __shared__ double sm[kWarps * 10];
     __shared__ double slots[10 * kBlock];
