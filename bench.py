@@ -442,9 +442,9 @@ TEST_SEED0 = 10_000_000          # held-out seeds (training used 0 .. 19 999)
 
 def run_warmstart(args, rank, world):
     """Learned warm start on the 200 x 400 transportation family: ``--batch``
-    held-out seeds (per GPU).  One step = GNN inference (device features) +
-    warm starts + one batched solve of every seed, batch resident; value =
-    solves/s.  Reported beside it: the same batch solved cold, and cold
+    held-out seeds (per GPU).  One step = GNN inference on the device straight
+    into the batch's warm-start buffers + one batched solve of every seed,
+    batch resident; value = solves/s.  Reported beside it: the same batch solved cold, and cold
     single-instance PDHG (create + solve + read-back per LP) on a sample.
     e2e = sps_batch_create + inference + warm starts + solve + read-back of
     every instance from host arrays."""
@@ -474,9 +474,8 @@ def run_warmstart(args, rank, world):
     # warm batched (resident): inference + warm starts + solve
     def warm_step():
         t0 = time.perf_counter()
-        starts = net.predict(probs)
+        b.set_warm_starts_gnn(net)              # inference on the device into the batch's buffers
         t1 = time.perf_counter()
-        b.set_warm_starts(starts)
         st = b.solve_raw()
         return t1 - t0, st.solve_ms / 1e3, time.perf_counter() - t0
     for _ in range(args.warmup):
@@ -503,16 +502,13 @@ def run_warmstart(args, rank, world):
     opts = pdhg.make_options(tol=args.tol, max_iters=args.max_iters, device=args.device)
     xs = [np.empty(p.n_vars) for p in probs]
     ys = [np.empty(p.n_ineq + p.n_eq) for p in probs]
+    scales = np.array([net.scales[k] for k in ("c", "b", "x", "y")], dtype=np.float64)
     e2e_s = []
     for _ in range(max(1, args.e2e_steps)):
         t0 = time.perf_counter()
         h = C.c_void_p()
         N.check(lib.sps_batch_create(len(descs), arr, C.byref(opts), C.byref(h)), None)
-        starts = net.predict(probs)
-        wx = np.concatenate([s_[0] for s_ in starts])
-        wy = np.concatenate([s_[1] for s_ in starts])
-        wo = np.array([s_[2] for s_ in starts])
-        rc = lib.sps_batch_set_warm_starts(h, N.f64p(wx), N.f64p(wy), N.f64p(wo))
+        rc = lib.sps_batch_set_warm_starts_gnn(h, net.h, N.f64p(scales))
         sst = N.BatchStats()
         rc = rc or lib.sps_batch_solve(h, C.byref(sst))
         rr = N.Result()
@@ -537,7 +533,9 @@ def run_warmstart(args, rank, world):
     per_it = 16 * nnz + 4 * (m_ + 1) + 4 * n_ + 20 * m_ + 4 * (n_ + 1) + 4 * m_ + 28 * n_ + 16 * m_
     solve_s = np.mean([s_[1] for s_ in steps])
     achieved = float(wi.sum()) * per_it / solve_s / 1e9
-    fwd_launches = 9 + 4 * net.layers
+    # per chunk of 16 instances: 2 LP-feature kernels + 19 network kernels (L = 3) +
+    # the batch's input and output kernels; per step 3 batch kernels
+    fwd_launches = 9 + 4 * net.layers + 2
     line = {
         "metric": METRIC,
         "value": value, "unit": "solves/s",

@@ -31,6 +31,8 @@
 
 #include <stdint.h>
 
+#include "sps_pdhg.h"
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -86,6 +88,18 @@ int sps_gnn_get_params(sps_gnn *g, float *out);
 int sps_gnn_set_params(sps_gnn *g, const float *in);
 const char *sps_gnn_last_error(const sps_gnn *g);
 void sps_gnn_destroy(sps_gnn *g);
+
+/* Warm starts for every instance of a batch predicted on the device: the
+ * network's inputs are built from the batch's own data (c / c_scale, b /
+ * b_scale), the forward pass runs in chunks of max_batch instances, and the
+ * outputs (x0 * x_scale, y0 * y_scale, exp(log_omega)) go straight into the
+ * batch's warm-start buffers — nothing crosses the host.  scales = {c_scale,
+ * b_scale, x_scale, y_scale}.  The network must use lp_features, live on the
+ * batch's device, and every instance must have the network's n and m (same
+ * constraint pattern; only the sizes are checked).  The batch's cold-start
+ * fallback applies as for sps_batch_set_warm_starts.  Errors:
+ * sps_batch_last_error(b). */
+int sps_batch_set_warm_starts_gnn(sps_batch *b, sps_gnn *g, const double *scales);
 
 #ifdef __cplusplus
 }

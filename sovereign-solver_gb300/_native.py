@@ -142,6 +142,7 @@ def load() -> C.CDLL:
         "sps_gnn_set_params": (C.c_int, [H, _f32p]),
         "sps_gnn_last_error": (C.c_char_p, [H]),
         "sps_gnn_destroy": (None, [H]),
+        "sps_batch_set_warm_starts_gnn": (C.c_int, [H, H, _f64p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -81,6 +81,13 @@ class PDHGBatch:
         y = np.ascontiguousarray(np.concatenate(ys))
         self._check(self.lib.sps_batch_set_warm_starts(self.h, N.f64p(x), N.f64p(y), N.f64p(om)))
 
+    def set_warm_starts_gnn(self, net) -> None:
+        """Warm starts predicted on the device by ``net`` (a ``WarmStartGNN`` with LP
+        features for this batch's constraint pattern) for every problem; nothing
+        crosses the host."""
+        sc = np.array([net.scales[k] for k in ("c", "b", "x", "y")], dtype=np.float64)
+        self._check(self.lib.sps_batch_set_warm_starts_gnn(self.h, net.h, N.f64p(sc)))
+
     def solve_raw(self) -> N.BatchStats:
         st = N.BatchStats()
         self._check(self.lib.sps_batch_solve(self.h, C.byref(st)))

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "batch.cuh"
+#include "gnn_internal.cuh"
 
 namespace sps {
 void set_create_error(const std::string& msg);
@@ -570,6 +571,37 @@ __global__ void __launch_bounds__(kBlock) k_batch_setup(SetupArgs S) {
         S.eta0[k] = mx > 0.0 ? 1.0 / mx : 1.0;
         S.omega0[k] = (s2[0] > 1e-20 && s2[1] > 1e-20) ? sqrt(s2[0]) / sqrt(s2[1]) : 1.0;
     }
+}
+
+// Inputs of the warm-start network for instances s0 .. s0+cnt-1 from the batch's
+// scaled data: c = c~ / dc, b = b~ / dr (the original costs and right-hand sides).
+__global__ void __launch_bounds__(kBlock) k_gnn_inputs(const Inst* inst, int s0, int cnt, Arrays a, int n, int m,
+                                                       double inv_cs, double inv_bs, float* c_in, float* b_in) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)cnt * n; t += stride) {
+        const Inst& I = inst[s0 + t / n];
+        const int64_t q = I.vc + t % n;
+        c_in[t] = float(double(a.c[q]) / a.dc[q] * inv_cs);
+    }
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)cnt * m; t += stride) {
+        const Inst& I = inst[s0 + t / m];
+        const int64_t q = I.vr + t % m;
+        b_in[t] = float(double(a.b[q]) / a.dr[q] * inv_bs);
+    }
+}
+
+// Network outputs of instances s0 .. s0+cnt-1 into the warm-start buffers (the
+// start-up kernel projects them on the bounds and signs).
+__global__ void __launch_bounds__(kBlock) k_gnn_outputs(const Inst* inst, int s0, int cnt, int n, int m,
+                                                        const float* x0, const float* y0, const float* lw, double xs,
+                                                        double ys, double* wx, double* wy, double* wom) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)cnt * n; t += stride)
+        wx[inst[s0 + t / n].vc + t % n] = double(x0[t]) * xs;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)cnt * m; t += stride)
+        wy[inst[s0 + t / m].vr + t % m] = double(y0[t]) * ys;
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < cnt; t += stride)
+        wom[s0 + t] = exp(fmin(fmax(double(lw[t]), -30.0), 30.0));
 }
 
 // Absolute device deadline of a batched solve (0 = none), set at the start of
@@ -1217,6 +1249,45 @@ extern "C" int sps_batch_set_warm_starts(sps_batch* b, const double* x0, const d
     else SPB_CK(cudaMemsetAsync(b->d_wy, 0, sizeof(double) * b->sum_m, b->st));
     SPB_CK(cudaMemcpyAsync(b->d_wom, om.data(), sizeof(double) * b->count, cudaMemcpyHostToDevice, b->st));
     SPB_CK(cudaStreamSynchronize(b->st));
+    b->warm = 1;
+    return SPS_OK;
+}
+
+extern "C" int sps_batch_set_warm_starts_gnn(sps_batch* b, sps_gnn* g, const double* scales) {
+    if (!b) return SPS_ERR_INVALID;
+    if (!g || !scales) return b->fail(SPS_ERR_INVALID, "need a network and its four scales");
+    for (int q = 0; q < 4; ++q)
+        if (!(scales[q] > 0.0) || !std::isfinite(scales[q])) return b->fail(SPS_ERR_INVALID, "scales must be positive");
+    sps::gnn::DeviceIO io{};
+    if (sps::gnn::device_io(g, &io) != 0) return b->fail(SPS_ERR_INVALID, "invalid network");
+    if (!io.lp_features) return b->fail(SPS_ERR_INVALID, "the network must take LP features (lp_features = 1)");
+    if (io.device != b->opt.device) return b->fail(SPS_ERR_INVALID, "the network lives on another device");
+    if (b->opt.mode != SPS_MODE_ADAPTIVE) return b->fail(SPS_ERR_STATE, "warm starts need the adaptive mode");
+    for (int32_t k = 0; k < b->count; ++k)
+        if (b->inst[k].n != io.n || b->inst[k].m != io.m)
+            return b->fail(SPS_ERR_INVALID, "instance " + std::to_string(k) + " does not have the network's shape");
+    SPB_CK(cudaSetDevice(b->opt.device));
+    if (!b->d_wx) {
+        SPB_CK(b->alloc(&b->d_wx, b->sum_n));
+        SPB_CK(b->alloc(&b->d_wy, b->sum_m));
+        SPB_CK(b->alloc(&b->d_wom, b->count));
+    }
+    for (int32_t s0 = 0; s0 < b->count; s0 += io.max_batch) {
+        const int cnt = std::min<int32_t>(io.max_batch, b->count - s0);
+        const int64_t work = (int64_t)cnt * std::max(io.n, io.m);
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((work + 255) / 256, 152 * 8));
+        sps::batch::k_gnn_inputs<<<grid, sps::kBlock, 0, io.stream>>>(b->d_inst, s0, cnt, b->arr, io.n, io.m,
+                                                                      1.0 / scales[0], 1.0 / scales[1], io.c_in,
+                                                                      io.b_in);
+        SPB_CK(cudaGetLastError());
+        if (int rc = sps::gnn::forward_in_place(g, cnt))
+            return b->fail(rc == -1 ? SPS_ERR_INVALID : SPS_ERR_CUDA, std::string("network: ") + sps_gnn_last_error(g));
+        sps::batch::k_gnn_outputs<<<grid, sps::kBlock, 0, io.stream>>>(b->d_inst, s0, cnt, io.n, io.m, io.x0, io.y0,
+                                                                       io.log_omega, scales[2], scales[3], b->d_wx,
+                                                                       b->d_wy, b->d_wom);
+        SPB_CK(cudaGetLastError());
+    }
+    SPB_CK(cudaStreamSynchronize(io.stream));
     b->warm = 1;
     return SPS_OK;
 }

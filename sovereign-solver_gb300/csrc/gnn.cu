@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "../../include/sps_gnn.h"
+#include "gnn_internal.cuh"
 
 namespace {
 
@@ -724,6 +725,38 @@ int run_loss_grad(sps_gnn* g, int batch, double* loss) {
 }
 
 }  // namespace
+
+namespace sps {
+namespace gnn {
+
+int device_io(sps_gnn* g, DeviceIO* io) {
+    if (!g || !io) return -1;
+    io->n = g->n;
+    io->m = g->m;
+    io->max_batch = g->B;
+    io->lp_features = g->lpf;
+    io->device = g->opt.device;
+    io->stream = g->st;
+    io->c_in = g->craw;
+    io->b_in = g->braw;
+    io->x0 = g->x0;
+    io->y0 = g->y0;
+    io->log_omega = g->lw;
+    return 0;
+}
+
+int forward_in_place(sps_gnn* g, int batch) {
+    if (!g || !g->lpf || batch < 1 || batch > g->B) return g ? g->fail(-1, "forward_in_place needs lp_features") : -1;
+    k_lp_con_features<<<grid_for((int64_t)g->m * batch * 32, kT), kT, 0, g->st>>>(
+        g->cptr, g->cidx, g->kind, g->craw, g->braw, g->n, g->m, batch, g->fc, g->cmin);
+    k_lp_var_features<<<grid_for((int64_t)g->n * batch, kT), kT, 0, g->st>>>(g->vptr, g->vidx, g->kind, g->craw,
+                                                                          g->cmin, g->n, g->m, batch, g->fv);
+    if (cudaGetLastError() != cudaSuccess) return g->fail(-2, "feature kernels failed to launch");
+    return g->H == 64 ? forward<64>(g, batch) : forward<32>(g, batch);
+}
+
+}  // namespace gnn
+}  // namespace sps
 
 extern "C" {
 

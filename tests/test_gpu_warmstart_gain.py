@@ -39,3 +39,26 @@ def test_learned_warm_start_gain_on_held_out_seeds():
     for p, r in zip(probs, warm):
         assert r.status == "optimal"
         assert kkt.box_rel_kkt(p, r.x, r.y)["err"] < 1.5 * TOL
+
+
+def test_device_predicted_warm_starts():
+    """The same network predicting on the device straight into the batch's
+    warm-start buffers (sps_batch_set_warm_starts_gnn) gives the same gain."""
+    fam = TransportFamily()
+    template = fam.problem(0)
+    probs = transport_instances(fam, template, range(20_000_100, 20_000_140))
+    with WarmStartGNN.load(WEIGHTS, template, max_batch=16) as net, sps.PDHGBatch(probs, tol=TOL) as b:
+        cold = b.solve()
+        b.set_warm_starts_gnn(net)
+        warm = b.solve()
+        b.set_warm_starts(net.predict(probs))      # host path, for comparison
+        host = b.solve()
+    ci = np.array([r.iterations for r in cold], float)
+    wi = np.array([r.iterations for r in warm], float)
+    hi = np.array([r.iterations for r in host], float)
+    assert sum(r.stats["warm_start_used"] for r in warm) >= 0.9 * len(probs)
+    assert wi.mean() <= 0.75 * ci.mean()
+    assert abs(wi.mean() - hi.mean()) <= 0.1 * hi.mean()
+    for p, r in zip(probs, warm):
+        assert r.status == "optimal"
+        assert kkt.box_rel_kkt(p, r.x, r.y)["err"] < 1.5 * TOL
