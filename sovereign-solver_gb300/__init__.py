@@ -12,7 +12,8 @@ from .result import SolveResult
 from .pdhg import PDHGEngine, get_available_device, solve_lp_pdhg, solve_lp_pdhg_gpu
 from .solver import Solver
 from .batch import PDHGBatch, solve_lp_pdhg_batch
+from .mps import read_mps
 
 __version__ = "0.1.0"
 __all__ = ["Solver", "Problem", "SolveResult", "PDHGEngine", "solve_lp_pdhg",
-           "solve_lp_pdhg_gpu", "get_available_device", "PDHGBatch", "solve_lp_pdhg_batch"]
+           "solve_lp_pdhg_gpu", "get_available_device", "PDHGBatch", "solve_lp_pdhg_batch", "read_mps"]
