@@ -41,6 +41,10 @@ extern "C" {
 #define SPS_STATUS_NUMERIC_ERROR    3   /* NaN/Inf appeared in the iterates */
 #define SPS_STATUS_STALLED          4   /* FP32 iterates stopped making progress (returned
                                            only with sps_options.escalate = 2) */
+#define SPS_STATUS_INFEASIBLE       5   /* adaptive mode: the change of y since the last restart is
+                                           a Farkas certificate (primal infeasible) */
+#define SPS_STATUS_UNBOUNDED        6   /* adaptive mode: the change of x since the last restart is
+                                           an improving ray (dual infeasible) */
 
 /* algorithm */
 #define SPS_MODE_REFERENCE  0  /* the reference's rules: standard form with bound rows and

@@ -22,7 +22,8 @@ ERRORS = {
     -4: "SPS_ERR_STATE",
     -5: "SPS_ERR_TIMEOUT",
 }
-STATUS = {0: "optimal", 1: "iteration_limit", 2: "time_limit", 3: "numeric_error", 4: "stalled"}
+STATUS = {0: "optimal", 1: "iteration_limit", 2: "time_limit", 3: "numeric_error", 4: "stalled",
+          5: "infeasible", 6: "unbounded"}
 ESCALATE = {"off": 0, "fp64": 1, "stop": 2}
 MODES = {"reference": 0, "adaptive": 1}
 PRECISIONS = {"fp32": 0, "fp64": 1}

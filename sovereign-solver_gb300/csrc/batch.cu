@@ -242,7 +242,7 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     }
     if (!team_total<19>(tt, T)) return false;
     if (threadIdx.x == 0) {
-        double tr[8], tc[10];
+        double tr[kRowPartials] = {}, tc[kColPartials] = {};   // no infeasibility partials here
         for (int q = 0; q < 8; ++q) tr[q] = tt[q];
         for (int q = 0; q < 10; ++q) tc[q] = tt[8 + q];
         decide_check(c, tc, tr, I.inv_nb, I.inv_nc, tt[18] > 0.0);

@@ -15,6 +15,12 @@ enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4, AP_STEP_PEND
 // Stall test: the best relative KKT error has not halved for
 // max(kStallMin, anchor / 2) attempts, anchor = attempt of the last halving.
 constexpr int64_t kStallMin = 2048;
+// Infeasibility tests on the change since the last restart (scaled space): a
+// certificate's residual must be at most kRayTol of its objective.
+constexpr double kRayTol = 1e-6;
+// Partials of a check: column pass tc[kColPartials], row pass tr[kRowPartials].
+constexpr int kColPartials = 14;
+constexpr int kRowPartials = 11;
 
 // Adaptive step (PDLP): limit = ||dz||_w^2 / (2 |dy^T K dx|); the attempt is
 // accepted if eta <= limit; next eta = min((1 - (k+1)^-0.3) limit, (1 + (k+1)^-0.6) eta).
@@ -50,6 +56,12 @@ __device__ __forceinline__ bool decide_step(Ctl& c, double dy2, double inter_sig
 // Check of the average (point 0) and the current iterate (point 1).
 //   tr[4q + 0..3]: scaled primal residual^2, original primal residual^2, b^T y, ||y - y_last||^2
 //   tc[5q + 0..4]: scaled dual residual^2, original dual residual^2, c^T x, bound terms, ||x - x_last||^2
+// and, for the change (dx, dy) of the current iterate since the last restart
+// (zeros where a caller does not compute them):
+//   tr[8]: ||K dx||^2 on the row kinds' cones,  tr[9]: b^T dy,
+//   tr[10]: violation^2 of dy against the dual cone (dy <= 0 on '<=' rows)
+//   tc[10]: cone residual^2 of lambda = -K^T dy,  tc[11]: its bound terms,
+//   tc[12]: violation^2 of dx against the bounds' recession cone,  tc[13]: c^T dx
 // Termination on the relative KKT error of the original problem; restart on the
 // weighted KKT of the scaled problem (to the better of average and current) when
 // it dropped below 0.2x the last restart's, or below 0.8x while rising, or after
@@ -58,8 +70,9 @@ __device__ __forceinline__ bool decide_step(Ctl& c, double dy2, double inter_sig
 // copying (AP_SAVE_BEST, with the primal weight in c.omega_best) and the solve
 // finishes with SPS_STATUS_STALLED when the best error stops halving (FP32
 // precision floor; the host continues in FP64 from the saved point).  Sets c.apply.
-__device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], const double (&tr)[8], double inv_nb,
-                                             double inv_nc, bool stop) {
+__device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[kColPartials],
+                                             const double (&tr)[kRowPartials], double inv_nb, double inv_nc,
+                                             bool stop) {
     const bool has_avg = c.w_sum > 0.0;
     const double w = c.omega;
     double rel[2], kw[2], rp[2], rd[2], gp[2], po[2], dob[2];
@@ -86,7 +99,7 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], con
         c.kkt_prev_cand = kw[1];
         c.rel_kkt = rel[1]; c.rel_p = rp[1]; c.rel_d = rd[1]; c.rel_gap = gp[1];
         c.pobj = po[1]; c.dobj = dob[1];
-        c.apply = AP_CANDIDATE;
+        c.apply = AP_CANDIDATE | AP_RESTART;   // the start point is the first restart point
         return;
     }
     const int best = (has_avg && rel[0] < rel[1]) ? 0 : 1;
@@ -113,6 +126,13 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[10], con
         c.status = SPS_STATUS_NUMERIC_ERROR; finish = true;
     } else if (rel[best] < c.tol) {
         c.status = SPS_STATUS_OPTIMAL; finish = true;
+    } else if (tr[9] + tc[11] > 0.0 && sqrt(tc[10] + tr[10]) <= kRayTol * (tr[9] + tc[11])) {
+        // y's change is a Farkas ray: lambda = -K^T dy lies in the bounds' cone and the
+        // dual objective of the ray, b^T dy + bound terms, is positive
+        c.status = SPS_STATUS_INFEASIBLE; finish = true;
+    } else if (tc[13] < 0.0 && sqrt(tr[8] + tc[12]) <= kRayTol * (-tc[13])) {
+        // x's change is an improving ray: K dx on the row cones, dx in the recession cone, c^T dx < 0
+        c.status = SPS_STATUS_UNBOUNDED; finish = true;
     } else if (c.iters >= c.max_iters) {
         c.status = SPS_STATUS_ITERATION_LIMIT; finish = true;
     } else if (stop) {

@@ -63,7 +63,7 @@ struct Layout {
     int32_t nsegrows;        // SEGMENT rows of this orientation
 };
 
-constexpr int kMaxEpiPartials = 10;
+constexpr int kMaxEpiPartials = 14;
 
 // Control block, one per handle, in device memory.  Written only by single
 // threads of "last blocks" or by block 0 thread 0, read by every kernel.

@@ -333,8 +333,8 @@ struct Engine : EngineBase {
         // ---- persistent arena
         const int tail = std::min(grid_for(m), kSms * 4);
         const int apply_blocks = grid_for(std::max(n, m), kBlock, kSms * 8);
-        const size_t part_row_n = (size_t)std::max(rp.bt.total_blocks, 1) * 8;
-        const size_t part_col_n = (size_t)(cp.bt.total_blocks + tail) * 10;
+        const size_t part_row_n = (size_t)std::max(rp.bt.total_blocks, 1) * kRowPartials;
+        const size_t part_col_n = (size_t)(cp.bt.total_blocks + tail) * kColPartials;
         const size_t part_aux_n = (size_t)std::max(apply_blocks, kSms * 16) * 3;
         const size_t nseg = std::max<size_t>(std::max(rp.seg_row.size(), cp.seg_row.size()), 1);
         const size_t ntk = (size_t)std::max(std::max(rp.ntickets, cp.ntickets), 1);
@@ -347,7 +347,7 @@ struct Engine : EngineBase {
         uint32_t* d_tickets;
         V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
         V *xs, *ys, *xl = nullptr, *yl = nullptr, *AXa = nullptr, *ATYa = nullptr, *xbar = nullptr;
-        V *xb = nullptr, *yb = nullptr;
+        V *xb = nullptr, *yb = nullptr, *AXl = nullptr, *ATYl = nullptr;
 
         // uniform bounds: every column [L, U] with L in {0, -inf}, U = +inf
         bool uniform = true;
@@ -393,6 +393,7 @@ struct Engine : EngineBase {
             add(&xl, sizeof(V) * n); add(&yl, sizeof(V) * m);
             add(&AXa, sizeof(V) * m); add(&ATYa, sizeof(V) * n);
             add(&d_idr, sizeof(double) * m); add(&d_idc, sizeof(double) * n);
+            add(&AXl, sizeof(V) * m); add(&ATYl, sizeof(V) * n);
             if (stall_test()) { add(&xb, sizeof(V) * n); add(&yb, sizeof(V) * m); }
         } else {
             add(&xbar, sizeof(V) * n);
@@ -578,6 +579,7 @@ struct Engine : EngineBase {
         a.AX[0] = AX0; a.AX[1] = AX1; a.ATY[0] = ATY0; a.ATY[1] = ATY1;
         a.xs = xs; a.ys = ys; a.xl = xl; a.yl = yl; a.AXa = AXa; a.ATYa = ATYa; a.xbar = xbar;
         a.xb = xb; a.yb = yb;
+        a.AXl = AXl; a.ATYl = ATYl;
         a.part_row = d_pr; a.part_col = d_pc; a.part_aux = d_pa;
         a.ctl = d_ctl;
         a.abort_flag = d_abort;

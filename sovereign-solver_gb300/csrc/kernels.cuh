@@ -42,6 +42,7 @@ struct Args {
     V* X[2]; V* Y[2]; V* AX[2]; V* ATY[2];
     V* xs; V* ys; V* xl; V* yl; V* AXa; V* ATYa; V* xbar;
     V* xb; V* yb;              // best point of the stall test (null unless it is on)
+    V* AXl; V* ATYl;           // adaptive: K x_last, K^T y_last (infeasibility tests)
     double* part_row; double* part_col; double* part_aux;
     Ctl* ctl;
     const volatile int32_t* abort_flag;
@@ -237,9 +238,11 @@ struct AdRowCheckEpi {
     const V *ys, *ylb, *yc, *yl;
     V* axa;
     double inv_w;
-    double p[8] = {0, 0, 0, 0, 0, 0, 0, 0};   // per point q: res_scaled^2, res_orig^2, b^T y, ||y - y_last||^2
+    // per point q: res_scaled^2, res_orig^2, b^T y, ||y - y_last||^2; then ||K dx||^2 (row cones),
+    // b^T dy, and dy's violation of the dual cone
+    double p[kRowPartials] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     using Pre = NoPre;
-    static constexpr int NP = 8;
+    static constexpr int NP = kRowPartials;
     __device__ __forceinline__ void zero() { for (int q = 0; q < NP; ++q) p[q] = 0.0; }
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
@@ -258,6 +261,12 @@ struct AdRowCheckEpi {
             const double d = yv - double(yl[r]);
             p[4 * q + 3] += d * d;
         }
+        double kdx = acc[1] - double(a->AXl[r]);
+        if (kind) kdx = fmax(kdx, 0.0);
+        p[8] += kdx * kdx;
+        const double dy = double(yc[r]) - double(yl[r]);
+        p[9] += br * dy;
+        if (kind) p[10] += fmax(dy, 0.0) * fmax(dy, 0.0);
     }
 };
 
@@ -265,7 +274,7 @@ template <class V>
 SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done) return;
-    __shared__ double sm[kWarps * 8];
+    __shared__ double sm[kWarps * kRowPartials];
     const int cur = ctl->cur;
     // with no average yet, point 0 aliases the current iterate
     const bool has_avg = ctl->w_sum > 0.0;
@@ -273,9 +282,9 @@ SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
     GatherTwo<V> g{has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], inv_w};
     AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], a.yl, a.AXa, inv_w};
     visit_bins<2, double>(a.rows, blockIdx.x, a.csr, g, e);
-    block_sum<8>(e.p, sm);
+    block_sum<kRowPartials>(e.p, sm);
     if (threadIdx.x == 0)
-        for (int q = 0; q < 8; ++q) a.part_row[(size_t)blockIdx.x * 8 + q] = e.p[q];
+        for (int q = 0; q < kRowPartials; ++q) a.part_row[(size_t)blockIdx.x * kRowPartials + q] = e.p[q];
 }
 
 template <class V>
@@ -284,9 +293,12 @@ struct AdColCheckEpi {
     const V *xs, *xlb, *xc, *xl;
     V* atya;
     double inv_w;
-    double p[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};  // per point: dres_s^2, dres_o^2, c^T x, bound terms, ||x - x_last||^2
+    // per point: dres_s^2, dres_o^2, c^T x, bound terms, ||x - x_last||^2; then for the
+    // change since the last restart: cone residual^2 of -K^T dy, its bound terms,
+    // recession-cone violation^2 of dx, c^T dx
+    double p[kColPartials] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     using Pre = NoPre;
-    static constexpr int NP = 10;
+    static constexpr int NP = kColPartials;
     __device__ __forceinline__ void zero() { for (int q = 0; q < NP; ++q) p[q] = 0.0; }
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
@@ -309,6 +321,14 @@ struct AdColCheckEpi {
             const double d = xv - double(xl[j]);
             p[5 * q + 4] += d * d;
         }
+        const double lr = -(acc[1] - double(a->ATYl[j]));
+        const double lp = (hl && hh) ? lr : hl ? fmax(lr, 0.0) : hh ? fmin(lr, 0.0) : 0.0;
+        p[10] += (lr - lp) * (lr - lp);
+        p[11] += (hl ? lo * fmax(lp, 0.0) : 0.0) + (hh ? hi * fmin(lp, 0.0) : 0.0);
+        const double dx = double(xc[j]) - double(xl[j]);
+        const double vx = (hl && hh) ? dx : hl ? fmin(dx, 0.0) : hh ? fmax(dx, 0.0) : 0.0;
+        p[12] += vx * vx;
+        p[13] += cj * dx;
     }
 };
 
@@ -316,7 +336,7 @@ template <class V>
 SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done) return;
-    __shared__ double sm[kWarps * 10];
+    __shared__ double sm[kWarps * kColPartials];
     __shared__ bool last;
     const int cur = ctl->cur;
     const bool has_avg = ctl->w_sum > 0.0;
@@ -324,12 +344,12 @@ SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], inv_w};
     AdColCheckEpi<V> e{&a, has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], a.xl, a.ATYa, inv_w};
     visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e);
-    if (!publish_partials<10>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
-    double tc[10], tr[8];
-    gather_partials<10>(tc, a.part_col, gridDim.x, sm);
-    gather_partials<8>(tr, a.part_row, a.rows.total_blocks, sm);
-    add_segment_rows<10>(tc, a.csc, sm);
-    add_segment_rows<8>(tr, a.csr, sm);
+    if (!publish_partials<kColPartials>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
+    double tc[kColPartials], tr[kRowPartials];
+    gather_partials<kColPartials>(tc, a.part_col, gridDim.x, sm);
+    gather_partials<kRowPartials>(tr, a.part_row, a.rows.total_blocks, sm);
+    add_segment_rows<kColPartials>(tc, a.csc, sm);
+    add_segment_rows<kRowPartials>(tr, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_CHECK] = 0;
     decide_check(*ctl, tc, tr, a.inv_nb, a.inv_nc, stop_requested(ctl, a.abort_flag));
@@ -359,7 +379,11 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
             } else {
                 xv = a.X[cur][j];
             }
-            if (rst) { a.xl[j] = xv; a.xs[j] = V(0); }
+            if (rst) {
+                a.xl[j] = xv;
+                a.xs[j] = V(0);
+                a.ATYl[j] = a.ATY[cur][j];
+            }
             if (cand) {
                 const V x2 = clampv(xv - tau * (a.c[j] - a.ATY[cur][j]), lo_at(a, j), hi_at(a, j));
                 a.X[1 - cur][j] = x2;
@@ -377,7 +401,11 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
             } else {
                 yv = a.Y[cur][i];
             }
-            if (rst) { a.yl[i] = yv; a.ys[i] = V(0); }
+            if (rst) {
+                a.yl[i] = yv;
+                a.ys[i] = V(0);
+                a.AXl[i] = a.AX[cur][i];
+            }
         }
         double v[1] = {double(dx2)};
         if (publish_partials<1>(v, a.part_aux, &ctl->ticket[T_APPLY], sm, &last)) {

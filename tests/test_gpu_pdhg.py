@@ -157,3 +157,32 @@ def test_solver_facade_drop_in():
 def test_empty_problem():
     r = sps.solve_lp_pdhg(sps.Problem.empty(3), mode="reference")
     assert r.status == "optimal" and r.iterations == 0 and np.all(r.x == 0)
+
+
+def _lp(c, A_ub, b_ub, lb, ub, A_eq=None, b_eq=None):
+    n = len(c)
+    return sps.Problem(c=np.asarray(c, float), A_ub=sp.csr_matrix(np.asarray(A_ub, float).reshape(-1, n)),
+                       b_ub=np.asarray(b_ub, float),
+                       A_eq=sp.csr_matrix((0, n)) if A_eq is None else sp.csr_matrix(np.asarray(A_eq, float)),
+                       b_eq=np.zeros(0) if b_eq is None else np.asarray(b_eq, float),
+                       lb=np.asarray(lb, float), ub=np.asarray(ub, float), integer_mask=np.zeros(n, bool))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_infeasible_and_unbounded_detected(precision):
+    """Certificates from the change since the last restart (the reference PDHG
+    has none and runs to its iteration limit)."""
+    inf = np.inf
+    infeasible = _lp([1, 1], [[1, 1], [-1, -1]], [1, -2], [0, 0], [inf, inf])       # x1+x2 <= 1 and >= 2
+    r = sps.solve_lp_pdhg(infeasible, max_iters=100000, tol=1e-6, precision=precision)
+    assert r.status == "infeasible", (r.status, r.iterations)
+    infeasible_eq = _lp([1, 2, 0], [[1, 1, 0]], [3], [0, 0, 0], [1, inf, inf],
+                        A_eq=[[1, 0, 1], [0, 1, -1]], b_eq=[-1, 2])                    # x1 + x3 = -1 with x >= 0
+    r = sps.solve_lp_pdhg(infeasible_eq, max_iters=100000, tol=1e-6, precision=precision)
+    assert r.status == "infeasible", (r.status, r.iterations)
+    unbounded = _lp([-1, 0], [[1, -1]], [1], [0, 0], [inf, inf])                    # min -x1, x1 - x2 <= 1
+    r = sps.solve_lp_pdhg(unbounded, max_iters=100000, tol=1e-6, precision=precision)
+    assert r.status == "unbounded", (r.status, r.iterations)
+    free_unbounded = _lp([1, -1], [[1, 1]], [4], [-inf, 0], [inf, inf])              # x1 free, min x1 - x2
+    r = sps.solve_lp_pdhg(free_unbounded, max_iters=100000, tol=1e-6, precision=precision)
+    assert r.status == "unbounded", (r.status, r.iterations)
