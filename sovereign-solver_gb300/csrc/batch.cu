@@ -113,6 +113,7 @@ struct RowCheckE {
     const int8_t* kind;
     float* axa;
     double inv_w;
+    const float* axl;          // K x_last
     double* p;                 // this thread's slots
     struct Pre {};
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
@@ -129,6 +130,12 @@ struct RowCheckE {
             const double dd = yv - double(yl[r]);
             p[(4 * q + 3) * kBlock] += dd * dd;
         }
+        double kdx = acc[1] - double(axl[r]);
+        if (kind[r]) kdx = fmax(kdx, 0.0);
+        p[8 * kBlock] += kdx * kdx;
+        const double dy = double(yc[r]) - double(yl[r]);
+        p[9 * kBlock] += br * dy;
+        if (kind[r]) p[10 * kBlock] += fmax(dy, 0.0) * fmax(dy, 0.0);
     }
 };
 
@@ -137,6 +144,7 @@ struct ColCheckE {
     const double* dc;
     float* atya;
     double inv_w;
+    const float* atyl;         // K^T y_last
     double* p;                 // this thread's slots
     struct Pre {};
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
@@ -156,6 +164,14 @@ struct ColCheckE {
             const double dd = xv - double(xl[j]);
             p[(5 * q + 4) * kBlock] += dd * dd;
         }
+        const double lr = -(acc[1] - double(atyl[j]));
+        const double lp = (hl && hh) ? lr : hl ? fmax(lr, 0.0) : hh ? fmin(lr, 0.0) : 0.0;
+        p[10 * kBlock] += (lr - lp) * (lr - lp);
+        p[11 * kBlock] += (hl ? l * fmax(lp, 0.0) : 0.0) + (hh ? h * fmin(lp, 0.0) : 0.0);
+        const double dx = double(xc[j]) - double(xl[j]);
+        const double vx = (hl && hh) ? dx : hl ? fmin(dx, 0.0) : hh ? fmax(dx, 0.0) : 0.0;
+        p[12 * kBlock] += vx * vx;
+        p[13 * kBlock] += cj * dx;
     }
 };
 
@@ -169,6 +185,7 @@ struct View {                 // one instance's arrays
     float *X[2], *ATY[2], *xs, *xl, *atya;
     float *Y[2], *AX[2], *ys, *yl, *axa;
     float *xb, *yb;
+    float *axl, *atyl;
 };
 
 __device__ __forceinline__ View make_view(const Args& A, const Inst& I, int G) {
@@ -186,6 +203,8 @@ __device__ __forceinline__ View make_view(const Args& A, const Inst& I, int G) {
     v.ys = a.ys + I.vr; v.yl = a.yl + I.vr; v.axa = a.axa + I.vr;
     v.xb = a.xb ? a.xb + I.vc : nullptr;
     v.yb = a.yb ? a.yb + I.vr : nullptr;
+    v.axl = a.axl + I.vr;
+    v.atyl = a.atyl + I.vc;
     return v;
 }
 
@@ -220,32 +239,33 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     const double inv_w = has_avg ? 1.0 / c.w_sum : 1.0;
     const int cur = c.cur;
     double* mine = slots + threadIdx.x;
-    for (int q = 0; q < 8; ++q) mine[q * kBlock] = 0.0;
+    for (int q = 0; q < kRowPartials; ++q) mine[q * kBlock] = 0.0;
     RowCheckE er{v.b, has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], v.yl, v.dr, v.kind, v.axa, inv_w,
-                 mine};
+                 v.axl, mine};
     group_rows_r<2, double>(v.Gr, v.rptr, v.ridx, v.rval, v.m,
                             Gather2{has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], inv_w, T.size > 1}, er,
                             T.rank, T.size);
-    slot_sums<8>(slots, sm);                       // sm[0..7]: row partials
-    for (int q = 0; q < 10; ++q) mine[q * kBlock] = 0.0;
+    slot_sums<kRowPartials>(slots, sm);            // sm[0..10]: row partials
+    for (int q = 0; q < kColPartials; ++q) mine[q * kBlock] = 0.0;
     ColCheckE ec{v.c, v.lo, v.hi, has_avg ? v.xs : v.X[cur], has_avg ? v.xl : nullptr, v.X[cur], v.xl, v.dc, v.atya,
-                 inv_w, mine};
+                 inv_w, v.atyl, mine};
     group_rows_dyn<2, double>(v.G, v.cptr, v.cidx, v.cval, v.n,
                               Gather2{has_avg ? v.ys : v.Y[cur], has_avg ? v.yl : nullptr, v.Y[cur], inv_w, T.size > 1}, ec,
                               T.rank, T.size);
-    slot_sums<10>(slots, sm + 8);                  // sm[8..17]: column partials
-    // team totals of the 18 partials and of the deadline test (any block past it stops all)
-    double tt[19];
+    slot_sums<kColPartials>(slots, sm + kRowPartials);   // then the column partials
+    // team totals of the partials and of the deadline test (any block past it stops all)
+    constexpr int NT = kRowPartials + kColPartials;
+    double tt[NT + 1];
     if (threadIdx.x == 0) {
-        for (int q = 0; q < 18; ++q) tt[q] = sm[q];
-        tt[18] = (deadline && global_ns() > deadline) ? 1.0 : 0.0;
+        for (int q = 0; q < NT; ++q) tt[q] = sm[q];
+        tt[NT] = (deadline && global_ns() > deadline) ? 1.0 : 0.0;
     }
-    if (!team_total<19>(tt, T)) return false;
+    if (!team_total<NT + 1>(tt, T)) return false;
     if (threadIdx.x == 0) {
-        double tr[kRowPartials] = {}, tc[kColPartials] = {};   // no infeasibility partials here
-        for (int q = 0; q < 8; ++q) tr[q] = tt[q];
-        for (int q = 0; q < 10; ++q) tc[q] = tt[8 + q];
-        decide_check(c, tc, tr, I.inv_nb, I.inv_nc, tt[18] > 0.0);
+        double tr[kRowPartials], tc[kColPartials];
+        for (int q = 0; q < kRowPartials; ++q) tr[q] = tt[q];
+        for (int q = 0; q < kColPartials; ++q) tc[q] = tt[kRowPartials + q];
+        decide_check(c, tc, tr, I.inv_nb, I.inv_nc, tt[NT] > 0.0);
     }
     __syncthreads();
     const int ap = c.apply;
@@ -265,7 +285,11 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
         } else {
             xv = v.X[cur][j];
         }
-        if (rst) { v.xl[j] = xv; v.xs[j] = 0.f; }
+        if (rst) {
+            v.xl[j] = xv;
+            v.xs[j] = 0.f;
+            v.atyl[j] = v.ATY[cur][j];
+        }
         if (cand) {
             const float x2 = fminf(fmaxf(xv - tau * (v.c[j] - v.ATY[cur][j]), v.lo[j]), v.hi[j]);
             v.X[1 - cur][j] = x2;
@@ -282,7 +306,11 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
         } else {
             yv = v.Y[cur][i];
         }
-        if (rst) { v.yl[i] = yv; v.ys[i] = 0.f; }
+        if (rst) {
+            v.yl[i] = yv;
+            v.ys[i] = 0.f;
+            v.axl[i] = v.AX[cur][i];
+        }
     }
     double t[1] = {double(dx2)};
     block_sum<1>(t, sm);
@@ -422,7 +450,7 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
 __global__ void __launch_bounds__(kBlock, 4) k_batch_solve(Args A, int G) {
     __shared__ Ctl c;
     __shared__ double sm[kWarps * 10];
-    __shared__ double slots[10 * kBlock];
+    __shared__ double slots[kColPartials * kBlock];
     __shared__ double xch[2 * kXch];
     __shared__ uint32_t counter;
     __shared__ int s_inst, s_err;
@@ -967,8 +995,9 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         SPB_CK(b->alloc(&b->d_cold_rel, count));
         SPB_CK(b->alloc(&b->d_team_error, 1));
         SPB_CK(cudaMemsetAsync(b->d_cold_rel, 0xFF, sizeof(double) * count, b->st));   // NaN = unknown
-        float *d_xb = nullptr, *d_yb = nullptr;
+        float *d_xb = nullptr, *d_yb = nullptr, *d_axl, *d_atyl;
         if (opt.escalate != 0) { SPB_CK(b->alloc(&d_xb, vc)); SPB_CK(b->alloc(&d_yb, vr)); }
+        SPB_CK(b->alloc(&d_axl, vr)); SPB_CK(b->alloc(&d_atyl, vc));
         double *t_rv, *t_cv, *t_c, *t_lo, *t_hi, *t_b;
         SPB_CK(cudaMalloc(&t_rv, sizeof(double) * std::max<int64_t>(NNZ, 1)));
         SPB_CK(cudaMalloc(&t_cv, sizeof(double) * std::max<int64_t>(NNZ, 1)));
@@ -996,7 +1025,8 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         a = sps::batch::Arrays{d_rptr, d_ridx, d_cptr, d_cidx, d_rval, d_cval, d_kind, d_c, d_lo, d_hi, d_b,
                                d_dc, d_dr, d_eta0, d_om0,
                                st_f[0], st_f[1], st_f[2], st_f[3], st_f[4], st_f[5], st_f[6],
-                               st_f[7], st_f[8], st_f[9], st_f[10], st_f[11], st_f[12], st_f[13], d_xb, d_yb};
+                               st_f[7], st_f[8], st_f[9], st_f[10], st_f[11], st_f[12], st_f[13], d_xb, d_yb,
+                               d_axl, d_atyl};
         if (opt.escalate == 1) {
             b->h_rptr = std::move(rptr);
             b->h_ridx = std::move(ridx);

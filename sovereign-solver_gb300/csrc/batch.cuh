@@ -34,6 +34,7 @@ struct Arrays {
     float *x0, *x1, *aty0, *aty1, *xs, *xl, *atya;
     float *y0, *y1, *ax0, *ax1, *ys, *yl, *axa;
     float *xb, *yb;           // best point of the stall test (null when it is off)
+    float *axl, *atyl;        // K x_last, K^T y_last (infeasibility tests)
 };
 
 struct Args {
@@ -64,7 +65,7 @@ struct Args {
 // The team barrier is a counter in rank 0's shared memory (release-add,
 // acquire-poll at cluster scope) with a bounded wait: a block that waits
 // longer than kTeamSpin polls (about a second) records an error and leaves.
-constexpr int kXch = 24;                  // doubles per exchange buffer
+constexpr int kXch = 32;                  // doubles per exchange buffer
 constexpr int32_t kTeamNnz = 65536;       // smallest size solved by a team
 constexpr uint32_t kTeamSpin = 1u << 21;
 

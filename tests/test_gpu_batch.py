@@ -128,3 +128,21 @@ def test_batch_time_limit():
         res = b.solve()
         assert b.stats.solve_ms < 5000
     assert sum(r.status == "time_limit" for r in res) >= 32
+
+
+def test_batch_detects_infeasible_and_unbounded():
+    import scipy.sparse as sp
+    inf = np.inf
+
+    def lp(c, A_ub, b_ub, lb, ub):
+        n = len(c)
+        return sps.Problem(c=np.asarray(c, float), A_ub=sp.csr_matrix(np.asarray(A_ub, float)),
+                           b_ub=np.asarray(b_ub, float), A_eq=sp.csr_matrix((0, n)), b_eq=np.zeros(0),
+                           lb=np.asarray(lb, float), ub=np.asarray(ub, float), integer_mask=np.zeros(n, bool))
+    probs = [wl.batch_planted_lp(7, m_range=(50, 200))[0],
+             lp([1, 1], [[1, 1], [-1, -1]], [1, -2], [0, 0], [inf, inf]),          # infeasible
+             lp([-1, 0], [[1, -1]], [1], [0, 0], [inf, inf]),                       # unbounded
+             wl.batch_planted_lp(8, m_range=(50, 200))[0]]
+    with sps.PDHGBatch(probs, tol=1e-6) as b:
+        res = b.solve()
+    assert [r.status for r in res] == ["optimal", "infeasible", "unbounded", "optimal"]
