@@ -13,6 +13,15 @@
 //   SEGMENT  longer rows, CSR, cut into 512-nonzero segments; one warp per
 //            segment; the last warp to finish a row (per-row ticket) adds the
 //            segment partials in segment order and runs the row's epilogue.
+//   SLAB     longer rows whose neighbours share their column pattern shifted by
+//            one (the k-th nonzeros of rows r and r+1 sit in adjacent columns:
+//            demand rows of a transportation LP, time-expanded flows), stored
+//            SELL-32 like SLICED and cut into units of 32 steps (1024 entries);
+//            lane t owns row t of the slice, so the gathers of a step are one
+//            128-byte line where CSR would touch 32 sectors.  The last warp to
+//            finish a slice (per-slice ticket) adds the units' partials in unit
+//            order and runs the slice's 32 epilogues.  The host picks SLAB per
+//            group of 32 rows when it touches at most half the sectors of CSR.
 //
 // Index arrays are int32, values V (float or double); every reduction is FP64
 // at block level.  Scale factors are FP64.
@@ -28,8 +37,9 @@ constexpr int kWarps = kBlock / 32;
 constexpr int kMaxBins = 8;
 constexpr int kSliceMax = 32;        // rows up to this length are SLICED
 constexpr int kSegment = 512;        // WARP rows up to this length; SEGMENT size above it
+constexpr int kSlabSteps = 32;       // steps (32-entry columns of a slice) per SLAB unit
 
-enum BinMode { BM_SLICED = 0, BM_WARP = 1, BM_SEGMENT = 2 };
+enum BinMode { BM_SLICED = 0, BM_WARP = 1, BM_SEGMENT = 2, BM_SLAB = 3 };
 
 // One contiguous range of internal rows (or columns) with one schedule.
 struct Bin {
@@ -38,9 +48,12 @@ struct Bin {
     int32_t kind;            // row pass: 1 = '<=' rows, 0 = '=' rows; column pass: 0
     int32_t block_begin;     // first block of this bin in a launch
     int32_t nblocks;
-    int32_t units;           // slices (SLICED), rows (WARP) or segments (SEGMENT)
-    int32_t aux;             // SLICED: first global slice; SEGMENT: first global segment
-    int32_t aux2;            // SEGMENT: first per-row ticket index
+    int32_t units;           // slices (SLICED), rows (WARP), segments (SEGMENT) or units (SLAB)
+    int32_t aux;             // SLICED: first global slice; SEGMENT / SLAB: first global unit
+    int32_t aux2;            // SEGMENT: first per-row ticket; SLAB: first per-slice ticket
+    int32_t slice0;          // SLAB: first global slice
+    int32_t part0;           // SLAB: first unit in the layout's SLAB partials
+    int32_t slot0;           // SEGMENT / SLAB: first row slot of epilogue partials
 };
 
 struct BinTable {
@@ -55,12 +68,13 @@ struct Layout {
     const int32_t* idx;
     const V* val;
     const int32_t* soff;     // slice offsets (slices + 1)
-    const int32_t* seg_row;  // internal row of each segment
-    const int32_t* seg_k;    // segment number inside its row
+    const int32_t* seg_row;  // internal row of each segment (SLAB: slice inside its bin)
+    const int32_t* seg_k;    // segment number inside its row (SLAB: unit inside its slice)
     double* seg_part;        // per-segment partial sums (2 doubles of room each)
+    double* slab_part;       // per SLAB unit: 32 lanes' partial sums (64 doubles of room each)
     uint32_t* seg_ticket;    // per-row tickets of SEGMENT rows (left at 0 after every pass)
-    double* seg_rowpart;     // per SEGMENT row: its epilogue's reduction partials (room for 10)
-    int32_t nsegrows;        // SEGMENT rows of this orientation
+    double* seg_rowpart;     // per SEGMENT / SLAB row: its epilogue's reduction partials
+    int32_t nsegrows;        // SEGMENT and SLAB rows (slots) of this orientation
 };
 
 constexpr int kMaxEpiPartials = 14;
@@ -118,9 +132,12 @@ __device__ __forceinline__ T group_sum(T v) {
     return v;
 }
 
-// Sum NP doubles over the block; result valid in thread 0.  Fixed order.
-template <int NP>
-__device__ __forceinline__ void block_sum(double (&v)[NP], double* smem /* kWarps*NP */) {
+// Sum NP values over the block; result valid in thread 0.  Fixed order.  T is
+// float in the FP32 engine's iteration kernels: this GPU issues FP64 at 1/64 of
+// the FP32 rate (2 thread operations per SM cycle), so a 256-thread FP64 shuffle
+// tree per block and per attempt costs more than the block's own FP32 work.
+template <int NP, class T>
+__device__ __forceinline__ void block_sum(T (&v)[NP], T* smem /* kWarps*NP */) {
 #pragma unroll
     for (int p = 0; p < NP; ++p) v[p] = group_sum<32>(v[p]);
     const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -133,7 +150,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NP], double* smem /* kWarp
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int p = 0; p < NP; ++p) {
-            double s = 0.0;
+            T s = T(0);
             for (int q = 0; q < kWarps; ++q) s += smem[q * NP + p];
             v[p] = s;
         }
@@ -143,9 +160,9 @@ __device__ __forceinline__ void block_sum(double (&v)[NP], double* smem /* kWarp
 
 // Write this block's NP partials, then report whether this block is the last
 // one of the grid to finish (ticket counter; no waiting).
-template <int NP>
-__device__ __forceinline__ bool publish_partials(double (&v)[NP], double* partials, uint32_t* ticket,
-                                                 double* smem, bool* am_last) {
+template <int NP, class T>
+__device__ __forceinline__ bool publish_partials(T (&v)[NP], T* partials, uint32_t* ticket,
+                                                 T* smem, bool* am_last) {
     block_sum<NP>(v, smem);
     if (threadIdx.x == 0) {
 #pragma unroll
@@ -158,18 +175,38 @@ __device__ __forceinline__ bool publish_partials(double (&v)[NP], double* partia
     return *am_last;
 }
 
-// In the last block: sum the partials of all nblk blocks (fixed order).
-template <int NP>
-__device__ __forceinline__ void gather_partials(double (&tot)[NP], const double* partials, int nblk,
-                                                double* smem) {
+// In the last block: sum the partials of all nblk blocks (fixed order; each
+// thread's loads are issued before its adds).
+template <int NP, class T>
+__device__ __forceinline__ void gather_partials(T (&tot)[NP], const T* partials, int nblk, T* smem) {
     __threadfence();
+    constexpr int B = 4;
 #pragma unroll
-    for (int p = 0; p < NP; ++p) tot[p] = 0.0;
-    for (int b = threadIdx.x; b < nblk; b += kBlock) {
+    for (int p = 0; p < NP; ++p) tot[p] = T(0);
+    for (int b0 = threadIdx.x; b0 < nblk; b0 += kBlock * B) {
+        T v[B][NP];
 #pragma unroll
-        for (int p = 0; p < NP; ++p) tot[p] += __ldcg(partials + (size_t)b * NP + p);
+        for (int u = 0; u < B; ++u) {
+            const int b = b0 + u * kBlock;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) v[u][p] = b < nblk ? __ldcg(partials + (size_t)b * NP + p) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) tot[p] += v[u][p];
     }
     block_sum<NP>(tot, smem);
+}
+
+// A value every thread of the block needs, computed once by thread 0 (FP64
+// divisions and products per thread would occupy the slow FP64 pipe).
+template <class T, class F>
+__device__ __forceinline__ T block_scalar(F f) {
+    __shared__ T s;
+    if (threadIdx.x == 0) s = T(f());
+    __syncthreads();
+    return s;
 }
 
 __device__ __forceinline__ uint64_t global_ns() {
@@ -369,32 +406,35 @@ __device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, in
     if constexpr (Epi::NP == 0) {
         e(r, b.kind, tot, pre);
     } else {
+        using R = typename Epi::R;
         // Which warp finishes a row last varies between runs: the row's share of
         // the kernel's reductions goes to its own slot, summed in row order by
         // the kernel's last block, so every run adds the same numbers in the same order.
         Epi one = e;
         one.zero();
         one(r, b.kind, tot, pre);
-        one.export_to(L.seg_rowpart + (size_t)(b.aux2 + (r - b.begin)) * Epi::NP);
+        one.export_to(reinterpret_cast<R*>(L.seg_rowpart) + (size_t)(b.slot0 + (r - b.begin)) * Epi::NP);
     }
 }
 
-// In a kernel's last block: add the SEGMENT rows' epilogue partials, in row order.
-template <int NP, class V>
-__device__ __forceinline__ void add_segment_rows(double (&tot)[NP], const Layout<V>& L, double* smem) {
+// In a kernel's last block: add the SEGMENT and SLAB rows' epilogue partials, in
+// slot order.
+template <int NP, class T, class V>
+__device__ __forceinline__ void add_segment_rows(T (&tot)[NP], const Layout<V>& L, T* smem) {
     // B rows' loads are issued before their adds: B round trips overlap instead
     // of one L2 round trip per row (fixed order, so the sum stays deterministic)
     constexpr int B = NP <= 2 ? 8 : 2;
-    double s[NP];
+    const T* part = reinterpret_cast<const T*>(L.seg_rowpart);
+    T s[NP];
 #pragma unroll
-    for (int p = 0; p < NP; ++p) s[p] = 0.0;
+    for (int p = 0; p < NP; ++p) s[p] = T(0);
     for (int k0 = threadIdx.x; k0 < L.nsegrows; k0 += kBlock * B) {
-        double v[B][NP];
+        T v[B][NP];
 #pragma unroll
         for (int u = 0; u < B; ++u) {
             const int k = k0 + u * kBlock;
 #pragma unroll
-            for (int p = 0; p < NP; ++p) v[u][p] = k < L.nsegrows ? __ldcg(L.seg_rowpart + (size_t)k * NP + p) : 0.0;
+            for (int p = 0; p < NP; ++p) v[u][p] = k < L.nsegrows ? __ldcg(part + (size_t)k * NP + p) : T(0);
         }
 #pragma unroll
         for (int u = 0; u < B; ++u)
@@ -405,6 +445,71 @@ __device__ __forceinline__ void add_segment_rows(double (&tot)[NP], const Layout
     if (threadIdx.x == 0)
 #pragma unroll
         for (int p = 0; p < NP; ++p) tot[p] += s[p];
+}
+
+// SLAB: unit u of the bin = steps [c S, min(L, (c+1) S)) of slice s (S =
+// kSlabSteps, L = the slice's padded length); lane t accumulates row t of the
+// slice.  A slice with more than one unit is finished by the unit that takes
+// the slice's ticket last: it adds the units' partials in unit order.  Every
+// row's epilogue partials go to its own slot (units finish in varying order).
+template <int NV, class Acc, class V, class Gather, class Epi>
+__device__ __forceinline__ void visit_slab_unit(const Bin& b, int u, const Layout<V>& L, const Gather& g, Epi& e) {
+    const int lane = threadIdx.x & 31;
+    const int s = __ldg(L.seg_row + b.aux + u), c = __ldg(L.seg_k + b.aux + u);
+    const int off = __ldg(L.soff + b.slice0 + s);
+    const int len = (__ldg(L.soff + b.slice0 + s + 1) - off) >> 5;
+    const int k0 = c * kSlabSteps, k1 = min(len, k0 + kSlabSteps);
+    Acc acc[NV];
+#pragma unroll
+    for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
+    for (int k = k0; k < k1; k += kUnroll) {
+        int j[kUnroll];
+        Acc a[kUnroll];
+#pragma unroll
+        for (int w = 0; w < kUnroll; ++w) {
+            const bool ok = k + w < k1;
+            const int p = off + 32 * (k + w) + lane;
+            j[w] = ok ? __ldg(L.idx + p) : 0;
+            a[w] = ok ? Acc(__ldg(L.val + p)) : Acc(0);
+        }
+#pragma unroll
+        for (int w = 0; w < kUnroll; ++w)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) acc[q] += a[w] * g(q, j[w]);
+    }
+    const int nunits = (len + kSlabSteps - 1) / kSlabSteps;
+    if (nunits > 1) {
+        Acc* part = reinterpret_cast<Acc*>(L.slab_part) + (size_t)(b.part0 + u) * 32 * NV;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) part[lane * NV + q] = acc[q];
+        __threadfence();
+        __syncwarp();
+        uint32_t t = 0;
+        uint32_t* tk = L.seg_ticket + b.aux2 + s;
+        if (lane == 0) t = atomicAdd(tk, 1u);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t != (uint32_t)(nunits - 1)) return;
+        __threadfence();
+        if (lane == 0) *tk = 0u;
+        const Acc* first = reinterpret_cast<const Acc*>(L.slab_part) + (size_t)(b.part0 + u - c) * 32 * NV;
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
+        for (int w = 0; w < nunits; ++w)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) acc[q] += __ldcg(first + (size_t)w * 32 * NV + lane * NV + q);
+    }
+    const int r = b.begin + 32 * s + lane;
+    if (r >= b.end) return;
+    typename Epi::Pre pre = e.pre(r);
+    if constexpr (Epi::NP == 0) {
+        e(r, b.kind, acc, pre);
+    } else {
+        using R = typename Epi::R;
+        Epi one = e;
+        one.zero();
+        one(r, b.kind, acc, pre);
+        one.export_to(reinterpret_cast<R*>(L.seg_rowpart) + (size_t)(b.slot0 + (r - b.begin)) * Epi::NP);
+    }
 }
 
 // Dispatch: find this block's bin; each warp walks the bin's units with a
@@ -425,8 +530,10 @@ __device__ __forceinline__ void visit_bins(const BinTable& bt, int block, const 
         for (int u = w0; u < b.units; u += 2 * stride) visit_slice_pair<NV, Acc>(b, u, u + stride, L, g, e);
     } else if (b.mode == BM_WARP) {
         for (int u = w0; u < b.units; u += 2 * stride) visit_warp_row_pair<NV, Acc>(b, u, u + stride, L, g, e);
-    } else {
+    } else if (b.mode == BM_SEGMENT) {
         for (int u = w0; u < b.units; u += 2 * stride) visit_segment_pair<NV, Acc>(b, u, u + stride, L, g, e);
+    } else {
+        for (int u = w0; u < b.units; u += stride) visit_slab_unit<NV, Acc>(b, u, L, g, e);
     }
 }
 

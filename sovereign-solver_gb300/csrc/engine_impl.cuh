@@ -124,27 +124,94 @@ struct Engine : EngineBase {
         std::vector<int32_t> soff;      // slice offsets, one sentinel after each SLICED bin
         std::vector<int32_t> seg_row, seg_k;
         int64_t total = 0;              // final index/value array length (with slice padding)
-        int32_t ntickets = 0;
+        int32_t ntickets = 0;           // SEGMENT rows and SLAB slices
+        int32_t nslots = 0;             // SEGMENT and SLAB rows (epilogue partial slots)
+        int32_t nslab_units = 0;
     };
 
     // Blocks that give every warp of the bin work for its first step (warps
-    // take two units per step).
-    static int64_t blocks_needed(const Bin& b) { return (b.units + 2 * kWarps - 1) / (2 * kWarps); }
+    // take two units per step, one in SLAB bins).
+    static int64_t blocks_needed(const Bin& b) {
+        const int per = b.mode == BM_SLAB ? kWarps : 2 * kWarps;
+        return (b.units + per - 1) / per;
+    }
 
-    static int mode_of(int64_t len) {
-        return len <= kSliceMax ? BM_SLICED : (len <= kSegment ? BM_WARP : BM_SEGMENT);
+    static int mode_of(int64_t len, bool slab) {
+        return len <= kSliceMax ? BM_SLICED : slab ? BM_SLAB : (len <= kSegment ? BM_WARP : BM_SEGMENT);
+    }
+
+    // SLAB choice per group of 32 consecutive long rows of one kind (original
+    // order), from the 32-byte sectors of the gathered vector that a warp
+    // touches, sampled at up to 32 steps of the group: CSR (a warp reads 32
+    // consecutive nonzeros of one row: a new sector where the column leaves the
+    // previous one's) against SLAB (a warp reads the k-th nonzero of the 32 rows:
+    // the distinct sectors in lane order), plus SLAB's padded entries (index and
+    // value reads).  SLAB when it needs at most half of CSR's sectors.  Columns
+    // in internal numbering (inv_col).
+    static std::vector<uint8_t> choose_slab(const HostProblem& hp, const std::vector<int32_t>& inv_col,
+                                            int elem_bytes) {
+        const int m = hp.m;
+        std::vector<uint8_t> slab(m, 0);
+        std::vector<int64_t> seg_end;
+        int64_t acc = 0;
+        for (const auto& sg : hp.segs) { acc += sg.cnt; seg_end.push_back(acc); }
+        auto col = [&](int64_t k) -> int32_t {
+            size_t q = 0;
+            while (q + 1 < seg_end.size() && k >= seg_end[q]) ++q;
+            const int64_t base = q ? seg_end[q - 1] : 0;
+            return inv_col[hp.segs[q].idx[k - base]];
+        };
+        const int sh = elem_bytes == 4 ? 3 : 2;        // log2(elements per 32-byte sector)
+        for (int kd = 0; kd < 2; ++kd) {
+            std::vector<int32_t> rows;
+            for (int i = 0; i < m; ++i)
+                if (hp.kind[i] == kd && hp.ptr[i + 1] - hp.ptr[i] > kSliceMax) rows.push_back(i);
+            for (size_t g = 0; g < rows.size(); g += 32) {
+                const int cnt = (int)std::min<size_t>(32, rows.size() - g);
+                int64_t lmin = INT64_MAX, lmax = 0, stored = 0;
+                for (int t = 0; t < cnt; ++t) {
+                    const int64_t len = hp.ptr[rows[g + t] + 1] - hp.ptr[rows[g + t]];
+                    lmin = std::min(lmin, len);
+                    lmax = std::max(lmax, len);
+                    stored += len;
+                }
+                const int ns = (int)std::min<int64_t>(32, lmin - 1);
+                double csr = 0.0, sl = 0.0;
+                for (int q = 0; q < ns; ++q) {
+                    const int64_t k = 1 + (lmin - 1) * q / ns;
+                    int32_t prev = -1;
+                    for (int t = 0; t < cnt; ++t) {
+                        const int64_t base = hp.ptr[rows[g + t]];
+                        const int32_t a = col(base + k) >> sh, a0 = col(base + k - 1) >> sh;
+                        csr += a != a0;
+                        sl += a != prev;
+                        prev = a;
+                    }
+                }
+                const double per = 1.0 / (double(ns) * cnt);
+                const double csr_cost = csr * per * double(stored);
+                const double slab_cost = sl * per * double(stored) +
+                                         double(32 * lmax - stored) * (4.0 + elem_bytes) / 32.0;
+                if (slab_cost <= 0.5 * csr_cost)
+                    for (int t = 0; t < cnt; ++t) slab[rows[g + t]] = 1;
+            }
+        }
+        return slab;
     }
 
     // Order: per kind, SLICED rows by decreasing length, then WARP rows, then
-    // SEGMENT rows (stable counting sort); one bin per (kind, schedule).
-    static void make_plan(const std::vector<int64_t>& lens, const std::vector<int8_t>* kinds, Plan& P,
-                          int block_cap) {
+    // SEGMENT rows, then SLAB rows (stable counting sort); one bin per (kind,
+    // schedule).
+    static void make_plan(const std::vector<int64_t>& lens, const std::vector<int8_t>* kinds,
+                          const std::vector<uint8_t>* slab, Plan& P, int block_cap) {
         const int R = (int)lens.size();
-        constexpr int NB = kSliceMax + 3;
+        constexpr int NB = kSliceMax + 4;
         auto kind_of = [&](int i) { return kinds ? (int)(*kinds)[i] : 0; };
+        auto mode_at = [&](int i) { return mode_of(lens[i], slab && (*slab)[i]); };
         auto bucket = [&](int i) {
-            const int md = mode_of(lens[i]);
-            const int sub = md == BM_SLICED ? (int)(kSliceMax - lens[i]) : (md == BM_WARP ? kSliceMax + 1 : kSliceMax + 2);
+            const int md = mode_at(i);
+            const int sub = md == BM_SLICED ? (int)(kSliceMax - lens[i])
+                                            : kSliceMax + (md == BM_WARP ? 1 : md == BM_SEGMENT ? 2 : 3);
             return kind_of(i) * NB + sub;
         };
         std::vector<int64_t> cnt(2 * NB + 1, 0);
@@ -160,9 +227,9 @@ struct Engine : EngineBase {
         int64_t off = 0;
         std::vector<int64_t> bin_store;              // stored entries per bin
         for (int r = 0; r < R;) {
-            const int kd = kind_of(P.perm[r]), md = mode_of(lens[P.perm[r]]);
+            const int kd = kind_of(P.perm[r]), md = mode_at(P.perm[r]);
             int e = r;
-            while (e < R && kind_of(P.perm[e]) == kd && mode_of(lens[P.perm[e]]) == md) ++e;
+            while (e < R && kind_of(P.perm[e]) == kd && mode_at(P.perm[e]) == md) ++e;
             Bin b{};
             b.begin = r;
             b.end = e;
@@ -181,9 +248,10 @@ struct Engine : EngineBase {
             } else if (md == BM_WARP) {
                 for (int q = r; q < e; ++q) { P.fptr[q] = (int32_t)off; off += lens[P.perm[q]]; }
                 b.units = e - r;
-            } else {
+            } else if (md == BM_SEGMENT) {
                 b.aux = (int32_t)P.seg_row.size();
                 b.aux2 = P.ntickets;
+                b.slot0 = P.nslots;
                 for (int q = r; q < e; ++q) {
                     P.fptr[q] = (int32_t)off;
                     const int64_t ns = (lens[P.perm[q]] + kSegment - 1) / kSegment;
@@ -192,6 +260,30 @@ struct Engine : EngineBase {
                 }
                 b.units = (int32_t)P.seg_row.size() - b.aux;
                 P.ntickets += e - r;
+                P.nslots += e - r;
+            } else {
+                // SLAB: slices of 32 rows padded to their longest row, one unit per
+                // kSlabSteps steps of a slice (units of one slice consecutive)
+                b.aux = (int32_t)P.seg_row.size();
+                b.slice0 = (int32_t)P.soff.size();
+                b.aux2 = P.ntickets;
+                b.slot0 = P.nslots;
+                b.part0 = P.nslab_units;
+                for (int q = r; q < e; ++q) P.fptr[q] = (int32_t)off;
+                int32_t s = 0;
+                for (int q = r; q < e; q += 32, ++s) {
+                    int64_t lmax = 0;
+                    for (int t = q; t < std::min(e, q + 32); ++t) lmax = std::max(lmax, lens[P.perm[t]]);
+                    P.soff.push_back((int32_t)off);
+                    off += 32 * lmax;
+                    const int64_t nu = (lmax + kSlabSteps - 1) / kSlabSteps;
+                    for (int64_t c = 0; c < nu; ++c) { P.seg_row.push_back(s); P.seg_k.push_back((int32_t)c); }
+                }
+                P.soff.push_back((int32_t)off);           // sentinel: end of the bin's last slice
+                b.units = (int32_t)P.seg_row.size() - b.aux;
+                P.ntickets += s;
+                P.nslots += e - r;
+                P.nslab_units += b.units;
             }
             bin_store.push_back(off - bin_off0);
             P.bt.bin[P.bt.nbins++] = b;
@@ -240,7 +332,11 @@ struct Engine : EngineBase {
             if (b.mode == BM_SLICED)
                 k_fill_sliced<V><<<grid_for((int64_t)b.units * 32), kBlock, 0, st>>>(
                     tptr, tidx, tval, d_soff, b.begin, b.end, b.aux, b.units, d_idx, d_val);
-            else
+            else if (b.mode == BM_SLAB) {
+                const int nsl = (b.end - b.begin + 31) / 32;
+                k_fill_sliced<V><<<grid_for((int64_t)nsl * 32), kBlock, 0, st>>>(
+                    tptr, tidx, tval, d_soff, b.begin, b.end, b.slice0, nsl, d_idx, d_val);
+            } else
                 k_fill_rows<V><<<grid_for((int64_t)(b.end - b.begin) * 32), kBlock, 0, st>>>(
                     tptr, tidx, tval, d_fptr, b.begin, b.end, d_idx, d_val);
         }
@@ -274,12 +370,8 @@ struct Engine : EngineBase {
         SPS_CK(cudaEventRecord(ev0, st));
         const int block_cap = opt.max_blocks > 0 ? opt.max_blocks : kSms * kPassMinBlocks;   // one resident wave
 
-        // ---- row plan (host): schedule bins by row kind and length
         std::vector<int64_t> rlen(m);
         for (int i = 0; i < m; ++i) rlen[i] = hp.ptr[i + 1] - hp.ptr[i];
-        Plan rp;
-        make_plan(rlen, &hp.kind, rp, block_cap);
-        const std::vector<int32_t>& perm_row = rp.perm;
 
         // ---- staging upload and validation
         int32_t *s_ptr, *s_idx, *s_colcount, *s_err;
@@ -318,14 +410,22 @@ struct Engine : EngineBase {
         std::vector<int64_t> clen(n);
         for (int j = 0; j < n; ++j) clen[j] = colcount[j];
         Plan cp;
-        make_plan(clen, nullptr, cp, block_cap);
+        make_plan(clen, nullptr, nullptr, cp, block_cap);
         const std::vector<int32_t>& perm_col = cp.perm;
+        std::vector<int32_t> inv_col(n);
+        for (int j = 0; j < n; ++j) inv_col[perm_col[j]] = j;
+
+        // ---- row plan: bins by row kind, length and gather locality (SLAB groups)
+        Plan rp;
+        {
+            const std::vector<uint8_t> slab = choose_slab(hp, inv_col, (int)sizeof(V));
+            make_plan(rlen, &hp.kind, &slab, rp, block_cap);
+        }
+        const std::vector<int32_t>& perm_row = rp.perm;
         if (rp.total > INT32_MAX || cp.total > INT32_MAX) {
             cudaFreeAsync(s_ptr, st); cudaFreeAsync(s_idx, st); cudaFreeAsync(s_val, st); cudaFreeAsync(s_colcount, st); cudaFreeAsync(s_err, st);
             return fail(SPS_ERR_INVALID, "padded matrix layout exceeds 2^31-1 entries");
         }
-        std::vector<int32_t> inv_col(n);
-        for (int j = 0; j < n; ++j) inv_col[perm_col[j]] = j;
         std::vector<int32_t> nptr(m + 1, 0), cptr(n + 1, 0);
         for (int r = 0; r < m; ++r) nptr[r + 1] = nptr[r] + (int32_t)rlen[perm_row[r]];
         for (int j = 0; j < n; ++j) cptr[j + 1] = cptr[j] + colcount[perm_col[j]];
@@ -338,11 +438,12 @@ struct Engine : EngineBase {
         const size_t part_aux_n = (size_t)std::max(apply_blocks, kSms * 16) * 3;
         const size_t nseg = std::max<size_t>(std::max(rp.seg_row.size(), cp.seg_row.size()), 1);
         const size_t ntk = (size_t)std::max(std::max(rp.ntickets, cp.ntickets), 1);
+        const size_t nslab = (size_t)std::max(std::max(rp.nslab_units, cp.nslab_units), 1);
         const bool adaptive = mode == SPS_MODE_ADAPTIVE;
         std::vector<std::pair<void**, size_t>> plan;
         int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx, *d_rsoff, *d_csoff, *d_rseg, *d_rsegk, *d_cseg, *d_csegk;
         V *d_rval, *d_cval, *d_c, *d_b, *d_lo = nullptr, *d_hi = nullptr, *d_tau = nullptr, *d_sigma = nullptr;
-        double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa, *d_segpart, *d_rowpart_r, *d_rowpart_c;
+        double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa, *d_segpart, *d_slabpart, *d_rowpart_r, *d_rowpart_c;
         double *d_idr = nullptr, *d_idc = nullptr;
         uint32_t* d_tickets;
         V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
@@ -370,9 +471,10 @@ struct Engine : EngineBase {
         add(&d_cseg, sizeof(int32_t) * (cp.seg_row.size() + 1));
         add(&d_csegk, sizeof(int32_t) * (cp.seg_row.size() + 1));
         add(&d_segpart, sizeof(double) * 2 * nseg);
+        add(&d_slabpart, sizeof(double) * 64 * nslab);
         add(&d_tickets, sizeof(uint32_t) * ntk);
-        add(&d_rowpart_r, sizeof(double) * kMaxEpiPartials * std::max(rp.ntickets, 1));
-        add(&d_rowpart_c, sizeof(double) * kMaxEpiPartials * std::max(cp.ntickets, 1));
+        add(&d_rowpart_r, sizeof(double) * kMaxEpiPartials * std::max(rp.nslots, 1));
+        add(&d_rowpart_c, sizeof(double) * kMaxEpiPartials * std::max(cp.nslots, 1));
         add(&d_perm_row, sizeof(int32_t) * m);
         add(&d_perm_col, sizeof(int32_t) * n);
         add(&d_rkind, m);
@@ -507,11 +609,12 @@ struct Engine : EngineBase {
         if (int rc = build_layout(rp, m, t_ptr, t_idx, t_rvV, Lr, d_rptr, d_rsoff, d_rseg, d_rsegk, d_ridx, d_rval)) return rc;
         if (int rc = build_layout(cp, n, t_cptr, t_cidx, t_cvV, Lc, d_cptr, d_csoff, d_cseg, d_csegk, d_cidx, d_cval)) return rc;
         Lr.seg_part = Lc.seg_part = d_segpart;
+        Lr.slab_part = Lc.slab_part = d_slabpart;
         Lr.seg_ticket = Lc.seg_ticket = d_tickets;
         Lr.seg_rowpart = d_rowpart_r;
         Lc.seg_rowpart = d_rowpart_c;
-        Lr.nsegrows = rp.ntickets;
-        Lc.nsegrows = cp.ntickets;
+        Lr.nsegrows = rp.nslots;
+        Lc.nsegrows = cp.nslots;
 
         // ---- vectors in internal order
         {

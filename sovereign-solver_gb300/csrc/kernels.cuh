@@ -107,8 +107,9 @@ struct AdRowStepEpi {
     V dy2 = V(0), inter = V(0);          // per-thread partials; FP64 from the block sum on
     struct Pre { V ao, yv, br; };
     static constexpr int NP = 2;
+    using R = V;
     __device__ __forceinline__ void zero() { dy2 = inter = V(0); }
-    __device__ __forceinline__ void export_to(double* d) const { d[0] = double(dy2); d[1] = double(inter); }
+    __device__ __forceinline__ void export_to(R* d) const { d[0] = dy2; d[1] = inter; }
     __device__ __forceinline__ Pre pre(int r) const { return Pre{axo[r], yo[r], b[r]}; }
     __device__ __forceinline__ void operator()(int r, int kind, const V (&acc)[1], const Pre& p) {
         const V ax = acc[0];
@@ -126,19 +127,22 @@ template <class V>
 SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
-    __shared__ double sm[kWarps * 4];
+    __shared__ V sm[kWarps * 2];
     __shared__ bool last;
     const int cur = ctl->cur;
-    AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], V(ctl->eta * ctl->omega)};
+    const V sigma = block_scalar<V>([&] { return ctl->eta * ctl->omega; });
+    AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], sigma};
     visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e);
-    double v[2] = {double(e.dy2), double(e.inter)};
-    if (!publish_partials<2>(v, a.part_row, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
-    double t[2];
-    gather_partials<2>(t, a.part_row, gridDim.x, sm);
+    // reductions in V: FP32 sums in the FP32 engine (the step rule's inputs)
+    V v[2] = {e.dy2, e.inter};
+    V* part = reinterpret_cast<V*>(a.part_row);
+    if (!publish_partials<2>(v, part, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
+    V t[2];
+    gather_partials<2>(t, part, gridDim.x, sm);
     add_segment_rows<2>(t, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_ROW_STEP] = 0;
-    decide_step(*ctl, t[0], t[1]);
+    decide_step(*ctl, double(t[0]), double(t[1]));
 }
 
 template <class V>
@@ -152,8 +156,9 @@ struct AdColStepEpi {
     V dx2 = V(0);
     struct Pre { V xj, cj, lo, hi, s, l; };
     static constexpr int NP = 1;
+    using R = V;
     __device__ __forceinline__ void zero() { dx2 = V(0); }
-    __device__ __forceinline__ void export_to(double* d) const { d[0] = double(dx2); }
+    __device__ __forceinline__ void export_to(R* d) const { d[0] = dx2; }
     __device__ __forceinline__ Pre pre(int j) const {
         Pre p;
         p.xj = xc[j];
@@ -178,12 +183,13 @@ template <class V>
 SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->apply != AP_STEP_PENDING) return;
-    __shared__ double sm[kWarps * 2];
+    __shared__ V sm[kWarps];
     __shared__ bool last;
     const int cur = ctl->cur;
     const bool acc = ctl->accepted;
-    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.xl, a.ATY[cur], a.X[1 - cur], a.xs,
-                      V(ctl->eta / ctl->omega), V(ctl->eta_used), acc};
+    const V tau = block_scalar<V>([&] { return ctl->eta / ctl->omega; });
+    const V wgt = block_scalar<V>([&] { return ctl->eta_used; });
+    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.xl, a.ATY[cur], a.X[1 - cur], a.xs, tau, wgt, acc};
     const int colblocks = a.cols.total_blocks;
     if ((int)blockIdx.x < colblocks) {
         if (acc) {
@@ -193,19 +199,19 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
                 e.finish(j, e.atyo[j], e.pre(j));
         }
     } else if (acc) {
-        const V wgt = V(ctl->eta_used);
         const V* yc = a.Y[cur];
         for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
             a.ys[i] += wgt * (yc[i] - a.yl[i]);
     }
-    double v[1] = {double(e.dx2)};
-    if (!publish_partials<1>(v, a.part_col, &ctl->ticket[T_COL_STEP], sm, &last)) return;
-    double t[1];
-    gather_partials<1>(t, a.part_col, gridDim.x, sm);
+    V v[1] = {e.dx2};
+    V* part = reinterpret_cast<V*>(a.part_col);
+    if (!publish_partials<1>(v, part, &ctl->ticket[T_COL_STEP], sm, &last)) return;
+    V t[1];
+    gather_partials<1>(t, part, gridDim.x, sm);
     add_segment_rows<1>(t, a.csc, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_STEP] = 0;
-    ctl->dx2 = t[0];
+    ctl->dx2 = double(t[0]);
     ctl->apply = 0;
 }
 
@@ -243,6 +249,7 @@ struct AdRowCheckEpi {
     double p[kRowPartials] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     using Pre = NoPre;
     static constexpr int NP = kRowPartials;
+    using R = double;
     __device__ __forceinline__ void zero() { for (int q = 0; q < NP; ++q) p[q] = 0.0; }
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
@@ -299,6 +306,7 @@ struct AdColCheckEpi {
     double p[kColPartials] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     using Pre = NoPre;
     static constexpr int NP = kColPartials;
+    using R = double;
     __device__ __forceinline__ void zero() { for (int q = 0; q < NP; ++q) p[q] = 0.0; }
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
@@ -359,14 +367,14 @@ template <class V>
 __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
     Ctl* ctl = a.ctl;
     const int ap = ctl->apply;
-    __shared__ double sm[kWarps];
+    __shared__ V sm[kWarps];
     __shared__ bool last;
     if (ap != 0 && ap != AP_STEP_PENDING) {
         const int cur = ctl->cur;
         const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !ctl->done;
         const bool save = (ap & AP_SAVE_BEST) && a.xb, save_avg = ap & AP_SAVE_AVG;
-        const double inv_w = ctl->w_sum > 0.0 ? 1.0 / ctl->w_sum : 0.0;
-        const V tau = V(ctl->eta / ctl->omega);
+        const double inv_w = block_scalar<double>([&] { return ctl->w_sum > 0.0 ? 1.0 / ctl->w_sum : 0.0; });
+        const V tau = block_scalar<V>([&] { return ctl->eta / ctl->omega; });
         V dx2 = V(0);
         const int stride = gridDim.x * kBlock;
         for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += stride) {
@@ -407,13 +415,14 @@ __global__ void __launch_bounds__(kBlock) ad_apply(Args<V> a) {
                 a.AXl[i] = a.AX[cur][i];
             }
         }
-        double v[1] = {double(dx2)};
-        if (publish_partials<1>(v, a.part_aux, &ctl->ticket[T_APPLY], sm, &last)) {
-            double t[1];
-            gather_partials<1>(t, a.part_aux, gridDim.x, sm);
+        V v[1] = {dx2};
+        V* part = reinterpret_cast<V*>(a.part_aux);
+        if (publish_partials<1>(v, part, &ctl->ticket[T_APPLY], sm, &last)) {
+            V t[1];
+            gather_partials<1>(t, part, gridDim.x, sm);
             if (threadIdx.x == 0) {
                 ctl->ticket[T_APPLY] = 0;
-                if (cand) ctl->dx2 = t[0];
+                if (cand) ctl->dx2 = double(t[0]);
                 if (rst) ctl->w_sum = 0.0;
                 ctl->apply = 0;
                 set_loop_condition(a, ctl);
@@ -529,6 +538,7 @@ struct RfRowCheckEpi {
     double p[2] = {0, 0};     // ||A x - b||^2, b^T y
     using Pre = NoPre;
     static constexpr int NP = 2;
+    using R = double;
     __device__ __forceinline__ void zero() { p[0] = p[1] = 0.0; }
     __device__ __forceinline__ void export_to(double* d) const { d[0] = p[0]; d[1] = p[1]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
@@ -567,6 +577,7 @@ struct RfColCheckEpi {
     double p[2] = {0, 0};     // ||min(c - A^T y, 0)||^2, c^T x
     using Pre = NoPre;
     static constexpr int NP = 2;
+    using R = double;
     __device__ __forceinline__ void zero() { p[0] = p[1] = 0.0; }
     __device__ __forceinline__ void export_to(double* d) const { d[0] = p[0]; d[1] = p[1]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
