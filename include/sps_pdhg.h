@@ -96,9 +96,12 @@ typedef struct {
                                  the cold start's (x = clip(0, lb, ub), y = 0) is dropped and the
                                  solve starts cold; 0: always start from the warm point */
     int32_t batch_team;       /* batched solver: blocks (one thread-block cluster) per large
-                                 instance, 1..8; 0 = 2; 1 = one block per instance */
+                                 instance, 1..8; 1 = one block per instance; 0 = 2, or in a
+                                 batch of fewer instances than half the resident blocks the
+                                 largest of 2, 4, 8 that keeps every instance resident */
     int32_t batch_team_nnz;   /* batched solver: instances with at least this many nonzeros are
-                                 large; 0 = the larger of 65536 and twice the median instance */
+                                 large; 0 = 65536 in such a small batch, else the larger of
+                                 65536 and twice the median instance */
     int32_t reserved[1];
 } sps_options;
 

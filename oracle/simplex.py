@@ -18,7 +18,10 @@ revised simplex, two phases):
   (Dantzig's rule, Bland's rule after a run of degenerate pivots), and takes
   the bounded ratio test, including a bound flip of the entering column.
 
-Dense and meant for m up to a few hundred rows.
+The basis is dense (LU of m x m, meant for m up to a few hundred rows); the
+constraint matrix stays sparse, so pricing costs O(nnz) per iteration.  Phase 1
+starts from a slack basis where a row's slack has coefficient +1 (its
+artificial only where it has none), and a bound flip keeps the factorization.
 """
 
 from __future__ import annotations
@@ -45,33 +48,33 @@ def _standardize(problem):
     lb = np.asarray(problem.lb, float)
     ub = np.asarray(problem.ub, float)
     n = c0.size
-    K = sp.vstack([sp.csr_matrix(problem.A_ub), sp.csr_matrix(problem.A_eq)]).toarray()
+    K = sp.vstack([sp.csr_matrix(problem.A_ub), sp.csr_matrix(problem.A_eq)]).tocsc()
     rhs = np.concatenate([np.asarray(problem.b_ub, float), np.asarray(problem.b_eq, float)])
     m_ub = problem.A_ub.shape[0]
-    cols, costs, uppers, maps = [], [], [], []      # maps: (orig j, sign, shift)
-    shift_rhs = np.zeros(rhs.size)
+    costs, uppers, maps = [], [], []                 # maps: (orig j, sign, shift)
+    src, sign = [], []                               # column of K and its sign
+    shift = np.zeros(n)                              # x_j's value at z = 0 (0 for free columns)
     const = 0.0
     for j in range(n):
-        a = K[:, j]
         if np.isfinite(lb[j]):                       # x = lb + z, z in [0, ub - lb]
-            cols.append(a); costs.append(c0[j]); uppers.append(ub[j] - lb[j]); maps.append((j, 1.0, lb[j]))
-            shift_rhs += a * lb[j]
+            src.append(j); sign.append(1.0); costs.append(c0[j]); uppers.append(ub[j] - lb[j])
+            maps.append((j, 1.0, lb[j])); shift[j] = lb[j]
             const += c0[j] * lb[j]
         elif np.isfinite(ub[j]):                     # x = ub - z, z >= 0
-            cols.append(-a); costs.append(-c0[j]); uppers.append(np.inf); maps.append((j, -1.0, ub[j]))
-            shift_rhs += a * ub[j]
+            src.append(j); sign.append(-1.0); costs.append(-c0[j]); uppers.append(np.inf)
+            maps.append((j, -1.0, ub[j])); shift[j] = ub[j]
             const += c0[j] * ub[j]
         else:                                        # free: x = z+ - z-
-            cols.append(a); costs.append(c0[j]); uppers.append(np.inf); maps.append((j, 1.0, 0.0))
-            cols.append(-a); costs.append(-c0[j]); uppers.append(np.inf); maps.append((j, -1.0, 0.0))
-    for i in range(m_ub):                            # slacks of the '<=' rows
-        e = np.zeros(rhs.size)
-        e[i] = 1.0
-        cols.append(e); costs.append(0.0); uppers.append(np.inf); maps.append((-1, 0.0, 0.0))
-    A = np.column_stack(cols) if cols else np.zeros((rhs.size, 0))
-    b = rhs - shift_rhs
+            src.append(j); sign.append(1.0); costs.append(c0[j]); uppers.append(np.inf); maps.append((j, 1.0, 0.0))
+            src.append(j); sign.append(-1.0); costs.append(-c0[j]); uppers.append(np.inf); maps.append((j, -1.0, 0.0))
+    Z = K[:, src] @ sp.diags(np.asarray(sign, float)) if src else sp.csc_matrix((rhs.size, 0))
+    S = sp.eye(rhs.size, m_ub, format="csc")        # slacks of the '<=' rows
+    costs += [0.0] * m_ub
+    uppers += [np.inf] * m_ub
+    maps += [(-1, 0.0, 0.0)] * m_ub
+    b = rhs - K @ shift
     sgn = np.where(b < 0, -1.0, 1.0)
-    A = A * sgn[:, None]
+    A = (sp.diags(sgn) @ sp.hstack([Z, S], format="csc")).tocsc()
     b = b * sgn
 
     def recover(z):
@@ -94,18 +97,21 @@ def _simplex(A, b, c, u, basis, at_upper, max_iters, tol=1e-9):
     """Bounded revised simplex from a feasible basis.  `at_upper` marks nonbasic
     columns held at their (finite) upper bound.  Returns (status, z, basis, iters)."""
     m, N = A.shape
+    A = sp.csc_matrix(A)
+    AT = A.T.tocsr()
     basis = list(basis)
     in_basis = np.zeros(N, bool)
     in_basis[basis] = True
     degenerate = 0
+    lu = None
     for it in range(max_iters):
-        B = A[:, basis]
-        lu = la.lu_factor(B)
+        if lu is None:                               # refactor after a basis change only
+            lu = la.lu_factor(A[:, basis].toarray())
+            pi = la.lu_solve(lu, c[basis], trans=1)
+            d = c - AT @ pi
         zN = np.where(at_upper, u, 0.0)
         zN[in_basis] = 0.0
         xB = la.lu_solve(lu, b - A @ zN)
-        pi = la.lu_solve(lu, c[basis], trans=1)
-        d = c - pi @ A
         d[in_basis] = 0.0
         # candidates: at lower with d < 0, at upper with d > 0
         score = np.where(at_upper, d, -d)
@@ -122,7 +128,7 @@ def _simplex(A, b, c, u, basis, at_upper, max_iters, tol=1e-9):
             z = zN.copy()
             z[basis] = xB
             return "optimal", z, basis, it
-        w = la.lu_solve(lu, A[:, q])
+        w = la.lu_solve(lu, A[:, [q]].toarray().ravel())
         dirn = -1.0 if at_upper[q] else 1.0         # entering column moves up from 0 or down from u
         # x_B(t) = x_B - t * dirn * w
         step = dirn * w
@@ -155,6 +161,7 @@ def _simplex(A, b, c, u, basis, at_upper, max_iters, tol=1e-9):
         in_basis[q] = True
         at_upper[q] = False
         at_upper[out] = leave_to_upper
+        lu = None
     return "iteration_limit", None, basis, max_iters
 
 
@@ -169,12 +176,20 @@ def solve(problem, max_iters: int = 50000) -> SimplexResult:
             return SimplexResult("unbounded", np.zeros(n), -np.inf, 0)
         x = recover(z)
         return SimplexResult("optimal", x, float(np.asarray(problem.c) @ x), 0)
-    # phase 1: artificials (identity) make the all-artificial basis feasible
-    A1 = np.hstack([A, np.eye(m)])
+    # phase 1: one artificial per row (identity); the starting basis takes a
+    # row's slack where its coefficient is +1 (feasible at b >= 0), else the
+    # row's artificial
+    A1 = sp.hstack([A, sp.eye(m, format="csc")], format="csc")
     u1 = np.concatenate([u, np.full(m, np.inf)])
     c1 = np.concatenate([np.zeros(N), np.ones(m)])
     at_upper = np.zeros(N + m, bool)
-    st, z1, basis, it1 = _simplex(A1, b, c1, u1, list(range(N, N + m)), at_upper, max_iters)
+    start = list(range(N, N + m))
+    m_ub = problem.A_ub.shape[0]
+    for i in range(m_ub):
+        k = N - m_ub + i                             # slack of row i (the last m_ub columns)
+        if A[i, k] > 0:
+            start[i] = k
+    st, z1, basis, it1 = _simplex(A1, b, c1, u1, start, at_upper, max_iters)
     if st != "optimal":
         return SimplexResult(st, np.zeros(n), np.nan, it1)
     if z1[N:].sum() > 1e-7 * max(1.0, np.abs(b).max()):

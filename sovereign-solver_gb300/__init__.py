@@ -4,7 +4,9 @@
 Public names mirror the reference package exports (``solver/__init__.py:22-38``)
 for this path: ``Solver``, ``Problem``, ``SolveResult``, ``solve_lp_pdhg``,
 ``solve_lp_pdhg_gpu``, ``get_available_device``; plus ``PDHGEngine`` (a problem
-kept resident on the GPU for repeated / warm-started solves).
+kept resident on the GPU for repeated / warm-started solves), ``PDHGBatch``
+(many LPs in one persistent launch) and ``branching`` (strong branching with
+the child LPs solved as one batch, ``solver/milp/branching.py``).
 """
 
 from .problem import Problem
@@ -13,6 +15,7 @@ from .pdhg import PDHGEngine, get_available_device, solve_lp_pdhg, solve_lp_pdhg
 from .solver import Solver
 from .batch import PDHGBatch, solve_lp_pdhg_batch
 from .mps import read_mps
+from . import branching
 
 __version__ = "0.1.0"
 __all__ = ["Solver", "Problem", "SolveResult", "PDHGEngine", "solve_lp_pdhg",

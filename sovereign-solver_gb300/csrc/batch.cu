@@ -272,8 +272,8 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     if (ap == 0) return true;
     const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !c.done;
     const bool save = (ap & AP_SAVE_BEST) && v.xb, save_avg = ap & AP_SAVE_AVG;
-    const double iw = c.w_sum > 0.0 ? 1.0 / c.w_sum : 0.0;
-    const float tau = float(c.eta / c.omega);
+    const double iw = block_scalar<double>([&] { return c.w_sum > 0.0 ? 1.0 / c.w_sum : 0.0; });
+    const float tau = block_scalar<float>([&] { return c.eta / c.omega; });
     float dx2 = 0.f;
     TEAM_OWNED(j, v.n, chc) {
         if (save) v.xb[j] = save_avg ? float(double(v.xl[j]) + double(v.xs[j]) * iw) : v.X[cur][j];
@@ -312,8 +312,9 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
             v.axl[i] = v.AX[cur][i];
         }
     }
-    double t[1] = {double(dx2)};
-    block_sum<1>(t, sm);
+    float f[1] = {dx2};
+    block_sum<1>(f, reinterpret_cast<float*>(sm));
+    double t[1] = {double(f[0])};
     if (!team_total<1>(t, T)) return false;
     if (threadIdx.x == 0) {
         if (cand) c.dx2 = t[0];
@@ -390,25 +391,36 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
     } else {
         if (!start_point(A, k, I, v, warm, c, sm, slots, T)) return false;
     }
+    // Step sizes of the next attempt, computed once by thread 0 (FP64 products
+    // and divisions per thread would occupy this GPU's FP64 pipe, 1/64 of the
+    // FP32 rate); the attempt's reductions are FP32 within the block.
+    __shared__ float s_sigma, s_tau, s_wgt;
+    float* smf = reinterpret_cast<float*>(sm);
     if (threadIdx.x == 0) {
         c.t_begin = t_begin;
         c.warm_used = used ? 1 : 0;
+        s_sigma = float(c.eta * c.omega);
     }
     __syncthreads();
     for (;;) {
         for (int w = 0; w < A.check_interval; ++w) {
             if (c.done || c.iters >= c.max_iters) break;
             int cur = c.cur;
-            RowStepE er{v.b, v.AX[cur], v.Y[cur], v.kind, v.AX[1 - cur], v.Y[1 - cur], float(c.eta * c.omega)};
+            RowStepE er{v.b, v.AX[cur], v.Y[cur], v.kind, v.AX[1 - cur], v.Y[1 - cur], s_sigma};
             group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur], T.size > 1}, er, T.rank, T.size);
-            double t2[2] = {double(er.dy2), double(er.inter)};
-            block_sum<2>(t2, sm);
+            float f2[2] = {er.dy2, er.inter};
+            block_sum<2>(f2, smf);
+            double t2[2] = {double(f2[0]), double(f2[1])};
             if (!team_total<2>(t2, T)) return false;
-            if (threadIdx.x == 0) decide_step(c, t2[0], t2[1]);
+            if (threadIdx.x == 0) {
+                decide_step(c, t2[0], t2[1]);
+                s_tau = float(c.eta / c.omega);
+                s_wgt = float(c.eta_used);
+            }
             __syncthreads();
             if (c.done) break;
             cur = c.cur;
-            const float tau = float(c.eta / c.omega), wgt = float(c.eta_used);
+            const float tau = s_tau, wgt = s_wgt;
             float dx2;
             if (c.accepted) {
                 ColStepE ec{v.X[cur], v.c, v.lo, v.hi, v.xl, v.ATY[cur], v.X[1 - cur], v.xs, tau, wgt};
@@ -424,15 +436,22 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
                     dx2 += (x2 - xj) * (x2 - xj);
                 }
             }
-            double t1[1] = {double(dx2)};
-            block_sum<1>(t1, sm);
+            float f1[1] = {dx2};
+            block_sum<1>(f1, smf);
+            double t1[1] = {double(f1[0])};
             if (!team_total<1>(t1, T)) return false;
-            if (threadIdx.x == 0) { c.dx2 = t1[0]; c.apply = 0; }
+            if (threadIdx.x == 0) {
+                c.dx2 = t1[0];
+                c.apply = 0;
+                s_sigma = float(c.eta * c.omega);
+            }
             __syncthreads();
         }
         if (c.done) break;
         if (!check_and_apply(v, I, c, sm, slots, A.deadline, T)) return false;
         if (c.done) break;
+        if (threadIdx.x == 0) s_sigma = float(c.eta * c.omega);
+        __syncthreads();
     }
     if (threadIdx.x == 0 && T.rank == 0) {
         c.t_end = global_ns();
@@ -949,16 +968,6 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
     b->order.resize(count);
     std::iota(b->order.begin(), b->order.end(), 0);
     std::stable_sort(b->order.begin(), b->order.end(), [&](int32_t a, int32_t c) { return work[a] > work[c]; });
-    // large instances (solved by a team of blocks when clusters are available)
-    // large = at least 65536 nonzeros and twice the median instance: teams shorten the
-    // tail of uneven batches; in batches of similar sizes they would only halve
-    // the number of instances in flight
-    if (opt.batch_team_nnz > 0) {
-        b->team_nnz = opt.batch_team_nnz;
-    } else {
-        const int32_t med = b->inst[b->order[count / 2]].nnz;
-        b->team_nnz = (int32_t)std::max<int64_t>(sps::batch::kTeamNnz, 2LL * med);
-    }
 
     // ---- device
     sps_batch* bp = b.get();
@@ -1036,24 +1045,46 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         int nb = 0, dev = opt.device, sms = 152;
         SPB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sps::batch::k_batch_solve, sps::kBlock, 0));
         SPB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        b->blocks = std::max(1, std::min(count, nb * sms));
+        const int64_t slots = (int64_t)std::max(nb, 1) * sms;      // resident blocks of one wave
+        b->blocks = (int)std::max<int64_t>(1, std::min<int64_t>(count, slots));
+        // Large instances are solved by a team of blocks (one thread-block cluster).
+        // Large = at least batch_team_nnz nonzeros; by default at least 65536 and,
+        // in a batch that fills the GPU, twice the median instance: teams shorten
+        // the tail of uneven batches, and in batches of similar sizes they would
+        // only halve the instances in flight.  A batch of fewer than half as many
+        // instances as resident blocks (strong branching's children) leaves SMs
+        // idle instead: there every instance of 65536 nonzeros or more gets a
+        // team, 2, 4 or 8 blocks, the largest that still fits the resident wave.
+        int want = opt.batch_team > 0 ? std::min(opt.batch_team, 8) : 2;
+        if (opt.batch_team_nnz > 0) {
+            b->team_nnz = opt.batch_team_nnz;
+        } else if ((int64_t)count * 2 <= slots) {
+            b->team_nnz = sps::batch::kTeamNnz;
+            if (opt.batch_team <= 0)
+                while (want < 8 && (int64_t)count * want * 2 <= slots) want *= 2;
+        } else {
+            const int32_t med = b->inst[b->order[count / 2]].nnz;
+            b->team_nnz = (int32_t)std::max<int64_t>(sps::batch::kTeamNnz, 2LL * med);
+        }
+        int64_t n_large = 0;
+        for (int32_t k = 0; k < count; ++k) n_large += b->inst[k].nnz >= b->team_nnz;
         // clusters for the large instances: used when such a launch can be scheduled
-        const int want = opt.batch_team > 0 ? std::min(opt.batch_team, 8) : 2;
-        if (want > 1 && b->blocks >= want) {
+        const int64_t need = std::min<int64_t>(slots, (count - n_large) + n_large * want);
+        if (want > 1 && n_large > 0 && need >= want) {
             cudaLaunchConfig_t cfg = {};
             cudaLaunchAttribute attr[1];
             attr[0].id = cudaLaunchAttributeClusterDimension;
             attr[0].val.clusterDim.x = want;
             attr[0].val.clusterDim.y = 1;
             attr[0].val.clusterDim.z = 1;
-            cfg.gridDim = dim3((b->blocks / want) * want);
+            cfg.gridDim = dim3((unsigned)((need / want) * want));
             cfg.blockDim = dim3(sps::kBlock);
             cfg.attrs = attr;
             cfg.numAttrs = 1;
             int ncl = 0;
             if (cudaOccupancyMaxActiveClusters(&ncl, sps::batch::k_batch_solve, &cfg) == cudaSuccess && ncl > 0) {
                 b->team = want;
-                b->blocks = (b->blocks / want) * want;
+                b->blocks = (int)((need / want) * want);
             }
             cudaGetLastError();
         }

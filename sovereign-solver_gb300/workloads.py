@@ -27,6 +27,9 @@ Workloads (sizes as named):
 * ``transport_family``      200 × 400 transportation LPs on one fixed
                             geometry; per-seed demand × U[0.8, 1.2] and cost
                             × (1 + N(0, 0.05)).
+* ``set_cover_milp``        a node of a branch-and-bound search: 0/1 set
+                            covering, m = 200 rows, n = 2000 binaries, 2 %
+                            density (strong branching's parent problem).
 """
 
 from __future__ import annotations
@@ -231,3 +234,20 @@ class TransportFamily:
 def transport_family(seed: int, family: TransportFamily | None = None) -> tuple[Problem, dict]:
     fam = family or TransportFamily()
     return fam.problem(seed), {}
+
+
+def set_cover_milp(m: int = 200, n: int = 2000, density: float = 0.02, seed: int = 0
+                   ) -> tuple[Problem, dict]:
+    """0/1 set covering MILP: min cᵀx s.t. A x ≥ 1, x ∈ {0, 1}ⁿ, with A binary
+    of the given density (every row covered at least once) and c = U[1, 10];
+    the rows are stored as −A x ≤ −1.  Its LP relaxation is fractional and one
+    branching step moves the objective by about 0.1–1 %."""
+    rng = np.random.default_rng(seed)
+    M = rng.random((m, n)) < density
+    bare = np.flatnonzero(~M.any(1))
+    M[bare, rng.integers(0, n, bare.size)] = True
+    A = sp.csr_matrix(M.astype(float))
+    p = Problem(c=rng.uniform(1.0, 10.0, n), A_ub=-A, b_ub=-np.ones(m), A_eq=sp.csr_matrix((0, n)),
+                b_eq=np.zeros(0), lb=np.zeros(n), ub=np.ones(n), integer_mask=np.ones(n, dtype=bool),
+                name=f"setcover_{m}x{n}_s{seed}")
+    return p, {}

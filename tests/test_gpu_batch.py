@@ -81,12 +81,13 @@ def _large_batch():
     return probs
 
 
-def test_team_solves_large_instances():
+@pytest.mark.parametrize("size", [4, 8])
+def test_team_solves_large_instances(size):
     probs = _large_batch()
     assert sum(p.A_eq.nnz >= 65536 for p in probs) >= 4
-    with sps.PDHGBatch(probs, tol=TOL, batch_team=4) as b:
+    with sps.PDHGBatch(probs, tol=TOL, batch_team=size) as b:
         team = b.solve()
-        assert b.stats.team == 4
+        assert b.stats.team == size
         again = b.solve()                     # graph replay: same bits
     with sps.PDHGBatch(probs, tol=TOL, batch_team=1) as b:
         solo = b.solve()
@@ -97,6 +98,19 @@ def test_team_solves_large_instances():
         assert t.iterations == a.iterations
         np.testing.assert_array_equal(t.x, a.x)
         assert abs(t.objective - s.objective) <= 50 * TOL * (1 + abs(s.objective))
+
+
+def test_small_batch_gets_wide_teams():
+    """16 instances on 608 resident blocks: every instance of 65 536 nonzeros or
+    more is solved by a cluster of 8 blocks by default."""
+    probs = _large_batch()
+    with sps.PDHGBatch(probs, tol=TOL) as b:
+        res = b.solve()
+        assert b.stats.team == 8
+        assert b.stats.blocks >= 8 * sum(p.A_eq.nnz >= 65536 for p in probs)
+    for p, r in zip(probs, res):
+        assert r.status == "optimal", p.name
+        assert kkt.box_rel_kkt(p, r.x, r.y)["err"] < 1.5 * TOL, p.name
 
 
 def test_batch_edge_cases():
