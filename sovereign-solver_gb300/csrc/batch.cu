@@ -43,6 +43,24 @@ struct Gather1 {
 // point 0 aliases the current iterate.
 __device__ __forceinline__ float ld_vec(const float* p, bool coh) { return coh ? __ldcg(p) : __ldg(p); }
 
+// Gathers of the FP32 steps from a copy of the vector in shared memory (when
+// it fits the 7168-float staging buffer): an instance's gathers are random,
+// one 32-byte L1 sector (one L1 wavefront) per nonzero even on an L1 hit,
+// while a warp's 32 random shared-memory reads cost a few bank cycles.
+struct GatherS {
+    const float* s;
+    __device__ __forceinline__ float operator()(int, int j) const { return s[j]; }
+};
+
+// Copy x[0, n) into the staging buffer (coherent loads in a team, where other
+// blocks wrote x).  The first barrier keeps the copy from overwriting entries
+// the block's previous pass may still read.
+__device__ __forceinline__ void stage_vector(float* s, const float* x, int n, bool coh) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < n; j += kBlock) s[j] = ld_vec(x + j, coh);
+    __syncthreads();
+}
+
 __device__ __forceinline__ double avg_at(const float* s, const float* l, double inv_w, int j, bool coh = false) {
     const double v = double(ld_vec(s + j, coh)) * inv_w;
     return l ? v + double(ld_vec(l + j, coh)) : v;
@@ -396,6 +414,9 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
     // FP32 rate); the attempt's reductions are FP32 within the block.
     __shared__ float s_sigma, s_tau, s_wgt;
     float* smf = reinterpret_cast<float*>(sm);
+    // the staging buffer shares its memory with the check's partial slots
+    float* stage = reinterpret_cast<float*>(slots);
+    const bool stage_x = v.n <= A.stage_cap, stage_y = v.m <= A.stage_cap;
     if (threadIdx.x == 0) {
         c.t_begin = t_begin;
         c.warm_used = used ? 1 : 0;
@@ -407,7 +428,13 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             if (c.done || c.iters >= c.max_iters) break;
             int cur = c.cur;
             RowStepE er{v.b, v.AX[cur], v.Y[cur], v.kind, v.AX[1 - cur], v.Y[1 - cur], s_sigma};
-            group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur], T.size > 1}, er, T.rank, T.size);
+            if (stage_x) {
+                stage_vector(stage, v.X[1 - cur], v.n, T.size > 1);
+                group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, GatherS{stage}, er, T.rank, T.size);
+            } else {
+                group_rows_r<1, float>(v.Gr, v.rptr, v.ridx, v.rval, v.m, Gather1{v.X[1 - cur], T.size > 1}, er,
+                                       T.rank, T.size);
+            }
             float f2[2] = {er.dy2, er.inter};
             block_sum<2>(f2, smf);
             double t2[2] = {double(f2[0]), double(f2[1])};
@@ -424,7 +451,13 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             float dx2;
             if (c.accepted) {
                 ColStepE ec{v.X[cur], v.c, v.lo, v.hi, v.xl, v.ATY[cur], v.X[1 - cur], v.xs, tau, wgt};
-                group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur], T.size > 1}, ec, T.rank, T.size);
+                if (stage_y) {
+                    stage_vector(stage, v.Y[cur], v.m, T.size > 1);
+                    group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, GatherS{stage}, ec, T.rank, T.size);
+                } else {
+                    group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[cur], T.size > 1}, ec,
+                                             T.rank, T.size);
+                }
                 dx2 = ec.dx2;
                 TEAM_OWNED(i, v.m, chr) v.ys[i] += wgt * (v.Y[cur][i] - v.yl[i]);
             } else {
@@ -469,7 +502,9 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
 __global__ void __launch_bounds__(kBlock, 4) k_batch_solve(Args A, int G) {
     __shared__ Ctl c;
     __shared__ double sm[kWarps * 10];
-    __shared__ double slots[kColPartials * kBlock];
+    // dynamic: the check partial slots (kColPartials * kBlock doubles), reused as the
+    // steps' staging buffer of A.stage_cap floats
+    extern __shared__ double slots[];
     __shared__ double xch[2 * kXch];
     __shared__ uint32_t counter;
     __shared__ int s_inst, s_err;
@@ -684,6 +719,8 @@ struct sps_batch {
     int32_t count = 0;
     sps_options opt{};
     int32_t G = 8, Gr = 32, blocks = 0;      // lanes per column / per row, persistent blocks
+    int32_t stage_cap = 0;                    // floats of the kernel's shared staging buffer
+    size_t dyn_smem = 0;                      // dynamic shared memory of the solve launch
     int32_t team = 1;                         // cluster size of the solve launch
     int32_t team_nnz = 65536;                 // instances at least this large are solved by a team
     int32_t* d_team_error = nullptr;
@@ -1043,7 +1080,15 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
             b->h_b = std::move(b64);
         }
         int nb = 0, dev = opt.device, sms = 152;
-        SPB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sps::batch::k_batch_solve, sps::kBlock, 0));
+        // Shared staging buffer of the steps' gathers: the memory of the check's
+        // partial slots (7168 floats), which the steps do not use.  A larger
+        // buffer would stage longer vectors but, at 4 blocks per SM, leave the SM
+        // too little L1 for everything else (measured: slower on the
+        // 80k-column transportation family).
+        b->dyn_smem = sizeof(double) * sps::kColPartials * sps::kBlock;
+        b->stage_cap = (int32_t)(b->dyn_smem / sizeof(float));
+        SPB_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, sps::batch::k_batch_solve, sps::kBlock,
+                                                             b->dyn_smem));
         SPB_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const int64_t slots = (int64_t)std::max(nb, 1) * sms;      // resident blocks of one wave
         b->blocks = (int)std::max<int64_t>(1, std::min<int64_t>(count, slots));
@@ -1079,6 +1124,7 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
             attr[0].val.clusterDim.z = 1;
             cfg.gridDim = dim3((unsigned)((need / want) * want));
             cfg.blockDim = dim3(sps::kBlock);
+            cfg.dynamicSmemBytes = b->dyn_smem;
             cfg.attrs = attr;
             cfg.numAttrs = 1;
             int ncl = 0;
@@ -1114,8 +1160,9 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         auto time_one = [&](int sched, float* cost) -> bool {
             sps::batch::Args A{bb->d_inst, d_pick, sample, 32, 32, 0.0, bb->d_deadline, bb->arr, bb->d_out,
                                bb->d_counter, 0};
+            A.stage_cap = bb->stage_cap;
             cudaMemsetAsync(bb->d_counter, 0, sizeof(uint32_t), bb->st);
-            sps::batch::k_batch_solve<<<std::min(bb->blocks, sample), sps::kBlock, 0, bb->st>>>(A, sched);
+            sps::batch::k_batch_solve<<<std::min(bb->blocks, sample), sps::kBlock, bb->dyn_smem, bb->st>>>(A, sched);
             cudaMemcpyAsync(outs.data(), bb->d_out, sizeof(Ctl) * count, cudaMemcpyDeviceToHost, bb->st);
             if (cudaStreamSynchronize(bb->st) != cudaSuccess) return false;
             double tot = 0.0;
@@ -1161,7 +1208,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     sps::batch::Args A{b->d_inst, b->d_order, b->count, (int32_t)W, b->opt.max_iters, b->opt.tol, b->d_deadline,
                        b->arr, b->d_out, b->d_counter, b->opt.escalate != 0 ? 1 : 0, b->warm,
                        b->opt.warm_fallback ? 1 : 0, b->d_wx, b->d_wy, b->d_wom, b->d_cold_rel,
-                       b->team, b->team_nnz, b->d_team_error};
+                       b->team, b->team_nnz, b->d_team_error, b->stage_cap};
     auto enqueue = [&](cudaStream_t s) {
         cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
         sps::batch::k_set_deadline<<<1, 32, 0, s>>>(b->d_deadline, tl);
@@ -1176,12 +1223,13 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
             attr[0].val.clusterDim.z = 1;
             cfg.gridDim = dim3(b->blocks);
             cfg.blockDim = dim3(sps::kBlock);
+            cfg.dynamicSmemBytes = b->dyn_smem;
             cfg.stream = s;
             cfg.attrs = attr;
             cfg.numAttrs = 1;
             cudaLaunchKernelEx(&cfg, sps::batch::k_batch_solve, A, sched);
         } else {
-            sps::batch::k_batch_solve<<<b->blocks, sps::kBlock, 0, s>>>(A, sched);
+            sps::batch::k_batch_solve<<<b->blocks, sps::kBlock, b->dyn_smem, s>>>(A, sched);
         }
     };
     SPB_CK(cudaEventRecord(b->e0, b->st));

@@ -55,6 +55,7 @@ struct Args {
     int32_t team;             // cluster size of the launch (1 = one block per instance)
     int32_t team_nnz;         // instances with at least this many nonzeros are solved by a whole cluster
     int32_t* team_error;      // set when a team barrier gave up waiting
+    int32_t stage_cap;        // floats of the block's shared staging buffer (0 = gathers from global)
 };
 
 // ---------------------------------------------------------------------------
