@@ -1282,8 +1282,10 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     int32_t n_esc = 0;
     double esc_ms = 0.0;
     if (b->opt.escalate == 1) {
-        // FP64 continuations of the stalled instances, several at once: each has its
-        // own engine and stream, so their small kernels overlap on the GPU
+        // FP64 continuations of the stalled instances, all at once (up to 32 host
+        // threads): each has its own engine and stream, and their latency-bound
+        // kernels overlap on the GPU (8 at a time left 2-3 rounds of 100-300 ms
+        // on the 4096-LP batch)
         const auto t0 = std::chrono::steady_clock::now();
         std::vector<int32_t> todo;
         for (int32_t k = 0; k < b->count; ++k)
@@ -1300,7 +1302,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
                 b->esc_ms[k] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
             }
         };
-        const int nt = (int)std::min<size_t>(todo.size(), 8);
+        const int nt = (int)std::min<size_t>(todo.size(), 32);
         std::vector<std::thread> pool;
         for (int t = 1; t < nt; ++t) pool.emplace_back(work);
         if (!todo.empty()) work();
