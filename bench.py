@@ -372,7 +372,7 @@ def run_batch(args, rank, world):
         n_, m_ = p.n_vars, p.n_ineq + p.n_eq
         z = p.A_eq.nnz + p.A_ub.nnz
         alg += r.iterations * (16 * z + 4 * (m_ + 1) + 4 * n_ + 20 * m_ + 4 * (n_ + 1) + 4 * m_ + 36 * n_ + 16 * m_)
-    lanes, blocks, esc = st.lanes_per_column, st.blocks, st.escalated
+    lanes, blocks, esc, hand = st.lanes_per_column, st.blocks, st.escalated, st.handed_off
     b.close()
 
     # end to end through the C ABI from host arrays
@@ -419,7 +419,8 @@ def run_batch(args, rank, world):
                    "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)"},
         "iters_p50": float(np.percentile(its, 50)), "iters_p99": float(np.percentile(its, 99)),
         "iters_max": int(its.max()), "optimal": int(sum(r.status == "optimal" for r in res)),
-        "escalated_fp64": int(esc), "max_rel_kkt": float(kkts.max()), "max_obj_error_vs_planted": float(obj_err),
+        "escalated_fp64": int(esc), "handed_off": int(hand),
+        "max_rel_kkt": float(kkts.max()), "max_obj_error_vs_planted": float(obj_err),
         "lanes_per_column": int(lanes), "persistent_blocks": int(blocks),
         "gpu_launches": 3 * args.steps,
         "e2e": {"value": total / e2e_t, "unit": "solves/s", "sec_per_batch": e2e_t,

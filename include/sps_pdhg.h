@@ -102,6 +102,13 @@ typedef struct {
     int32_t batch_team_nnz;   /* batched solver: instances with at least this many nonzeros are
                                  large; 0 = 65536 in such a small batch, else the larger of
                                  65536 and twice the median instance */
+    int32_t batch_handoff_nnz;/* batched solver: > 0: once the instance queue is empty and half
+                                 the blocks have left, an instance with at least this many
+                                 nonzeros and 512 attempts still running stops at its next check
+                                 and is finished by the single-LP engine (FP32, the whole GPU)
+                                 from its current point.  Which instances leave depends on
+                                 timing, so results are no longer bit-identical from run to run;
+                                 0 (default) = never */
     int32_t reserved[1];
 } sps_options;
 
@@ -186,7 +193,7 @@ typedef struct sps_batch sps_batch;
 
 typedef struct {
     double  setup_ms;           /* sps_batch_create device work (upload excluded) */
-    double  solve_ms;           /* device time of the persistent launch */
+    double  solve_ms;           /* the persistent launch plus the continuations after it */
     int64_t total_iterations;   /* sum over instances */
     int32_t optimal;            /* instances that reached tol */
     int32_t lanes_per_column;   /* schedule used (autotuned or given) */
@@ -195,7 +202,9 @@ typedef struct {
                                    single-LP engine after the persistent launch (in solve_ms) */
     int32_t lanes_per_row;      /* row-pass schedule (4, 8, 16, 32 lanes per row; timed) */
     int32_t team;               /* blocks per large instance in the launch (1 = no clusters) */
-    int32_t reserved[2];
+    int32_t handed_off;         /* instances finished by the single-LP engine after leaving the
+                                   launch's tail (batch_handoff_nnz; in solve_ms) */
+    int32_t reserved[1];
 } sps_batch_stats;
 
 /* Pack `count` problems, upload and scale them (one block per instance) and pick

@@ -44,7 +44,8 @@ class Options(C.Structure):
         ("check_interval", C.c_int32), ("ruiz_iters", C.c_int32), ("time_limit_s", C.c_double),
         ("graph_mode", C.c_int32), ("device", C.c_int32), ("max_blocks", C.c_int32),
         ("batch_group", C.c_int32), ("escalate", C.c_int32), ("warm_fallback", C.c_int32),
-        ("batch_team", C.c_int32), ("batch_team_nnz", C.c_int32), ("reserved", C.c_int32 * 1),
+        ("batch_team", C.c_int32), ("batch_team_nnz", C.c_int32), ("batch_handoff_nnz", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 
@@ -52,7 +53,8 @@ class BatchStats(C.Structure):
     _fields_ = [
         ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("total_iterations", C.c_int64),
         ("optimal", C.c_int32), ("lanes_per_column", C.c_int32), ("blocks", C.c_int32),
-        ("escalated", C.c_int32), ("lanes_per_row", C.c_int32), ("team", C.c_int32), ("reserved", C.c_int32 * 2),
+        ("escalated", C.c_int32), ("lanes_per_row", C.c_int32), ("team", C.c_int32), ("handed_off", C.c_int32),
+        ("reserved", C.c_int32 * 1),
     ]
 
 

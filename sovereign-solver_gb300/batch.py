@@ -34,12 +34,18 @@ class PDHGBatch:
     such a small batch, else the larger of 65 536 and twice the median).
     ``escalate``: "fp64" (FP64 continuation of stalled instances), "stop"
     (status "stalled") or "off" (FP32 to the iteration limit).
+    ``batch_handoff_nnz`` (> 0): once the instance queue is empty and half the
+    blocks have left, instances with at least this many nonzeros (and 512
+    attempts) still running leave the launch and are finished by the single-LP
+    engine on the whole GPU; which ones leave depends on timing, so results are
+    not bit-identical from run to run.  0 (default) = never.
     """
 
     def __init__(self, problems: Sequence, tol: float = 1e-4, max_iters: int = MAX_PDHG_ITERS,
                  batch_group: int = 0, time_limit: float = 0.0, check_interval: int = 0,
                  graph_mode: int = 2, device: int = 0, ruiz_iters: int = 10, escalate: str = "fp64",
-                 warm_fallback: bool = True, batch_team: int = 0, batch_team_nnz: int = 0):
+                 warm_fallback: bool = True, batch_team: int = 0, batch_team_nnz: int = 0,
+                 batch_handoff_nnz: int = 0):
         self.lib = N.load()
         self.problems = list(problems)
         if not self.problems:
@@ -52,6 +58,7 @@ class PDHGBatch:
         o.batch_group = int(batch_group)
         o.batch_team = int(batch_team)
         o.batch_team_nnz = int(batch_team_nnz)
+        o.batch_handoff_nnz = int(batch_handoff_nnz)
         h = C.c_void_p()
         N.check(self.lib.sps_batch_create(len(self._descs), arr, C.byref(o), C.byref(h)), None)
         self.h = h

@@ -249,8 +249,19 @@ __device__ __forceinline__ void slot_sums(const double* slots, double* out) {
     for (int o_ = threadIdx.x, var; (var = (T.rank + (o_ / (CH)) * T.size) * (CH) + o_ % (CH)) < (count); \
          o_ += kBlock)
 
+// Hand-off test of a check: the queue is empty, half the launch's blocks have
+// left, and this instance is large and has made kHandoffMin attempts.  Each
+// block reads the idle counter itself; the team adds the blocks' votes, so all
+// its blocks take the same decision.
+struct Handoff {
+    const uint32_t* idle;
+    uint32_t need;
+    bool eligible;            // instance large enough (and hand-off on)
+};
+
 __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm, double* slots, const uint64_t* dl,
-                                const Team& T) {
+                                const Team& T, const Handoff& H) {
+    __shared__ bool s_handoff;
     const int chc = kWarps * (32 / v.G), chr = kWarps * (32 / v.Gr);
     const uint64_t deadline = *dl;
     const bool has_avg = c.w_sum > 0.0;
@@ -273,21 +284,30 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
     slot_sums<kColPartials>(slots, sm + kRowPartials);   // then the column partials
     // team totals of the partials and of the deadline test (any block past it stops all)
     constexpr int NT = kRowPartials + kColPartials;
-    double tt[NT + 1];
+    double tt[NT + 2];
     if (threadIdx.x == 0) {
         for (int q = 0; q < NT; ++q) tt[q] = sm[q];
         tt[NT] = (deadline && global_ns() > deadline) ? 1.0 : 0.0;
+        tt[NT + 1] = (H.eligible && c.iters >= kHandoffMin &&
+                      *reinterpret_cast<const volatile uint32_t*>(H.idle) >= H.need) ? 1.0 : 0.0;
     }
-    if (!team_total<NT + 1>(tt, T)) return false;
+    if (!team_total<NT + 2>(tt, T)) return false;
     if (threadIdx.x == 0) {
         double tr[kRowPartials], tc[kColPartials];
         for (int q = 0; q < kRowPartials; ++q) tr[q] = tt[q];
         for (int q = 0; q < kColPartials; ++q) tc[q] = tt[kRowPartials + q];
         decide_check(c, tc, tr, I.inv_nb, I.inv_nc, tt[NT] > 0.0);
+        s_handoff = !c.done && tt[NT + 1] > 0.0;
     }
     __syncthreads();
     const int ap = c.apply;
-    if (ap == 0) return true;
+    if (ap == 0) {
+        if (s_handoff) {
+            if (threadIdx.x == 0) { c.done = 1; c.status = kStatusHandoff; }
+            __syncthreads();
+        }
+        return true;
+    }
     const bool load = ap & AP_LOAD_AVG, rst = ap & AP_RESTART, cand = (ap & AP_CANDIDATE) && !c.done;
     const bool save = (ap & AP_SAVE_BEST) && v.xb, save_avg = ap & AP_SAVE_AVG;
     const double iw = block_scalar<double>([&] { return c.w_sum > 0.0 ? 1.0 / c.w_sum : 0.0; });
@@ -338,6 +358,9 @@ __device__ bool check_and_apply(const View& v, const Inst& I, Ctl& c, double* sm
         if (cand) c.dx2 = t[0];
         if (rst) c.w_sum = 0.0;
         c.apply = 0;
+        // after the restart / averaging above: the handed-off point is the one
+        // the instance would have continued from
+        if (s_handoff) { c.done = 1; c.status = kStatusHandoff; }
     }
     __syncthreads();
     return true;
@@ -381,7 +404,7 @@ __device__ bool start_point(const Args& A, int k, const Inst& I, const View& v, 
     StoreE sy{v.ATY[0]};
     group_rows_dyn<1, float>(v.G, v.cptr, v.cidx, v.cval, v.n, Gather1{v.Y[0], T.size > 1}, sy, T.rank, T.size);
     if (!team_barrier(T)) return false;
-    return check_and_apply(v, I, c, sm, slots, A.deadline, T);
+    return check_and_apply(v, I, c, sm, slots, A.deadline, T, Handoff{A.idle, A.idle_need, false});
 }
 
 // The whole solve of instance k by this block (T.size == 1) or by the team of
@@ -414,6 +437,7 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
     // FP32 rate); the attempt's reductions are FP32 within the block.
     __shared__ float s_sigma, s_tau, s_wgt;
     float* smf = reinterpret_cast<float*>(sm);
+    const Handoff H{A.idle, A.idle_need, A.handoff_nnz > 0 && I.nnz >= A.handoff_nnz};
     // the staging buffer shares its memory with the check's partial slots
     float* stage = reinterpret_cast<float*>(slots);
     const bool stage_x = v.n <= A.stage_cap, stage_y = v.m <= A.stage_cap;
@@ -481,7 +505,7 @@ __device__ bool solve_one(const Args& A, int k, int G, Ctl& c, double* sm, doubl
             __syncthreads();
         }
         if (c.done) break;
-        if (!check_and_apply(v, I, c, sm, slots, A.deadline, T)) return false;
+        if (!check_and_apply(v, I, c, sm, slots, A.deadline, T, H)) return false;
         if (c.done) break;
         if (threadIdx.x == 0) s_sigma = float(c.eta * c.omega);
         __syncthreads();
@@ -559,6 +583,9 @@ __global__ void __launch_bounds__(kBlock, 4) k_batch_solve(Args A, int G) {
         solve_one(A, k, G, c, sm, slots, solo);
         __syncthreads();
     }
+    // this block found the queue empty (or its team gave up): it counts towards
+    // the hand-off threshold of the instances still running
+    if (threadIdx.x == 0 && A.idle) atomicAdd(A.idle, 1u);
     if (threadIdx.x == 0 && s_err) atomicExch(A.team_error, 1);
     // every block reaches this point once (all loops above are bounded): no block
     // leaves while a peer may still read its shared memory (the barrier counter,
@@ -724,6 +751,9 @@ struct sps_batch {
     int32_t team = 1;                         // cluster size of the solve launch
     int32_t team_nnz = 65536;                 // instances at least this large are solved by a team
     int32_t* d_team_error = nullptr;
+    uint32_t* d_idle = nullptr;               // blocks that found the queue empty (per launch)
+    int32_t handoff_nnz = 0;                  // instances this large may leave the tail (0 = never)
+    std::vector<int8_t> handed_off;
     cudaStream_t st = nullptr;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     std::vector<Inst> inst;
@@ -817,13 +847,17 @@ bool check_instance(const sps_problem_desc& d, std::string& why) {
     return true;
 }
 
-// FP64 continuation of stalled instance k (after the persistent launch): the
-// single-LP engine solves it in FP64, warm-started from the best point of the
-// FP32 stall test (in xo / yo) with the primal weight it had there, within the
-// iterations and time left; its result replaces the instance's.
-int continue_fp64(sps_batch* b, int32_t k, double used_s, std::string* why) {
+// Continuation of instance k on the single-LP engine after the persistent
+// launch, within the iterations and time left; its result replaces the
+// instance's.  A stalled instance continues in FP64 from the best point of the
+// FP32 stall test (in xo / yo) with the primal weight it had there; an instance
+// handed off from the launch's tail continues in FP32 (with its own stall test
+// and FP64 continuation) from its current point and primal weight.
+int continue_single(sps_batch* b, int32_t k, double used_s, std::string* why) {
     const Inst& I = b->inst[k];
     Ctl& c = b->out[k];
+    const bool handoff = c.status == sps::batch::kStatusHandoff;
+    const char* what = handoff ? " continuation after hand-off: " : " FP64 continuation: ";
     if (b->opt.time_limit_s > 0 && used_s >= b->opt.time_limit_s) {
         c.status = SPS_STATUS_TIME_LIMIT;
         return SPS_OK;
@@ -848,24 +882,24 @@ int continue_fp64(sps_batch* b, int32_t k, double used_s, std::string* why) {
     d.b_ub = b->h_b.data() + I.vr;
     d.b_eq = b->h_b.data() + I.vr + I.m_ub;
     sps_options o = b->opt;
-    o.precision = SPS_FP64;
-    o.escalate = 0;
+    o.precision = handoff ? SPS_FP32 : SPS_FP64;
+    o.escalate = handoff ? b->opt.escalate : 0;
     o.max_iters = std::max<int64_t>(b->opt.max_iters - c.iters, 1);
     o.time_limit_s = b->opt.time_limit_s > 0 ? b->opt.time_limit_s - used_s : 0.0;
     sps_handle* h = nullptr;
     int rc = sps_create(&d, &o, &h);
     if (rc != SPS_OK) {
-        *why = "instance " + std::to_string(k) + " FP64 continuation: " + sps_last_error(nullptr);
+        *why = "instance " + std::to_string(k) + what + sps_last_error(nullptr);
         return rc;
     }
     sps_result r;
     double* x = b->xo.data() + I.vc;
     double* y = b->yo.data() + I.vr;
-    rc = sps_set_warm_start(h, x, y, c.omega_best);
+    rc = sps_set_warm_start(h, x, y, handoff ? c.omega : c.omega_best);
     if (rc == SPS_OK) rc = sps_solve(h, &r);
     if (rc == SPS_OK) rc = sps_get_solution(h, x, y);
     if (rc != SPS_OK) {
-        *why = "instance " + std::to_string(k) + " FP64 continuation: " + sps_last_error(h);
+        *why = "instance " + std::to_string(k) + what + sps_last_error(h);
         sps_destroy(h);
         return rc;
     }
@@ -878,7 +912,8 @@ int continue_fp64(sps_batch* b, int32_t k, double used_s, std::string* why) {
     c.omega = r.primal_weight;
     c.eta = r.step_size;
     c.choice = r.returned_average;
-    b->escalated[k] = 1;
+    b->escalated[k] = handoff ? (int8_t)r.escalated : 1;
+    b->handed_off[k] = handoff ? 1 : 0;
     return SPS_OK;
 }
 
@@ -1040,6 +1075,7 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         SPB_CK(b->alloc(&b->d_yo, vr));
         SPB_CK(b->alloc(&b->d_cold_rel, count));
         SPB_CK(b->alloc(&b->d_team_error, 1));
+        SPB_CK(b->alloc(&b->d_idle, 1));
         SPB_CK(cudaMemsetAsync(b->d_cold_rel, 0xFF, sizeof(double) * count, b->st));   // NaN = unknown
         float *d_xb = nullptr, *d_yb = nullptr, *d_axl, *d_atyl;
         if (opt.escalate != 0) { SPB_CK(b->alloc(&d_xb, vc)); SPB_CK(b->alloc(&d_yb, vr)); }
@@ -1073,7 +1109,8 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
                                st_f[0], st_f[1], st_f[2], st_f[3], st_f[4], st_f[5], st_f[6],
                                st_f[7], st_f[8], st_f[9], st_f[10], st_f[11], st_f[12], st_f[13], d_xb, d_yb,
                                d_axl, d_atyl};
-        if (opt.escalate == 1) {
+        b->handoff_nnz = std::max(opt.batch_handoff_nnz, 0);
+        if (opt.escalate == 1 || b->handoff_nnz > 0) {       // host copy for continuations
             b->h_rptr = std::move(rptr);
             b->h_ridx = std::move(ridx);
             b->h_rv = std::move(rv);
@@ -1208,11 +1245,13 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     sps::batch::Args A{b->d_inst, b->d_order, b->count, (int32_t)W, b->opt.max_iters, b->opt.tol, b->d_deadline,
                        b->arr, b->d_out, b->d_counter, b->opt.escalate != 0 ? 1 : 0, b->warm,
                        b->opt.warm_fallback ? 1 : 0, b->d_wx, b->d_wy, b->d_wom, b->d_cold_rel,
-                       b->team, b->team_nnz, b->d_team_error, b->stage_cap};
+                       b->team, b->team_nnz, b->d_team_error, b->stage_cap, b->d_idle,
+                       (uint32_t)(b->blocks - b->blocks / 8), b->handoff_nnz};
     auto enqueue = [&](cudaStream_t s) {
         cudaMemsetAsync(b->d_counter, 0, sizeof(uint32_t), s);
         sps::batch::k_set_deadline<<<1, 32, 0, s>>>(b->d_deadline, tl);
         cudaMemsetAsync(b->d_team_error, 0, sizeof(int32_t), s);
+        cudaMemsetAsync(b->d_idle, 0, sizeof(uint32_t), s);
         const int sched = sps::batch::pack_schedule(b->G, b->Gr);
         if (b->team > 1) {
             cudaLaunchConfig_t cfg = {};
@@ -1278,18 +1317,21 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
     SPB_CK(cudaMemcpy(&team_err, b->d_team_error, sizeof(int32_t), cudaMemcpyDeviceToHost));
     if (team_err) return b->fail(SPS_ERR_CUDA, "a team barrier of the batched solve timed out");
     b->escalated.assign(b->count, 0);
+    b->handed_off.assign(b->count, 0);
     b->esc_ms.assign(b->count, 0.0);
-    int32_t n_esc = 0;
+    int32_t n_esc = 0, n_hand = 0;
     double esc_ms = 0.0;
-    if (b->opt.escalate == 1) {
-        // FP64 continuations of the stalled instances, all at once (up to 32 host
-        // threads): each has its own engine and stream, and their latency-bound
-        // kernels overlap on the GPU (8 at a time left 2-3 rounds of 100-300 ms
-        // on the 4096-LP batch)
+    {
+        // Continuations on the single-LP engine, all at once (up to 32 host
+        // threads; each has its own engine and stream, and their latency-bound
+        // kernels overlap on the GPU): FP64 for the instances that stalled in FP32
+        // (escalate = 1), FP32 for the ones handed off from the launch's tail.
         const auto t0 = std::chrono::steady_clock::now();
         std::vector<int32_t> todo;
-        for (int32_t k = 0; k < b->count; ++k)
-            if (b->out[k].status == SPS_STATUS_STALLED) todo.push_back(k);
+        for (int32_t k = 0; k < b->count; ++k) {
+            const int32_t st = b->out[k].status;
+            if ((st == SPS_STATUS_STALLED && b->opt.escalate == 1) || st == sps::batch::kStatusHandoff) todo.push_back(k);
+        }
         std::vector<int> rcs(todo.size(), SPS_OK);
         std::vector<std::string> whys(todo.size());
         std::atomic<size_t> next{0};
@@ -1298,7 +1340,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
                 const int32_t k = todo[i];
                 const auto t1 = std::chrono::steady_clock::now();
                 const double used = ms * 1e-3 + std::chrono::duration<double>(t1 - t0).count();
-                rcs[i] = continue_fp64(b, k, used, &whys[i]);
+                rcs[i] = continue_single(b, k, used, &whys[i]);
                 b->esc_ms[k] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t1).count();
             }
         };
@@ -1309,8 +1351,11 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
         for (auto& th : pool) th.join();
         for (size_t i = 0; i < todo.size(); ++i)
             if (rcs[i] != SPS_OK) return b->fail(rcs[i], whys[i]);
-        n_esc = (int32_t)todo.size();
-        esc_ms = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        for (int32_t k : todo) {
+            n_esc += b->escalated[k];
+            n_hand += b->handed_off[k];
+        }
+        esc_ms = todo.empty() ? 0.0 : 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     b->solve_ms = ms + esc_ms;
     b->solved = true;
@@ -1323,6 +1368,7 @@ extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
         stats->team = b->team;
         stats->blocks = b->blocks;
         stats->escalated = n_esc;
+        stats->handed_off = n_hand;
         for (const Ctl& c : b->out) {
             stats->total_iterations += c.iters;
             if (c.status == SPS_STATUS_OPTIMAL) stats->optimal += 1;
@@ -1431,7 +1477,7 @@ extern "C" int sps_batch_get(sps_batch* b, int32_t k, double* x, double* y, sps_
         res->primal_weight = c.omega;
         res->step_size = c.eta;
         res->setup_ms = b->setup_ms;
-        res->solve_ms = 1e-6 * double(c.t_end - c.t_begin) + (b->escalated[k] ? b->esc_ms[k] : 0.0);
+        res->solve_ms = 1e-6 * double(c.t_end - c.t_begin) + b->esc_ms[k];
         res->kernel_launches = 1;
         res->returned_average = c.choice;
         res->escalated = b->escalated[k];

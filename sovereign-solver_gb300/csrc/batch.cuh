@@ -56,7 +56,15 @@ struct Args {
     int32_t team_nnz;         // instances with at least this many nonzeros are solved by a whole cluster
     int32_t* team_error;      // set when a team barrier gave up waiting
     int32_t stage_cap;        // floats of the block's shared staging buffer (0 = gathers from global)
+    uint32_t* idle;           // blocks that found the instance queue empty (reset per launch)
+    uint32_t idle_need;       // hand-off threshold: half the launch's blocks
+    int32_t handoff_nnz;      // instances this large may be handed off (0 = never)
 };
+
+// Internal status of an instance that left the launch's tail for the single-LP
+// engine (replaced by the continuation's status before any caller sees it).
+constexpr int32_t kStatusHandoff = 100;
+constexpr int64_t kHandoffMin = 512;      // attempts an instance makes before it may be handed off
 
 // ---------------------------------------------------------------------------
 // Teams: the blocks of one thread-block cluster solving one large instance.

@@ -113,6 +113,25 @@ def test_small_batch_gets_wide_teams():
         assert kkt.box_rel_kkt(p, r.x, r.y)["err"] < 1.5 * TOL, p.name
 
 
+def test_tail_handoff_to_single_engine():
+    """12 tiny instances and 4 larger ones: once the tiny ones are done (more than
+    half the blocks idle) the larger ones leave the launch at their next check and
+    the single-LP engine finishes them; same answers as without hand-off."""
+    probs = [wl.batch_planted_lp(k, m_range=(20, 40))[0] for k in range(12)]
+    probs += [wl.batch_planted_lp(100 + k, m_range=(1500, 2000))[0] for k in range(4)]
+    with sps.PDHGBatch(probs, tol=TOL, batch_handoff_nnz=1) as b:
+        hand = b.solve()
+        n_hand = b.stats.handed_off
+    with sps.PDHGBatch(probs, tol=TOL) as b:                 # default: no hand-off
+        stay = b.solve()
+        assert b.stats.handed_off == 0
+    assert n_hand >= 1
+    for p, h, s in zip(probs, hand, stay):
+        assert h.status == "optimal" and s.status == "optimal", p.name
+        assert kkt.box_rel_kkt(p, h.x, h.y)["err"] < 1.5 * TOL, p.name
+        assert abs(h.objective - s.objective) <= 50 * TOL * (1 + abs(s.objective)), p.name
+
+
 def test_batch_edge_cases():
     """An instance with no rows, one with an empty column, beside a normal one."""
     import scipy.sparse as sp
