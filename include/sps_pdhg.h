@@ -102,8 +102,8 @@ typedef struct {
     int32_t batch_team_nnz;   /* batched solver: instances with at least this many nonzeros are
                                  large; 0 = 65536 in such a small batch, else the larger of
                                  65536 and twice the median instance */
-    int32_t batch_handoff_nnz;/* batched solver: > 0: once the instance queue is empty and half
-                                 the blocks have left, an instance with at least this many
+    int32_t batch_handoff_nnz;/* batched solver: > 0: once the instance queue is empty and 7/8
+                                 of the blocks have left, an instance with at least this many
                                  nonzeros and 512 attempts still running stops at its next check
                                  and is finished by the single-LP engine (FP32, the whole GPU)
                                  from its current point.  Which instances leave depends on

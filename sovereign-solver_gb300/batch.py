@@ -34,7 +34,7 @@ class PDHGBatch:
     such a small batch, else the larger of 65 536 and twice the median).
     ``escalate``: "fp64" (FP64 continuation of stalled instances), "stop"
     (status "stalled") or "off" (FP32 to the iteration limit).
-    ``batch_handoff_nnz`` (> 0): once the instance queue is empty and half the
+    ``batch_handoff_nnz`` (> 0): once the instance queue is empty and 7/8 of the
     blocks have left, instances with at least this many nonzeros (and 512
     attempts) still running leave the launch and are finished by the single-LP
     engine on the whole GPU; which ones leave depends on timing, so results are

@@ -249,7 +249,7 @@ __device__ __forceinline__ void slot_sums(const double* slots, double* out) {
     for (int o_ = threadIdx.x, var; (var = (T.rank + (o_ / (CH)) * T.size) * (CH) + o_ % (CH)) < (count); \
          o_ += kBlock)
 
-// Hand-off test of a check: the queue is empty, half the launch's blocks have
+// Hand-off test of a check: the queue is empty, 7/8 of the launch's blocks have
 // left, and this instance is large and has made kHandoffMin attempts.  Each
 // block reads the idle counter itself; the team adds the blocks' votes, so all
 // its blocks take the same decision.

@@ -57,7 +57,7 @@ struct Args {
     int32_t* team_error;      // set when a team barrier gave up waiting
     int32_t stage_cap;        // floats of the block's shared staging buffer (0 = gathers from global)
     uint32_t* idle;           // blocks that found the instance queue empty (reset per launch)
-    uint32_t idle_need;       // hand-off threshold: half the launch's blocks
+    uint32_t idle_need;       // hand-off threshold: 7/8 of the launch's blocks
     int32_t handoff_nnz;      // instances this large may be handed off (0 = never)
 };
 

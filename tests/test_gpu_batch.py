@@ -114,8 +114,8 @@ def test_small_batch_gets_wide_teams():
 
 
 def test_tail_handoff_to_single_engine():
-    """12 tiny instances and 4 larger ones: once the tiny ones are done (more than
-    half the blocks idle) the larger ones leave the launch at their next check and
+    """12 tiny instances and 4 larger ones: once the tiny ones are done (at least
+    7/8 of the blocks idle) the larger ones leave the launch at their next check and
     the single-LP engine finishes them; same answers as without hand-off."""
     probs = [wl.batch_planted_lp(k, m_range=(20, 40))[0] for k in range(12)]
     probs += [wl.batch_planted_lp(100 + k, m_range=(1500, 2000))[0] for k in range(4)]
