@@ -114,15 +114,16 @@ def test_small_batch_gets_wide_teams():
 
 
 def test_tail_handoff_to_single_engine():
-    """12 tiny instances and 4 larger ones: once the tiny ones are done (at least
-    7/8 of the blocks idle) the larger ones leave the launch at their next check and
-    the single-LP engine finishes them; same answers as without hand-off."""
-    probs = [wl.batch_planted_lp(k, m_range=(20, 40))[0] for k in range(12)]
+    """60 tiny instances and 4 larger ones, one block each: once the tiny ones are
+    done (at least 7/8 of the blocks idle) the larger ones leave the launch at
+    their first check after 512 attempts and the single-LP engine finishes them;
+    same answers as without hand-off (the default)."""
+    probs = [wl.batch_planted_lp(k, m_range=(20, 40))[0] for k in range(60)]
     probs += [wl.batch_planted_lp(100 + k, m_range=(1500, 2000))[0] for k in range(4)]
-    with sps.PDHGBatch(probs, tol=TOL, batch_handoff_nnz=1) as b:
+    with sps.PDHGBatch(probs, tol=TOL, batch_team=1, batch_handoff_nnz=1) as b:
         hand = b.solve()
         n_hand = b.stats.handed_off
-    with sps.PDHGBatch(probs, tol=TOL) as b:                 # default: no hand-off
+    with sps.PDHGBatch(probs, tol=TOL, batch_team=1) as b:
         stay = b.solve()
         assert b.stats.handed_off == 0
     assert n_hand >= 1
