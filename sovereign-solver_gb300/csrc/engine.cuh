@@ -68,8 +68,12 @@ struct Layout {
     const int32_t* idx;
     const V* val;
     const int32_t* soff;     // slice offsets (slices + 1)
-    const int32_t* seg_row;  // internal row of each segment (SLAB: slice inside its bin)
-    const int32_t* seg_k;    // segment number inside its row (SLAB: unit inside its slice)
+    const int4* unit;        // SEGMENT / SLAB unit descriptors, two int4 (32 bytes) per unit:
+                             //   SEGMENT {s, t, r, nseg} {kseg, 0, 0, 0}: nonzeros [s, t) of
+                             //     internal row r, segment kseg of its nseg
+                             //   SLAB    {off, len, sl, c} {0, 0, 0, 0}: unit c of slice sl of
+                             //     the bin, the slice's entries at off, len steps (padded)
+                             // one 32-byte read instead of a unit table -> row offset chain
     double* seg_part;        // per-segment partial sums (2 doubles of room each)
     double* slab_part;       // per SLAB unit: 32 lanes' partial sums (64 doubles of room each)
     uint32_t* seg_ticket;    // per-row tickets of SEGMENT rows (left at 0 after every pass)
@@ -311,17 +315,31 @@ __device__ __forceinline__ void warp_dot2(int s0, int t0, int s1, int t1, const 
 #pragma unroll
         for (int q = 0; q < NV; ++q) acc[h][q] = Acc(0);
     const int n0 = t0 - s0, n1 = t1 - s1, nmax = max(n0, n1);
+    // software-pipelined like the SLAB loop: the next group's indices load with
+    // this group's values and gathers
+    int jn[2][U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int kk = lane + 32 * u;
+        jn[0][u] = kk < n0 ? __ldg(L.idx + s0 + kk) : 0;
+        jn[1][u] = kk < n1 ? __ldg(L.idx + s1 + kk) : 0;
+    }
     for (int k = lane; k < nmax; k += 32 * U) {
         int j[2][U];
         Acc a[2][U];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int kk = k + 32 * u;
-            const bool ok0 = kk < n0, ok1 = kk < n1;
-            j[0][u] = ok0 ? __ldg(L.idx + s0 + kk) : 0;
-            a[0][u] = ok0 ? Acc(__ldg(L.val + s0 + kk)) : Acc(0);
-            j[1][u] = ok1 ? __ldg(L.idx + s1 + kk) : 0;
-            a[1][u] = ok1 ? Acc(__ldg(L.val + s1 + kk)) : Acc(0);
+            j[0][u] = jn[0][u];
+            j[1][u] = jn[1][u];
+            a[0][u] = kk < n0 ? Acc(__ldg(L.val + s0 + kk)) : Acc(0);
+            a[1][u] = kk < n1 ? Acc(__ldg(L.val + s1 + kk)) : Acc(0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int kn = k + 32 * (U + u);
+            jn[0][u] = kn < n0 ? __ldg(L.idx + s0 + kn) : 0;
+            jn[1][u] = kn < n1 ? __ldg(L.idx + s1 + kn) : 0;
         }
 #pragma unroll
         for (int h = 0; h < 2; ++h)
@@ -361,7 +379,7 @@ __device__ __forceinline__ void visit_warp_row_pair(const Bin& b, int u0, int u1
 // SEGMENT: the dot products of segments u0 and u1 (u1 may be past the bin),
 // then each segment's share of its row.
 template <int NV, class Acc, class V, class Epi>
-__device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, int kseg, int rs, int re,
+__device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, int kseg, int nseg,
                                                const Acc (&acc)[NV], const Layout<V>& L, Epi& e);
 
 template <int NV, class Acc, class V, class Gather, class Epi>
@@ -369,28 +387,23 @@ __device__ __forceinline__ void visit_segment_pair(const Bin& b, int u0, int u1,
                                                    const Gather& g, Epi& e) {
     const bool has1 = u1 < b.units;
     const int gs0 = b.aux + u0, gs1 = b.aux + (has1 ? u1 : u0);
-    const int r0 = __ldg(L.seg_row + gs0), k0 = __ldg(L.seg_k + gs0);
-    const int r1 = __ldg(L.seg_row + gs1), k1 = __ldg(L.seg_k + gs1);
-    const int rs0 = __ldg(L.ptr + r0), re0 = __ldg(L.ptr + r0 + 1);
-    const int rs1 = __ldg(L.ptr + r1), re1 = __ldg(L.ptr + r1 + 1);
-    const int s0 = rs0 + k0 * kSegment, t0 = min(re0, s0 + kSegment);
-    const int s1 = rs1 + k1 * kSegment, t1 = has1 ? min(re1, s1 + kSegment) : s1;
+    const int4 a0 = __ldg(L.unit + 2 * gs0), a1 = __ldg(L.unit + 2 * gs1);
+    const int k0 = __ldg(&L.unit[2 * gs0 + 1].x), k1 = __ldg(&L.unit[2 * gs1 + 1].x);
     Acc acc[2][NV];
-    warp_dot2<NV, Acc>(s0, t0, s1, t1, L, g, acc);
+    warp_dot2<NV, Acc>(a0.x, a0.y, a1.x, has1 ? a1.y : a1.x, L, g, acc);
     if ((threadIdx.x & 31) != 0) return;
-    finish_segment<NV, Acc>(b, gs0, r0, k0, rs0, re0, acc[0], L, e);
-    if (has1) finish_segment<NV, Acc>(b, gs1, r1, k1, rs1, re1, acc[1], L, e);
+    finish_segment<NV, Acc>(b, gs0, a0.z, k0, a0.w, acc[0], L, e);
+    if (has1) finish_segment<NV, Acc>(b, gs1, a1.z, k1, a1.w, acc[1], L, e);
 }
 
 // One lane: publish a segment's partial; the row's last segment adds them all.
 template <int NV, class Acc, class V, class Epi>
-__device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, int kseg, int rs, int re,
+__device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, int kseg, int nseg,
                                                const Acc (&acc)[NV], const Layout<V>& L, Epi& e) {
     Acc* part = reinterpret_cast<Acc*>(L.seg_part);
 #pragma unroll
     for (int q = 0; q < NV; ++q) part[(size_t)gseg * NV + q] = acc[q];
     __threadfence();
-    const int nseg = (re - rs + kSegment - 1) / kSegment;
     uint32_t* tk = L.seg_ticket + b.aux2 + (r - b.begin);
     if (atomicAdd(tk, 1u) != (uint32_t)(nseg - 1)) return;
     __threadfence();
@@ -455,22 +468,35 @@ __device__ __forceinline__ void add_segment_rows(T (&tot)[NP], const Layout<V>& 
 template <int NV, class Acc, class V, class Gather, class Epi>
 __device__ __forceinline__ void visit_slab_unit(const Bin& b, int u, const Layout<V>& L, const Gather& g, Epi& e) {
     const int lane = threadIdx.x & 31;
-    const int s = __ldg(L.seg_row + b.aux + u), c = __ldg(L.seg_k + b.aux + u);
-    const int off = __ldg(L.soff + b.slice0 + s);
-    const int len = (__ldg(L.soff + b.slice0 + s + 1) - off) >> 5;
+    const int4 d = __ldg(L.unit + 2 * (b.aux + u));
+    const int off = d.x, len = d.y, s = d.z, c = d.w;
     const int k0 = c * kSlabSteps, k1 = min(len, k0 + kSlabSteps);
+    const int r = b.begin + 32 * s + lane;
+    // the row's epilogue operands, loaded with the unit's entries (the slice's
+    // last unit to finish uses them)
+    typename Epi::Pre pre;
+    if (r < b.end) pre = e.pre(r);
     Acc acc[NV];
 #pragma unroll
     for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
+    // software-pipelined: the next step group's indices are loaded with this
+    // group's values and gathers, so the index -> gather chain costs one round
+    // trip per group instead of two
+    int jn[kUnroll];
+#pragma unroll
+    for (int w = 0; w < kUnroll; ++w) jn[w] = k0 + w < k1 ? __ldg(L.idx + off + 32 * (k0 + w) + lane) : 0;
     for (int k = k0; k < k1; k += kUnroll) {
         int j[kUnroll];
         Acc a[kUnroll];
 #pragma unroll
         for (int w = 0; w < kUnroll; ++w) {
-            const bool ok = k + w < k1;
-            const int p = off + 32 * (k + w) + lane;
-            j[w] = ok ? __ldg(L.idx + p) : 0;
-            a[w] = ok ? Acc(__ldg(L.val + p)) : Acc(0);
+            j[w] = jn[w];
+            a[w] = k + w < k1 ? Acc(__ldg(L.val + off + 32 * (k + w) + lane)) : Acc(0);
+        }
+#pragma unroll
+        for (int w = 0; w < kUnroll; ++w) {
+            const int kn = k + kUnroll + w;
+            jn[w] = kn < k1 ? __ldg(L.idx + off + 32 * kn + lane) : 0;
         }
 #pragma unroll
         for (int w = 0; w < kUnroll; ++w)
@@ -498,9 +524,7 @@ __device__ __forceinline__ void visit_slab_unit(const Bin& b, int u, const Layou
 #pragma unroll
             for (int q = 0; q < NV; ++q) acc[q] += __ldcg(first + (size_t)w * 32 * NV + lane * NV + q);
     }
-    const int r = b.begin + 32 * s + lane;
     if (r >= b.end) return;
-    typename Epi::Pre pre = e.pre(r);
     if constexpr (Epi::NP == 0) {
         e(r, b.kind, acc, pre);
     } else {

@@ -122,7 +122,8 @@ struct Engine : EngineBase {
         BinTable bt{};
         std::vector<int32_t> fptr;      // final CSR offsets (R + 1); SLICED rows hold their bin's start
         std::vector<int32_t> soff;      // slice offsets, one sentinel after each SLICED bin
-        std::vector<int32_t> seg_row, seg_k;
+        std::vector<int32_t> unit;      // SEGMENT / SLAB unit descriptors, 8 ints each (Layout::unit)
+        int32_t units() const { return (int32_t)(unit.size() / 8); }
         int64_t total = 0;              // final index/value array length (with slice padding)
         int32_t ntickets = 0;           // SEGMENT rows and SLAB slices
         int32_t nslots = 0;             // SEGMENT and SLAB rows (epilogue partial slots)
@@ -249,22 +250,27 @@ struct Engine : EngineBase {
                 for (int q = r; q < e; ++q) { P.fptr[q] = (int32_t)off; off += lens[P.perm[q]]; }
                 b.units = e - r;
             } else if (md == BM_SEGMENT) {
-                b.aux = (int32_t)P.seg_row.size();
+                b.aux = P.units();
                 b.aux2 = P.ntickets;
                 b.slot0 = P.nslots;
                 for (int q = r; q < e; ++q) {
                     P.fptr[q] = (int32_t)off;
-                    const int64_t ns = (lens[P.perm[q]] + kSegment - 1) / kSegment;
-                    for (int64_t k = 0; k < ns; ++k) { P.seg_row.push_back(q); P.seg_k.push_back((int32_t)k); }
-                    off += lens[P.perm[q]];
+                    const int64_t len = lens[P.perm[q]];
+                    const int64_t ns = (len + kSegment - 1) / kSegment;
+                    for (int64_t k = 0; k < ns; ++k) {
+                        const int64_t s0 = off + k * kSegment, t0 = std::min(off + len, s0 + kSegment);
+                        const int32_t d[8] = {(int32_t)s0, (int32_t)t0, q, (int32_t)ns, (int32_t)k, 0, 0, 0};
+                        P.unit.insert(P.unit.end(), d, d + 8);
+                    }
+                    off += len;
                 }
-                b.units = (int32_t)P.seg_row.size() - b.aux;
+                b.units = P.units() - b.aux;
                 P.ntickets += e - r;
                 P.nslots += e - r;
             } else {
                 // SLAB: slices of 32 rows padded to their longest row, one unit per
                 // kSlabSteps steps of a slice (units of one slice consecutive)
-                b.aux = (int32_t)P.seg_row.size();
+                b.aux = P.units();
                 b.slice0 = (int32_t)P.soff.size();
                 b.aux2 = P.ntickets;
                 b.slot0 = P.nslots;
@@ -275,12 +281,15 @@ struct Engine : EngineBase {
                     int64_t lmax = 0;
                     for (int t = q; t < std::min(e, q + 32); ++t) lmax = std::max(lmax, lens[P.perm[t]]);
                     P.soff.push_back((int32_t)off);
-                    off += 32 * lmax;
                     const int64_t nu = (lmax + kSlabSteps - 1) / kSlabSteps;
-                    for (int64_t c = 0; c < nu; ++c) { P.seg_row.push_back(s); P.seg_k.push_back((int32_t)c); }
+                    for (int64_t c = 0; c < nu; ++c) {
+                        const int32_t d[8] = {(int32_t)off, (int32_t)lmax, s, (int32_t)c, 0, 0, 0, 0};
+                        P.unit.insert(P.unit.end(), d, d + 8);
+                    }
+                    off += 32 * lmax;
                 }
                 P.soff.push_back((int32_t)off);           // sentinel: end of the bin's last slice
-                b.units = (int32_t)P.seg_row.size() - b.aux;
+                b.units = P.units() - b.aux;
                 P.ntickets += s;
                 P.nslots += e - r;
                 P.nslab_units += b.units;
@@ -318,15 +327,13 @@ struct Engine : EngineBase {
 
     // Final device layout of one orientation from the internal CSR temporaries.
     int build_layout(const Plan& P, int R, const int32_t* tptr, const int32_t* tidx, const V* tval,
-                     Layout<V>& L, int32_t* d_fptr, int32_t* d_soff, int32_t* d_segrow, int32_t* d_segk,
+                     Layout<V>& L, int32_t* d_fptr, int32_t* d_soff, int32_t* d_unit,
                      int32_t* d_idx, V* d_val) {
         SPS_CK(cudaMemcpyAsync(d_fptr, P.fptr.data(), sizeof(int32_t) * (R + 1), cudaMemcpyHostToDevice, st));
         if (!P.soff.empty())
             SPS_CK(cudaMemcpyAsync(d_soff, P.soff.data(), sizeof(int32_t) * P.soff.size(), cudaMemcpyHostToDevice, st));
-        if (!P.seg_row.empty()) {
-            SPS_CK(cudaMemcpyAsync(d_segrow, P.seg_row.data(), sizeof(int32_t) * P.seg_row.size(), cudaMemcpyHostToDevice, st));
-            SPS_CK(cudaMemcpyAsync(d_segk, P.seg_k.data(), sizeof(int32_t) * P.seg_k.size(), cudaMemcpyHostToDevice, st));
-        }
+        if (!P.unit.empty())
+            SPS_CK(cudaMemcpyAsync(d_unit, P.unit.data(), sizeof(int32_t) * P.unit.size(), cudaMemcpyHostToDevice, st));
         for (int i = 0; i < P.bt.nbins; ++i) {
             const Bin& b = P.bt.bin[i];
             if (b.mode == BM_SLICED)
@@ -345,8 +352,7 @@ struct Engine : EngineBase {
         L.idx = d_idx;
         L.val = d_val;
         L.soff = d_soff;
-        L.seg_row = d_segrow;
-        L.seg_k = d_segk;
+        L.unit = reinterpret_cast<const int4*>(d_unit);
         return SPS_OK;
     }
 
@@ -436,12 +442,12 @@ struct Engine : EngineBase {
         const size_t part_row_n = (size_t)std::max(rp.bt.total_blocks, 1) * kRowPartials;
         const size_t part_col_n = (size_t)(cp.bt.total_blocks + tail) * kColPartials;
         const size_t part_aux_n = (size_t)std::max(apply_blocks, kSms * 16) * 3;
-        const size_t nseg = std::max<size_t>(std::max(rp.seg_row.size(), cp.seg_row.size()), 1);
+        const size_t nseg = (size_t)std::max(std::max(rp.units(), cp.units()), 1);
         const size_t ntk = (size_t)std::max(std::max(rp.ntickets, cp.ntickets), 1);
         const size_t nslab = (size_t)std::max(std::max(rp.nslab_units, cp.nslab_units), 1);
         const bool adaptive = mode == SPS_MODE_ADAPTIVE;
         std::vector<std::pair<void**, size_t>> plan;
-        int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx, *d_rsoff, *d_csoff, *d_rseg, *d_rsegk, *d_cseg, *d_csegk;
+        int32_t *d_rptr, *d_ridx, *d_cptr, *d_cidx, *d_rsoff, *d_csoff, *d_runit, *d_cunit;
         V *d_rval, *d_cval, *d_c, *d_b, *d_lo = nullptr, *d_hi = nullptr, *d_tau = nullptr, *d_sigma = nullptr;
         double *d_dr, *d_dc, *d_pr, *d_pc, *d_pa, *d_segpart, *d_slabpart, *d_rowpart_r, *d_rowpart_c;
         double *d_idr = nullptr, *d_idc = nullptr;
@@ -462,14 +468,12 @@ struct Engine : EngineBase {
         add(&d_ridx, sizeof(int32_t) * std::max<int64_t>(rp.total, 1));
         add(&d_rval, sizeof(V) * std::max<int64_t>(rp.total, 1));
         add(&d_rsoff, sizeof(int32_t) * (rp.soff.size() + 1));
-        add(&d_rseg, sizeof(int32_t) * (rp.seg_row.size() + 1));
-        add(&d_rsegk, sizeof(int32_t) * (rp.seg_row.size() + 1));
+        add(&d_runit, sizeof(int32_t) * (rp.unit.size() + 8));
         add(&d_cptr, sizeof(int32_t) * (n + 1));
         add(&d_cidx, sizeof(int32_t) * std::max<int64_t>(cp.total, 1));
         add(&d_cval, sizeof(V) * std::max<int64_t>(cp.total, 1));
         add(&d_csoff, sizeof(int32_t) * (cp.soff.size() + 1));
-        add(&d_cseg, sizeof(int32_t) * (cp.seg_row.size() + 1));
-        add(&d_csegk, sizeof(int32_t) * (cp.seg_row.size() + 1));
+        add(&d_cunit, sizeof(int32_t) * (cp.unit.size() + 8));
         add(&d_segpart, sizeof(double) * 2 * nseg);
         add(&d_slabpart, sizeof(double) * 64 * nslab);
         add(&d_tickets, sizeof(uint32_t) * ntk);
@@ -606,8 +610,8 @@ struct Engine : EngineBase {
 
         // ---- final binned layouts
         Layout<V> Lr{}, Lc{};
-        if (int rc = build_layout(rp, m, t_ptr, t_idx, t_rvV, Lr, d_rptr, d_rsoff, d_rseg, d_rsegk, d_ridx, d_rval)) return rc;
-        if (int rc = build_layout(cp, n, t_cptr, t_cidx, t_cvV, Lc, d_cptr, d_csoff, d_cseg, d_csegk, d_cidx, d_cval)) return rc;
+        if (int rc = build_layout(rp, m, t_ptr, t_idx, t_rvV, Lr, d_rptr, d_rsoff, d_runit, d_ridx, d_rval)) return rc;
+        if (int rc = build_layout(cp, n, t_cptr, t_cidx, t_cvV, Lc, d_cptr, d_csoff, d_cunit, d_cidx, d_cval)) return rc;
         Lr.seg_part = Lc.seg_part = d_segpart;
         Lr.slab_part = Lc.slab_part = d_slabpart;
         Lr.seg_ticket = Lc.seg_ticket = d_tickets;
