@@ -304,6 +304,7 @@ struct AdColCheckEpi {
     // change since the last restart: cone residual^2 of -K^T dy, its bound terms,
     // recession-cone violation^2 of dx, c^T dx
     double p[kColPartials] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    bool nonneg;               // every column in [0, +inf): the bound terms vanish
     using Pre = NoPre;
     static constexpr int NP = kColPartials;
     using R = double;
@@ -311,6 +312,34 @@ struct AdColCheckEpi {
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
     __device__ __forceinline__ Pre pre(int) const { return Pre{}; }
     __device__ __forceinline__ void operator()(int j, int, const double (&acc)[2], const Pre&) {
+        if (nonneg) nonneg_column(j, acc);
+        else general_column(j, acc);
+    }
+    // x >= 0 only (lo = 0, hi = +inf): lambda = max(rc, 0), so the dual residual is
+    // min(rc, 0) and every bound term lo * max(lambda, 0) + hi * min(lambda, 0) is 0;
+    // the same partials as the general case with ~20 fewer FP64 operations per column
+    __device__ __forceinline__ void nonneg_column(int j, const double (&acc)[2]) {
+        const double cj = double(a->c[j]), idc = a->idc[j];
+        atya[j] = V(acc[0]);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const double dres = fmin(cj - acc[q], 0.0);
+            p[5 * q + 0] += dres * dres;
+            const double dor = dres * idc;
+            p[5 * q + 1] += dor * dor;
+            const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
+            p[5 * q + 2] += cj * xv;
+            const double d = xv - double(xl[j]);
+            p[5 * q + 4] += d * d;
+        }
+        const double lv = fmin(double(a->ATYl[j]) - acc[1], 0.0);
+        p[10] += lv * lv;
+        const double dx = double(xc[j]) - double(xl[j]);
+        const double vx = fmin(dx, 0.0);
+        p[12] += vx * vx;
+        p[13] += cj * dx;
+    }
+    __device__ __forceinline__ void general_column(int j, const double (&acc)[2]) {
         const double cj = double(a->c[j]), idc = a->idc[j];
         const double lo = double(lo_at(*a, j)), hi = double(hi_at(*a, j));
         const bool hl = isfinite(lo), hh = isfinite(hi);
@@ -351,6 +380,7 @@ SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
     GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], inv_w};
     AdColCheckEpi<V> e{&a, has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], a.xl, a.ATYa, inv_w};
+    e.nonneg = a.uniform_bounds && a.lo_u == V(0) && isinf(a.hi_u) && a.hi_u > V(0);
     visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e);
     if (!publish_partials<kColPartials>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
     double tc[kColPartials], tr[kRowPartials];
