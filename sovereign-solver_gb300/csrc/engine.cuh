@@ -229,6 +229,7 @@ __device__ __forceinline__ uint64_t global_ns() {
 // All control flow below is warp-uniform, so full-mask shuffles are safe.
 
 constexpr int kUnroll = 8;
+constexpr int kFinishBatch = 8;      // partial loads in flight when a row's (slice's) last unit adds them
 constexpr int kPassMinBlocks = 5;    // resident blocks per SM the iteration kernels are built for
 
 // SLICED: lane t of the warp owns row begin + 32*slice + t.  Two slices per
@@ -413,9 +414,19 @@ __device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, in
     Acc tot[NV];
 #pragma unroll
     for (int q = 0; q < NV; ++q) tot[q] = Acc(0);
-    for (int sg = 0; sg < nseg; ++sg)
+    // the row's segment partials, kFinishBatch loads in flight, added in order
+    for (int s0 = 0; s0 < nseg; s0 += kFinishBatch) {
+        Acc v[kFinishBatch][NV];
 #pragma unroll
-        for (int q = 0; q < NV; ++q) tot[q] += __ldcg(part + (size_t)(first + sg) * NV + q);
+        for (int w = 0; w < kFinishBatch; ++w)
+#pragma unroll
+            for (int q = 0; q < NV; ++q)
+                v[w][q] = s0 + w < nseg ? __ldcg(part + (size_t)(first + s0 + w) * NV + q) : Acc(0);
+#pragma unroll
+        for (int w = 0; w < kFinishBatch; ++w)
+#pragma unroll
+            for (int q = 0; q < NV; ++q) tot[q] += v[w][q];
+    }
     if constexpr (Epi::NP == 0) {
         e(r, b.kind, tot, pre);
     } else {
@@ -520,9 +531,19 @@ __device__ __forceinline__ void visit_slab_unit(const Bin& b, int u, const Layou
         const Acc* first = reinterpret_cast<const Acc*>(L.slab_part) + (size_t)(b.part0 + u - c) * 32 * NV;
 #pragma unroll
         for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
-        for (int w = 0; w < nunits; ++w)
+        // the slice's unit partials, kFinishBatch loads in flight, added in unit order
+        for (int w0 = 0; w0 < nunits; w0 += kFinishBatch) {
+            Acc v[kFinishBatch][NV];
 #pragma unroll
-            for (int q = 0; q < NV; ++q) acc[q] += __ldcg(first + (size_t)w * 32 * NV + lane * NV + q);
+            for (int w = 0; w < kFinishBatch; ++w)
+#pragma unroll
+                for (int q = 0; q < NV; ++q)
+                    v[w][q] = w0 + w < nunits ? __ldcg(first + (size_t)(w0 + w) * 32 * NV + lane * NV + q) : Acc(0);
+#pragma unroll
+            for (int w = 0; w < kFinishBatch; ++w)
+#pragma unroll
+                for (int q = 0; q < NV; ++q) acc[q] += v[w][q];
+        }
     }
     if (r >= b.end) return;
     if constexpr (Epi::NP == 0) {
