@@ -53,7 +53,7 @@ struct Bin {
     int32_t aux2;            // SEGMENT: first per-row ticket; SLAB: first per-slice ticket
     int32_t slice0;          // SLAB: first global slice
     int32_t part0;           // SLAB: first unit in the layout's SLAB partials
-    int32_t slot0;           // SEGMENT / SLAB: first row slot of epilogue partials
+    int32_t slot0;           // SEGMENT: first row slot of epilogue partials; SLAB: first slice slot
 };
 
 struct BinTable {
@@ -77,8 +77,8 @@ struct Layout {
     double* seg_part;        // per-segment partial sums (2 doubles of room each)
     double* slab_part;       // per SLAB unit: 32 lanes' partial sums (64 doubles of room each)
     uint32_t* seg_ticket;    // per-row tickets of SEGMENT rows (left at 0 after every pass)
-    double* seg_rowpart;     // per SEGMENT / SLAB row: its epilogue's reduction partials
-    int32_t nsegrows;        // SEGMENT and SLAB rows (slots) of this orientation
+    double* seg_rowpart;     // per SEGMENT row / SLAB slice: its epilogue's reduction partials
+    int32_t nsegrows;        // epilogue slots of this orientation (SEGMENT rows, SLAB slices)
 };
 
 constexpr int kMaxEpiPartials = 14;
@@ -474,8 +474,9 @@ __device__ __forceinline__ void add_segment_rows(T (&tot)[NP], const Layout<V>& 
 // SLAB: unit u of the bin = steps [c S, min(L, (c+1) S)) of slice s (S =
 // kSlabSteps, L = the slice's padded length); lane t accumulates row t of the
 // slice.  A slice with more than one unit is finished by the unit that takes
-// the slice's ticket last: it adds the units' partials in unit order.  Every
-// row's epilogue partials go to its own slot (units finish in varying order).
+// the slice's ticket last: it adds the units' partials in unit order.  The
+// slice's epilogue partials go to the slice's own slot (units finish in
+// varying order, slots are summed in order by the kernel's last block).
 template <int NV, class Acc, class V, class Gather, class Epi>
 __device__ __forceinline__ void visit_slab_unit(const Bin& b, int u, const Layout<V>& L, const Gather& g, Epi& e) {
     const int lane = threadIdx.x & 31;
@@ -545,15 +546,24 @@ __device__ __forceinline__ void visit_slab_unit(const Bin& b, int u, const Layou
                 for (int q = 0; q < NV; ++q) acc[q] += v[w][q];
         }
     }
-    if (r >= b.end) return;
     if constexpr (Epi::NP == 0) {
-        e(r, b.kind, acc, pre);
+        if (r < b.end) e(r, b.kind, acc, pre);
     } else {
+        // the slice's 32 rows' epilogue partials, added over the warp in a fixed
+        // butterfly order (lanes past the bin add zeros): one slot per slice
         using R = typename Epi::R;
         Epi one = e;
         one.zero();
-        one(r, b.kind, acc, pre);
-        one.export_to(reinterpret_cast<R*>(L.seg_rowpart) + (size_t)(b.slot0 + (r - b.begin)) * Epi::NP);
+        if (r < b.end) one(r, b.kind, acc, pre);
+        R v[Epi::NP];
+        one.export_to(v);
+#pragma unroll
+        for (int q = 0; q < Epi::NP; ++q) v[q] = group_sum<32>(v[q]);
+        if (lane == 0) {
+            R* slot = reinterpret_cast<R*>(L.seg_rowpart) + (size_t)(b.slot0 + s) * Epi::NP;
+#pragma unroll
+            for (int q = 0; q < Epi::NP; ++q) slot[q] = v[q];
+        }
     }
 }
 

@@ -126,7 +126,7 @@ struct Engine : EngineBase {
         int32_t units() const { return (int32_t)(unit.size() / 8); }
         int64_t total = 0;              // final index/value array length (with slice padding)
         int32_t ntickets = 0;           // SEGMENT rows and SLAB slices
-        int32_t nslots = 0;             // SEGMENT and SLAB rows (epilogue partial slots)
+        int32_t nslots = 0;             // epilogue partial slots: SEGMENT rows, SLAB slices
         int32_t nslab_units = 0;
     };
 
@@ -291,7 +291,7 @@ struct Engine : EngineBase {
                 P.soff.push_back((int32_t)off);           // sentinel: end of the bin's last slice
                 b.units = P.units() - b.aux;
                 P.ntickets += s;
-                P.nslots += e - r;
+                P.nslots += s;                             // one epilogue slot per slice
                 P.nslab_units += b.units;
             }
             bin_store.push_back(off - bin_off0);
