@@ -312,12 +312,17 @@ struct Engine : EngineBase {
             work[i] = double(bin_store[i]) + 32.0 * b.units;
             work_total += work[i];
         }
+        // When every bin's need fits the wave, every bin gets it (one step per
+        // warp); a proportional share here left a few warps two units in a row
+        // and the pass waited for them.
         const int64_t budget = std::min<int64_t>(block_cap, need_total);
         int blocks = 0;
         for (int i = 0; i < P.bt.nbins; ++i) {
             Bin& b = P.bt.bin[i];
             const int64_t need = blocks_needed(b);
-            const int64_t share = (int64_t)std::ceil(budget * work[i] / std::max(work_total, 1.0));
+            const int64_t share = need_total <= block_cap
+                                      ? need
+                                      : (int64_t)std::ceil(budget * work[i] / std::max(work_total, 1.0));
             b.nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(need, share));
             b.block_begin = blocks;
             blocks += b.nblocks;
