@@ -51,8 +51,9 @@ struct Bin {
     int32_t units;           // slices (SLICED), rows (WARP), segments (SEGMENT) or units (SLAB)
     int32_t aux;             // SLICED: first global slice; SEGMENT / SLAB: first global unit
     int32_t aux2;            // SEGMENT: first per-row ticket; SLAB: first per-slice ticket
-    int32_t slice0;          // SLAB: first global slice
-    int32_t part0;           // SLAB: first unit in the layout's SLAB partials
+    int32_t slice0;          // SLAB: first global slice; SLICED with uniform length: the bin's offset
+    int32_t part0;           // SLAB: first unit in the layout's SLAB partials; SLICED: the uniform
+                             // row length of every slice (0 = lengths vary, read soff)
     int32_t slot0;           // SEGMENT: first row slot of epilogue partials; SLAB: first slice slot
 };
 
@@ -245,8 +246,13 @@ __device__ __forceinline__ void visit_slice_pair(const Bin& b, int s0, int s1, c
     for (int h = 0; h < 2; ++h) {
         const int s = h ? (has1 ? s1 : s0) : s0;
         const int gs = b.aux + s;
-        off[h] = __ldg(L.soff + gs);
-        len[h] = (h && !has1) ? 0 : ((__ldg(L.soff + gs + 1) - off[h]) >> 5);
+        if (b.part0 > 0) {                 // every slice of the bin has part0 steps: no offset reads
+            off[h] = b.slice0 + s * 32 * b.part0;
+            len[h] = (h && !has1) ? 0 : b.part0;
+        } else {
+            off[h] = __ldg(L.soff + gs);
+            len[h] = (h && !has1) ? 0 : ((__ldg(L.soff + gs + 1) - off[h]) >> 5);
+        }
         r[h] = b.begin + s * 32 + lane;
         if (r[h] < b.end && (h == 0 || has1)) pre[h] = e.pre(r[h]);
     }

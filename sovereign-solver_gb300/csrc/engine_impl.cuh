@@ -239,6 +239,11 @@ struct Engine : EngineBase {
             const int64_t bin_off0 = off;
             if (md == BM_SLICED) {
                 b.aux = (int32_t)P.soff.size();
+                // rows sorted by decreasing length: first == last means one length
+                if (lens[P.perm[r]] == lens[P.perm[e - 1]] && lens[P.perm[r]] > 0) {
+                    b.slice0 = (int32_t)off;
+                    b.part0 = (int32_t)lens[P.perm[r]];
+                }
                 for (int q = r; q < e; ++q) P.fptr[q] = (int32_t)off;
                 for (int s = r; s < e; s += 32) {
                     P.soff.push_back((int32_t)off);
