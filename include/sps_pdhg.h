@@ -196,7 +196,8 @@ typedef struct {
     double  solve_ms;           /* the persistent launch plus the continuations after it */
     int64_t total_iterations;   /* sum over instances */
     int32_t optimal;            /* instances that reached tol */
-    int32_t lanes_per_column;   /* schedule used (autotuned or given) */
+    int32_t lanes_per_column;   /* schedule used: given, autotuned at create, or taken from an
+                                   earlier batch of the same shape in this process */
     int32_t blocks;             /* persistent blocks */
     int32_t escalated;          /* instances that stalled in FP32 and were finished in FP64 by the
                                    single-LP engine after the persistent launch (in solve_ms) */

@@ -13,7 +13,9 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <map>
 #include <memory>
+#include <mutex>
 #include <cmath>
 #include <cstring>
 #include <numeric>
@@ -919,6 +921,21 @@ int continue_single(sps_batch* b, int32_t k, double used_s, std::string* why) {
 
 }  // namespace
 
+// Autotuned schedules, kept for the process by a coarse shape of the batch, so
+// a caller that creates many similar batches (the children of every node of a
+// branch-and-bound search, a repeated workload) times the candidates once:
+// device, cluster size, given lanes per column (0 = tuned), and half-octave
+// buckets of the instance count, the mean nonzeros per column and per row, and
+// the largest instance.
+struct ScheduleKey {
+    int32_t v[7];
+    bool operator<(const ScheduleKey& o) const { return std::lexicographical_compare(v, v + 7, o.v, o.v + 7); }
+};
+static std::mutex g_schedule_mu;
+static std::map<ScheduleKey, std::pair<int32_t, int32_t>> g_schedules;
+
+static int32_t half_octave(double x) { return x > 0.0 ? (int32_t)std::floor(2.0 * std::log2(x)) : -1000; }
+
 extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, const sps_options* opt_in,
                                 sps_batch** out) {
     if (!out || count <= 0 || !probs) {
@@ -1181,6 +1198,22 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
     // schedule: lanes per column given (batch_group) or timed; lanes per row timed
     // second with the chosen column schedule (32 attempts and one check per
     // candidate on a sample of the largest instances)
+    ScheduleKey key{};
+    {
+        int64_t nz = 0, nn = 0, mm = 0, big = 0;
+        for (const Inst& I : b->inst) { nz += I.nnz; nn += I.n; mm += I.m; big = std::max<int64_t>(big, I.nnz); }
+        key = ScheduleKey{{opt.device, b->team, opt.batch_group, half_octave(double(count)),
+                           half_octave(nn ? double(nz) / double(nn) : 0.0), half_octave(mm ? double(nz) / double(mm) : 0.0),
+                           half_octave(double(big))}};
+        std::lock_guard<std::mutex> lk(g_schedule_mu);
+        auto it = g_schedules.find(key);
+        if (it != g_schedules.end()) {
+            b->G = it->second.first;
+            b->Gr = it->second.second;
+            *out = b.release();
+            return SPS_OK;
+        }
+    }
     {
         sps_batch* bb = bp;
         // A sample spread over the whole size range (every stride-th instance of the
@@ -1232,6 +1265,8 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         }
         bb->G = gc;
         bb->Gr = gr;
+        std::lock_guard<std::mutex> lk(g_schedule_mu);
+        g_schedules[key] = {gc, gr};
     }
     *out = b.release();
     return SPS_OK;
