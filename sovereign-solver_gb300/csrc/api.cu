@@ -6,6 +6,7 @@
 #include <cstring>
 #include <memory>
 #include <string>
+#include <thread>
 
 #include "engine_impl.cuh"
 
@@ -13,10 +14,13 @@ using namespace sps;
 
 // A caller problem copied into owned storage (the descriptor's arrays are only
 // valid during sps_create); kept when a stalled FP32 solve may continue in FP64.
+// The caller's problem kept for an FP64 continuation (the caller's buffers are
+// not retained): its constraint arrays and right-hand sides; c, lb and ub
+// point at the engine's own copies.
 struct ProblemCopy {
     sps_problem_desc d{};
     std::vector<int32_t> ubp, ubi, eqp, eqi;
-    std::vector<double> ubv, eqv, c, bub, beq, lb, ub;
+    std::vector<double> ubv, eqv, bub, beq;
 };
 
 struct sps_handle {
@@ -173,7 +177,7 @@ void build_standard(const sps_problem_desc* d, HostProblem& hp, StdMap& s) {
     hp.ub = hp.own_ub.data();
 }
 
-std::unique_ptr<ProblemCopy> copy_problem(const sps_problem_desc* d) {
+std::unique_ptr<ProblemCopy> copy_problem(const sps_problem_desc* d, const EngineBase* e) {
     auto p = std::make_unique<ProblemCopy>();
     const int64_t nub = d->m_ub ? d->ub_indptr[d->m_ub] : 0, neq = d->m_eq ? d->eq_indptr[d->m_eq] : 0;
     auto take = [](auto& v, const auto* src, int64_t len) {
@@ -181,17 +185,21 @@ std::unique_ptr<ProblemCopy> copy_problem(const sps_problem_desc* d) {
         return v.empty() ? nullptr : v.data();
     };
     p->d = *d;
-    p->d.ub_indptr = take(p->ubp, d->ub_indptr, d->m_ub ? d->m_ub + 1 : 0);
-    p->d.ub_indices = take(p->ubi, d->ub_indices, nub);
-    p->d.ub_values = take(p->ubv, d->ub_values, nub);
-    p->d.eq_indptr = take(p->eqp, d->eq_indptr, d->m_eq ? d->m_eq + 1 : 0);
-    p->d.eq_indices = take(p->eqi, d->eq_indices, neq);
+    // the nonzero arrays (tens of MB on large LPs) on their own threads
+    std::thread t1([&] { p->d.ub_indices = take(p->ubi, d->ub_indices, nub); });
+    std::thread t2([&] { p->d.ub_values = take(p->ubv, d->ub_values, nub); });
+    std::thread t3([&] { p->d.eq_indices = take(p->eqi, d->eq_indices, neq); });
     p->d.eq_values = take(p->eqv, d->eq_values, neq);
-    p->d.c = take(p->c, d->c, d->n);
+    p->d.ub_indptr = take(p->ubp, d->ub_indptr, d->m_ub ? d->m_ub + 1 : 0);
+    p->d.eq_indptr = take(p->eqp, d->eq_indptr, d->m_eq ? d->m_eq + 1 : 0);
     p->d.b_ub = take(p->bub, d->b_ub, d->m_ub);
     p->d.b_eq = take(p->beq, d->b_eq, d->m_eq);
-    p->d.lb = take(p->lb, d->lb, d->n);
-    p->d.ub = take(p->ub, d->ub, d->n);
+    p->d.c = e->c_user.empty() ? nullptr : e->c_user.data();
+    p->d.lb = e->lb_user.empty() ? nullptr : e->lb_user.data();
+    p->d.ub = e->ub_user.empty() ? nullptr : e->ub_user.data();
+    t1.join();
+    t2.join();
+    t3.join();
     return p;
 }
 
@@ -290,7 +298,6 @@ int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_hand
 
     sps_handle* h = new sps_handle();
     h->opt = opt;
-    if (opt.mode == SPS_MODE_ADAPTIVE && opt.precision == SPS_FP32 && opt.escalate == 1) h->copy = copy_problem(prob);
     h->eng = opt.precision == SPS_FP32 ? make_engine_f32() : make_engine_f64();
     EngineBase* e = h->eng;
     e->n_user = prob->n;
@@ -298,6 +305,7 @@ int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_hand
     e->c_user.assign(prob->c, prob->c + prob->n);
     e->lb_user.assign(prob->lb, prob->lb + prob->n);
     e->ub_user.assign(prob->ub, prob->ub + prob->n);
+    if (opt.mode == SPS_MODE_ADAPTIVE && opt.precision == SPS_FP32 && opt.escalate == 1) h->copy = copy_problem(prob, e);
     e->smap = sm;
     const int rc = opt.precision == SPS_FP32 ? setup_f32(e, hp, opt, opt.mode) : setup_f64(e, hp, opt, opt.mode);
     if (rc != SPS_OK) {
