@@ -215,22 +215,33 @@ struct Engine : EngineBase {
                                             : kSliceMax + (md == BM_WARP ? 1 : md == BM_SEGMENT ? 2 : 3);
             return kind_of(i) * NB + sub;
         };
+        // each row's bucket once (the sort and the bin boundaries read it again)
+        std::vector<uint8_t> bk(R);
+        for (int i = 0; i < R; ++i) bk[i] = (uint8_t)bucket(i);
         std::vector<int64_t> cnt(2 * NB + 1, 0);
-        for (int i = 0; i < R; ++i) cnt[bucket(i) + 1]++;
+        for (int i = 0; i < R; ++i) cnt[bk[i] + 1]++;
         for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] += cnt[b];
         P.perm.assign(R, 0);
         {
             std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
-            for (int i = 0; i < R; ++i) P.perm[pos[bucket(i)]++] = i;
+            for (int i = 0; i < R; ++i) P.perm[pos[bk[i]]++] = i;
         }
+        // (kind, schedule) of a bucket: rows of one bin are consecutive buckets
+        auto bin_of = [&](int bucket_id) {
+            const int kd = bucket_id / NB, sub = bucket_id % NB;
+            return kd * 4 + (sub <= kSliceMax ? (int)BM_SLICED : sub == kSliceMax + 1 ? (int)BM_WARP
+                                              : sub == kSliceMax + 2 ? (int)BM_SEGMENT : (int)BM_SLAB);
+        };
         P.fptr.assign(R + 1, 0);
         P.bt = BinTable{};
         int64_t off = 0;
         std::vector<int64_t> bin_store;              // stored entries per bin
         for (int r = 0; r < R;) {
             const int kd = kind_of(P.perm[r]), md = mode_at(P.perm[r]);
+            const int key = bin_of(bk[P.perm[r]]);
+            // the bin ends at the first row of another (kind, schedule): jump bucket by bucket
             int e = r;
-            while (e < R && kind_of(P.perm[e]) == kd && mode_at(P.perm[e]) == md) ++e;
+            for (int q = bk[P.perm[r]]; q < 2 * NB && bin_of(q) == key; ++q) e = (int)cnt[q + 1];
             Bin b{};
             b.begin = r;
             b.end = e;
@@ -630,20 +641,17 @@ struct Engine : EngineBase {
         Lr.nsegrows = rp.nslots;
         Lc.nsegrows = cp.nslots;
 
-        // ---- vectors in internal order
+        // ---- vectors in internal order (uploaded in the caller's order, permuted on the device)
         {
-            std::vector<double> ci(n), li(n), ui(n), bi(m);
-            for (int j = 0; j < n; ++j) { const int o = perm_col[j]; ci[j] = hp.c[o]; li[j] = hp.lb[o]; ui[j] = hp.ub[o]; }
-            for (int r = 0; r < m; ++r) bi[r] = hp.rhs[perm_row[r]];
             double *t_c, *t_l, *t_u, *t_b;
             SPS_CK(cudaMallocAsync(&t_c, sizeof(double) * (3 * (size_t)n + m), st));
             t_l = t_c + n; t_u = t_l + n; t_b = t_u + n;
-            SPS_CK(cudaMemcpyAsync(t_c, ci.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
-            SPS_CK(cudaMemcpyAsync(t_l, li.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
-            SPS_CK(cudaMemcpyAsync(t_u, ui.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st));
-            SPS_CK(cudaMemcpyAsync(t_b, bi.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
-            k_scale_vectors<V><<<grid_for(std::max(n, m)), kBlock, 0, st>>>(t_c, t_l, t_u, t_b, d_dc, d_dr, d_c,
-                                                                           d_lo, d_hi, d_b, n, m);
+            SPS_CK(cudaMemcpyAsync(t_c, hp.c, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(t_l, hp.lb, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(t_u, hp.ub, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+            SPS_CK(cudaMemcpyAsync(t_b, hp.rhs.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st));
+            k_scale_vectors<V><<<grid_for(std::max(n, m)), kBlock, 0, st>>>(t_c, t_l, t_u, t_b, d_perm_col, d_perm_row,
+                                                                           d_dc, d_dr, d_c, d_lo, d_hi, d_b, n, m);
             if (d_idc) k_reciprocals<<<grid_for(std::max(n, m)), kBlock, 0, st>>>(d_dc, d_dr, d_idc, d_idr, n, m);
             SPS_CK(cudaGetLastError());
             SPS_CK(cudaStreamSynchronize(st));

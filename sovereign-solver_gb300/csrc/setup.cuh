@@ -185,23 +185,26 @@ __global__ void k_fill_rows(const int32_t* __restrict__ tptr, const int32_t* __r
     }
 }
 
-// Scaled vectors from FP64 inputs already in internal order:
+// Scaled vectors in internal order from FP64 inputs in the caller's order
+// (gathered through the permutations on the device):
 //   c~ = c*dc, l~ = l/dc, u~ = u/dc (columns);  b~ = b*dr (rows).
 template <class V>
 __global__ void k_scale_vectors(const double* __restrict__ c, const double* __restrict__ lb,
                                 const double* __restrict__ ub, const double* __restrict__ b,
+                                const int32_t* __restrict__ perm_col, const int32_t* __restrict__ perm_row,
                                 const double* __restrict__ dc, const double* __restrict__ dr,
                                 V* __restrict__ cs, V* __restrict__ los, V* __restrict__ his,
                                 V* __restrict__ bs, int32_t n, int32_t m) {
     const int stride = gridDim.x * blockDim.x;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
-        cs[j] = V(c[j] * dc[j]);
+        const int o = perm_col[j];
+        cs[j] = V(c[o] * dc[j]);
         if (los) {
-            los[j] = V(lb[j] / dc[j]);
-            his[j] = V(ub[j] / dc[j]);
+            los[j] = V(lb[o] / dc[j]);
+            his[j] = V(ub[o] / dc[j]);
         }
     }
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) bs[i] = V(b[i] * dr[i]);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) bs[i] = V(b[perm_row[i]] * dr[i]);
 }
 
 // Reciprocal scale factors (FP64) for the adaptive checks, which multiply by them.
