@@ -577,17 +577,23 @@ def run_warmstart(args, rank, world):
     return line
 
 
-def branching_node(args, rank):
-    """Config 5: the set-covering MILP node, its LP relaxation solved to 1e-6 on the
-    GPU (outside every timed region), the strong-branching candidates and the
-    2K child problems (down_0, up_0, down_1, ...)."""
+def branching_node(args, rank, on_cpu=False):
+    """Config 5: the set-covering MILP node, its LP relaxation (solved to 1e-6 on
+    the GPU, or by the oracle's simplex for the CPU reference arm; outside every
+    timed region), the strong-branching candidates and the 2K child problems
+    (down_0, up_0, down_1, ...)."""
     import sovereign_solver_gb300 as sps
     import sovereign_solver_gb300.branching as br
     import sovereign_solver_gb300.workloads as wl
     p, _ = wl.set_cover_milp(seed=args.seed + rank)
     relax = sps.Problem(c=p.c, A_ub=p.A_ub, b_ub=p.b_ub, A_eq=p.A_eq, b_eq=p.b_eq, lb=p.lb, ub=p.ub,
                         integer_mask=np.zeros(p.n_vars, dtype=bool))
-    lp = sps.solve_lp_pdhg(relax, tol=1e-6, device=args.device)
+    if on_cpu:
+        from oracle import simplex
+        r = simplex.solve(relax)
+        lp = sps.SolveResult(r.status, r.x, r.objective, r.iterations, y=np.zeros(p.n_ineq + p.n_eq))
+    else:
+        lp = sps.solve_lp_pdhg(relax, tol=1e-6, device=args.device)
     top = br.strong_candidates(lp.x, p.integer_mask)
     kids = []
     for j in top:
@@ -780,7 +786,7 @@ def run_reference_batch(args, world):
 def run_reference_branching(args, world):
     """Reference arm of the strong-branching workload: one simplex solve per
     child (the reference's _lp_gain loop) on a budgeted sample per step."""
-    _, lp, top, kids = branching_node(args, 0)
+    _, lp, top, kids = branching_node(args, 0, on_cpu=True)
     for _ in range(max(1, args.warmup // 3)):
         branching_cpu_baseline(kids[:1], lp.objective, 0.0)
     vals = [branching_cpu_baseline(kids, lp.objective, args.cpu_budget) for _ in range(args.steps)]
