@@ -20,6 +20,13 @@ class Solver:
         self.problem: Optional[Problem] = None
         self._result = None
 
+    def read_mps(self, path) -> "Solver":
+        """Load a problem from an MPS file (``solver/solver.py:41-44``); returns
+        self for chaining, without validating, as the reference does."""
+        from .mps import read_mps as _read_mps
+        self.problem = _read_mps(path)
+        return self
+
     def set_problem(self, problem) -> "Solver":
         problem.validate()
         self.problem = problem

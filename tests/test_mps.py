@@ -102,3 +102,17 @@ def test_synthetic_file(tmp_path):
         assert bu == b
     np.testing.assert_array_equal(p.A_eq.toarray(), [[0, 1, 0]])
     np.testing.assert_array_equal(p.b_eq, [2.0])
+
+
+def test_solver_read_mps_chains(tmp_path):
+    """``Solver().read_mps(path)`` loads the file's LP and returns the solver
+    (the reference's loader, ``solver/solver.py:41-44``)."""
+    from sovereign_solver_gb300 import Solver
+    f = tmp_path / "toy.mps"
+    f.write_text(SYNTHETIC)
+    s = Solver()
+    assert s.read_mps(f) is s
+    q = read_mps(f)
+    np.testing.assert_array_equal(s.problem.c, q.c)
+    np.testing.assert_array_equal(s.problem.A_ub.toarray(), q.A_ub.toarray())
+    assert s.problem.sense == "max"
