@@ -331,15 +331,43 @@ struct Engine : EngineBase {
         // When every bin's need fits the wave, every bin gets it (one step per
         // warp); a proportional share here left a few warps two units in a row
         // and the pass waited for them.
+        // Otherwise the shares are rounded down (at least one block, at most the
+        // need) and the blocks left go to the largest remainders, so the bins
+        // add up to the wave: rounding every share up put up to one block per
+        // bin past it, and those blocks waited for a free slot.
         const int64_t budget = std::min<int64_t>(block_cap, need_total);
+        const int nb = P.bt.nbins;
+        std::vector<int64_t> share(nb), need(nb);
+        std::vector<double> raw(nb);
+        int64_t sum = 0;
+        for (int i = 0; i < nb; ++i) {
+            need[i] = blocks_needed(P.bt.bin[i]);
+            raw[i] = budget * work[i] / std::max(work_total, 1.0);
+            share[i] = need_total <= block_cap
+                           ? need[i]
+                           : std::max<int64_t>(1, std::min<int64_t>(need[i], (int64_t)std::floor(raw[i])));
+            sum += share[i];
+        }
+        while (sum < budget) {
+            int best = -1;
+            for (int i = 0; i < nb; ++i)
+                if (share[i] < need[i] && (best < 0 || raw[i] - share[i] > raw[best] - share[best])) best = i;
+            if (best < 0) break;
+            ++share[best];
+            ++sum;
+        }
+        while (sum > budget) {            // one-block floors of small bins: take from the largest share
+            int best = -1;
+            for (int i = 0; i < nb; ++i)
+                if (share[i] > 1 && (best < 0 || share[i] > share[best])) best = i;
+            if (best < 0) break;
+            --share[best];
+            --sum;
+        }
         int blocks = 0;
-        for (int i = 0; i < P.bt.nbins; ++i) {
+        for (int i = 0; i < nb; ++i) {
             Bin& b = P.bt.bin[i];
-            const int64_t need = blocks_needed(b);
-            const int64_t share = need_total <= block_cap
-                                      ? need
-                                      : (int64_t)std::ceil(budget * work[i] / std::max(work_total, 1.0));
-            b.nblocks = (int)std::max<int64_t>(1, std::min<int64_t>(need, share));
+            b.nblocks = (int)share[i];
             b.block_begin = blocks;
             blocks += b.nblocks;
         }

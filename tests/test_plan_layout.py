@@ -233,3 +233,20 @@ def test_uniform_short_rows_compute_offsets(plan_tool, tmp_path):
     P = run_plan(plan_tool, str(tmp_path), ptr, np.concatenate(rows), [0] * 300, 120, np.arange(120), 760)
     assert P["bins"][0][2] == SLICED and P["bins"][0][10] == 2
     check_plan(plan_tool, str(tmp_path), ptr, np.concatenate(rows), [0] * 300, 120, np.arange(120))
+
+
+@pytest.mark.parametrize("cap", [8, 9, 11, 12, 13])
+def test_block_shares_fit_the_cap(plan_tool, tmp_path, cap):
+    """Eight bins (four schedules x two row kinds) sharing fewer blocks than
+    they need (14 blocks): the proportional shares add up to the cap, never past
+    it (each block past one resident wave waits for a free slot)."""
+    rng = np.random.default_rng(1)
+    rows = [r + 50 * np.arange(int(rng.integers(40, 90))) for r in range(100)]
+    rows += [np.sort(rng.choice(6000, int(rng.integers(33, 1500)), replace=False)) for _ in range(50)]
+    rows += [np.sort(rng.choice(6000, int(rng.integers(1, 33)), replace=False)) for _ in range(70)]
+    ptr = np.cumsum([0] + [len(r) for r in rows])
+    idx = np.concatenate(rows)
+    kind = list(rng.integers(0, 2, len(rows)))
+    P = run_plan(plan_tool, str(tmp_path), ptr, idx, kind, 6000, np.arange(6000), cap)
+    assert len(P["bins"]) == 8 and P["total_blocks"] == cap
+    check_plan(plan_tool, str(tmp_path), ptr, idx, kind, 6000, np.arange(6000), cap=cap)
