@@ -95,7 +95,10 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------- workloads
-def make_workload(config: int, seed: int):
+def make_workload(config: int, seed: int, powerlaw_nnz: int = 20_000_000):
+    """The single-LP workloads.  ``powerlaw_nnz``: nonzero count the power-law
+    LP's Zipf(1.5) row lengths are rescaled to; 0 keeps the lengths as drawn
+    (clipped to [2, 5000]: about 1.1e8 nonzeros at m = 1M)."""
     import sovereign_solver_gb300.workloads as wl
     if config == 0:
         p, info = wl.planted_lp(seed=seed)
@@ -105,8 +108,10 @@ def make_workload(config: int, seed: int):
         return p, info, {"workload": "transportation LP 1000 sources x 2000 sinks (n=2M, m=3000, nnz=4M)",
                          "seed": seed}
     if config == 2:
-        p, info = wl.powerlaw_lp(seed=seed)
-        return p, info, {"workload": f"power-law LP m=1M n=2M Zipf(1.5) rows, nnz={p.A_eq.nnz}", "seed": seed}
+        p, info = wl.powerlaw_lp(seed=seed, target_nnz=powerlaw_nnz or None)
+        rows = f"rescaled to ~{powerlaw_nnz / 1e6:g}M nnz" if powerlaw_nnz else "lengths as drawn"
+        return p, info, {"workload": f"power-law LP m=1M n=2M Zipf(1.5) rows ({rows}), nnz={p.A_eq.nnz}",
+                         "seed": seed}
     raise SystemExit(f"unknown config {config}")
 
 
@@ -137,9 +142,11 @@ def problem_bytes(p) -> int:
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum per launch of the iteration kernels,
-# from one ncu capture of the default workload (transportation LP 1000 x 2000,
-# seed 0, FP32 adaptive; --graph-mode 0 so the kernels are separate launches).
-MEASURED_TRAFFIC = {1: {"row": 40.42e6 + 0.00e6, "col": 64.09e6 + 1.32e6}}
+# from one ncu capture per workload (seed 0, FP32 adaptive; --graph-mode 0 so the
+# kernels are separate launches): the transportation LP 1000 x 2000 and the
+# power-law LP rescaled to ~20M nonzeros.
+MEASURED_TRAFFIC = {1: {"row": 40.42e6 + 0.00e6, "col": 64.09e6 + 1.32e6},
+                    2: {"row": 189.1e6 + 9.1e6, "col": 228.3e6 + 15.1e6}}
 
 
 def iteration_bytes(p) -> dict:
@@ -206,7 +213,7 @@ def run_ours(args, rank, world):
     import sovereign_solver_gb300 as sps
     from sovereign_solver_gb300 import _native as N, pdhg
 
-    p, info, cfg = make_workload(args.config, seed=args.seed + rank)
+    p, info, cfg = make_workload(args.config, seed=args.seed + rank, powerlaw_nnz=args.powerlaw_nnz)
     hbm, peak_kind = peaks()
     eng = sps.PDHGEngine(p, tol=args.tol, max_iters=args.max_iters, device=args.device,
                          graph_mode=args.graph_mode)
@@ -292,7 +299,9 @@ def run_ours(args, rank, world):
         "roofline": {"bound": "hbm", "kernel": f"ad_{dom}_step (fused {'CSC' if dom == 'col' else 'CSR'} SpMV + update)",
                      "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_kind": peak_kind, "algorithmic_bytes": ib[dom],
-                     "traffic": MEASURED_TRAFFIC.get(args.config, {}).get(dom) if args.seed == 0 else None,
+                     "traffic": (MEASURED_TRAFFIC.get(args.config, {}).get(dom)
+                                 if args.seed == 0 and (args.config != 2 or args.powerlaw_nnz == 20_000_000)
+                                 else None),
                      "other_pass_gbs": (ib["row" if dom == "col" else "col"] /
                                         ((kt[0] if dom == "col" else kt[1]) / 1e3) / 1e9)},
         "clocks": clk.summary(),
@@ -729,7 +738,7 @@ def run_reference(args, rank, world):
         cfg = {"workload": "transportation family 200x400, held-out seed 10000000 (one cold solve per step)"}
         ref_key = f"4:{TEST_SEED0}"
     else:
-        p, info, cfg = make_workload(args.config, seed=args.seed)
+        p, info, cfg = make_workload(args.config, seed=args.seed, powerlaw_nnz=args.powerlaw_nnz)
         ref_key = args.config
     for _ in range(args.warmup):
         reference_sample(p, min(2.0, args.cpu_budget))
@@ -858,6 +867,9 @@ def main():
                          "(40 child LPs of a set-covering MILP node in one batch)")
     ap.add_argument("--batch", type=int, default=None,
                     help="instances per GPU: config 3 default 4096, config 4 default 1000")
+    ap.add_argument("--powerlaw-nnz", type=int, default=20_000_000,
+                    help="config 2: nonzeros the Zipf(1.5) row lengths are rescaled to; 0 = lengths as drawn "
+                         "(about 1.1e8 nonzeros)")
     ap.add_argument("--single-sample", type=int, default=32)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=TOL)

@@ -71,6 +71,23 @@ def test_adaptive_planted(seed, precision):
     assert ref["err"] < 10 * tol, ref
 
 
+@pytest.mark.parametrize("seed", [0, 1, 2, 3, 4])
+def test_adaptive_agrees_with_reference_pdhg(seed):
+    """The bar of the drop-in: on the same 200 x 500 planted LP, the adaptive
+    FP32 engine's (x, y) mapped into the reference's standard form has a
+    relative KKT error below 1e-4 by the reference's own formula
+    (``solver/lp/pdhg.py:181-196``, evaluated in FP64 on the CPU), and its
+    objective agrees with the reference PDHG's answer at tol 1e-4 to the
+    accuracy either tolerance allows."""
+    p, _ = wl.planted_lp(seed=seed)
+    r = sps.solve_lp_pdhg(p, tol=5e-5)
+    assert r.status == "optimal", r
+    assert kkt.ref_form_error(p, r.x, r.y)["err"] < 1e-4
+    o = pdhg_ref.solve(p, max_iters=100000, tol=1e-4)
+    assert o.status == "optimal"
+    assert abs(r.objective - o.objective) <= 2e-3 * (1 + abs(o.objective)), (r.objective, o.objective)
+
+
 @pytest.mark.parametrize("name", ["afiro", "blending", "adlittle", "t_2var", "t_simple_min",
                                   "t_random46", "t_ub_simple", "t_ub_tight", "mixed_bounds"])
 def test_adaptive_known_answers(name):
