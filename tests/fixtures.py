@@ -37,3 +37,12 @@ def load_problems():
 def load_golden():
     with open(os.path.join(GOLDEN, "pdhg_golden.json")) as f:
         return json.load(f)
+
+
+def load_stress():
+    """(name -> Problem, name -> golden entry) for the reference's three
+    seeded stress LPs (``tests/golden/make_stress_golden.py``)."""
+    z = np.load(os.path.join(GOLDEN, "stress_problems.npz"))
+    probs = {prefix: _unpack(z, prefix) for prefix in sorted({k.split("/")[0] for k in z.files})}
+    with open(os.path.join(GOLDEN, "stress_golden.json")) as f:
+        return probs, json.load(f)

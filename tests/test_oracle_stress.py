@@ -1,0 +1,48 @@
+"""Oracle pinned on the reference's three seeded stress LPs.
+
+The instances are the ones the reference benchmark runner builds
+(``benchmarks/run_benchmarks.py:314-378``), taken from that builder by
+``tests/golden/make_stress_golden.py``; the golden results are the reference
+``solve_lp_pdhg`` run on them (max_iters 100000, tol 1e-6).  Both restatements
+of the reference iteration (NumPy and C) must reproduce status, iteration
+count and objective.  The published CSV rows
+(``benchmarks/results/benchmark_comparison.csv:27,31,35``) agree with the
+reference run on random_n50_m30 and sparse_n500_m250 to the CSV's printed
+digits; on badly_scaled_1e8 they agree in status and iteration count (the
+100 000-iteration cap, far from the optimum 0) but not in the objective, which
+at the cap depends on the rounding of the whole unconverged trajectory.
+"""
+
+import pytest
+
+from fixtures import load_stress
+from oracle import pdhg_ref, pdhg_ref_c
+
+PROBS, GOLD = load_stress()
+
+
+@pytest.mark.parametrize("name", sorted(GOLD))
+def test_numpy_oracle_matches_reference(name):
+    g = GOLD[name]
+    r = pdhg_ref.solve(PROBS[name], max_iters=g["max_iters"], tol=g["tol"])
+    assert r.status == g["status"] and r.iterations == g["iterations"]
+    ref = float(g["objective"])
+    assert abs(r.objective - ref) <= 1e-12 * max(1.0, abs(ref)), (r.objective, ref)
+
+
+@pytest.mark.parametrize("name", sorted(GOLD))
+def test_c_oracle_matches_reference(name):
+    g = GOLD[name]
+    r = pdhg_ref_c.solve(PROBS[name], max_iters=g["max_iters"], tol=g["tol"])
+    assert r.status == g["status"] and r.iterations == g["iterations"]
+    ref = float(g["objective"])
+    assert abs(r.objective - ref) <= 1e-9 * max(1.0, abs(ref)), (r.objective, ref)
+
+
+@pytest.mark.parametrize("name", sorted(GOLD))
+def test_reference_run_against_published_row(name):
+    g = GOLD[name]
+    pub = g["published"]
+    assert pub["status"] == g["status"] and pub["iterations"] == g["iterations"]
+    if g["status"] == "optimal":
+        assert f"{float(g['objective']):.8f}" == pub["objective"]
