@@ -742,7 +742,7 @@ def run_reference(args, rank, world):
         ref_key = args.config
     for _ in range(args.warmup):
         reference_sample(p, min(2.0, args.cpu_budget))
-    vals, spi = [], []
+    spi = []
     for _ in range(args.steps):
         s = reference_sample(p, args.cpu_budget)
         spi.append(s["s_per_iter"])
