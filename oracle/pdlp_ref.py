@@ -85,9 +85,9 @@ def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="di
         kw = np.sqrt(omega ** 2 * float(res @ res) + float(dres @ dres) / omega ** 2 + (po - do) ** 2)
         return max(rp, rd, gap), kw, axv, KT.astype(float) @ yv.astype(float)
 
-    err0, kw0, _, _ = metrics(x, y)
+    _, kw0, _, _ = metrics(x, y)
     kkt_last = kkt_prev = kw0
-    status, it = "iteration_limit", 0
+    status = "iteration_limit"
     while k < max_iters:
         for _ in range(check):
             if k >= max_iters:

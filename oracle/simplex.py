@@ -167,7 +167,7 @@ def _simplex(A, b, c, u, basis, at_upper, max_iters, tol=1e-9):
 
 def solve(problem, max_iters: int = 50000) -> SimplexResult:
     """Optimal vertex of a small LP (status and x in the problem's variables)."""
-    A, b, c, u, recover, const = _standardize(problem)
+    A, b, c, u, recover, _const = _standardize(problem)
     m, N = A.shape
     n = np.asarray(problem.c).size
     if m == 0:

@@ -2,7 +2,6 @@
 simplex (config-0 LPs: 200 x 500 planted, equality rows, 0 <= x <= 2) at the
 benchmark tolerance, FP32 iterates."""
 
-import numpy as np
 import pytest
 
 import sovereign_solver_gb300 as sps

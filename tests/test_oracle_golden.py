@@ -5,7 +5,6 @@ the four Netlib rows also equal the reference's published benchmark rows
 (``benchmarks/results/benchmark_comparison.csv:5,9,13,17``).
 """
 
-import json
 import os
 
 import numpy as np
