@@ -17,7 +17,7 @@ mounted (pure Python, NumPy + SciPy):
 
 Writes ``stress_problems.npz`` (CSR arrays, the layout of
 ``small_problems.npz``) and ``stress_golden.json`` (reference result and the
-published CSV row per problem).
+published CSV row per problem, with the HiGHS optimum the CSV lists beside it).
 """
 
 from __future__ import annotations
@@ -63,7 +63,8 @@ def main(ref_root: str) -> None:
         for row in csv.DictReader(f):
             if row["solver"] == "Sovereign PDHG":
                 published[row["problem"]] = {"status": row["status"], "objective": row["objective"],
-                                             "iterations": int(row["iters_nodes"])}
+                                             "iterations": int(row["iters_nodes"]),
+                                             "highs_objective": row["highs_obj"]}
 
     out, gold = {}, {}
     for p in problems:
