@@ -250,3 +250,18 @@ def test_block_shares_fit_the_cap(plan_tool, tmp_path, cap):
     P = run_plan(plan_tool, str(tmp_path), ptr, idx, kind, 6000, np.arange(6000), cap)
     assert len(P["bins"]) == 8 and P["total_blocks"] == cap
     check_plan(plan_tool, str(tmp_path), ptr, idx, kind, 6000, np.arange(6000), cap=cap)
+
+
+@pytest.mark.parametrize("cap", [760, 16])
+def test_power_law_rows(plan_tool, tmp_path, cap):
+    """A small power-law LP (Zipf(1.5) row lengths clipped to [2, 3000], uniform
+    random columns, the shape of the 1M x 2M roofline workload): rows in every
+    CSR schedule, ragged SEGMENT rows of up to six segments, in one wave and
+    with proportional shares of a small cap."""
+    rng = np.random.default_rng(5)
+    m, n = 1500, 4000
+    lens = np.clip(rng.zipf(1.5, m), 2, 3000)
+    rows = [np.sort(rng.choice(n, int(k), replace=False)) for k in lens]
+    ptr = np.cumsum([0] + [len(r) for r in rows])
+    bins = check_plan(plan_tool, str(tmp_path), ptr, np.concatenate(rows), [0] * m, n, np.arange(n), cap=cap)
+    assert {b[0] for b in bins} == {SLICED, WARP, SEGMENT}
