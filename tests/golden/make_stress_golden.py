@@ -8,7 +8,10 @@ that builder unchanged: HiGHS (``highspy``, not installed here) is replaced by
 an empty module and the runner's solver calls by stubs that only record the
 problems, so the instances are the reference's own.  It then runs the
 reference ``solve_lp_pdhg`` with the runner's settings (its defaults:
-max_iters 100000, tol 1e-6) and reads the published rows from the CSV.
+max_iters 100000, tol 1e-6) and reads the published rows from the CSV.  A
+fourth LP comes the same way from the reference's own PDHG test
+``test_pdhg_large_sparse_terminates`` (``tests/test_pdhg.py:137-156``, solver
+call stubbed): it is unbounded, and the reference runs it to its cap.
 
 Run from the repository root, in a container where the reference checkout is
 mounted (pure Python, NumPy + SciPy):
@@ -57,6 +60,18 @@ def main(ref_root: str) -> None:
     rb.solve_lp_ipm = lambda p, *a, **k: _Skipped()
     rb.solve_lp_pdhg = lambda p, *a, **k: _Skipped()
     rb.run_synthetic_stress_benchmarks([])
+
+    # the reference's own PDHG test LP "large sparse" (tests/test_pdhg.py:137-156),
+    # taken from that test function with its solver call stubbed
+    import tests.test_pdhg as tp
+
+    def record_test(p, *a, **k):
+        p.name = "ref_test_large_sparse"
+        problems.append(p)
+        return types.SimpleNamespace(status="iteration_limit", x=np.zeros(p.n_vars))
+
+    tp.solve_lp_pdhg = record_test
+    tp.test_pdhg_large_sparse_terminates()
 
     published = {}
     with open(os.path.join(ref_root, "benchmarks", "results", "benchmark_comparison.csv")) as f:

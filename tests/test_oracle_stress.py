@@ -11,6 +11,11 @@ reference run on random_n50_m30 and sparse_n500_m250 to the CSV's printed
 digits; on badly_scaled_1e8 they agree in status and iteration count (the
 100 000-iteration cap, far from the optimum 0) but not in the objective, which
 at the cap depends on the rounding of the whole unconverged trajectory.
+
+A fourth LP is the reference's own PDHG test problem
+``test_pdhg_large_sparse_terminates`` (``tests/test_pdhg.py:137-156``): the
+restatements follow the reference to its 100 000-iteration cap on it, and the
+oracle simplex shows why the reference cannot finish: the LP is unbounded.
 """
 
 import pytest
@@ -39,7 +44,10 @@ def test_c_oracle_matches_reference(name):
     assert abs(r.objective - ref) <= 1e-9 * max(1.0, abs(ref)), (r.objective, ref)
 
 
-@pytest.mark.parametrize("name", sorted(GOLD))
+PUBLISHED = sorted(k for k, g in GOLD.items() if g["published"])
+
+
+@pytest.mark.parametrize("name", PUBLISHED)
 def test_reference_run_against_published_row(name):
     g = GOLD[name]
     pub = g["published"]
@@ -48,7 +56,7 @@ def test_reference_run_against_published_row(name):
         assert f"{float(g['objective']):.8f}" == pub["objective"]
 
 
-@pytest.mark.parametrize("name", sorted(GOLD))
+@pytest.mark.parametrize("name", PUBLISHED)
 def test_adaptive_rules_solve_the_stress_lps(name):
     """The engine's adaptive rules, in their CPU restatement (FP32 iterates,
     as the engine runs by default), reach relative KKT 1e-6 on all three,
@@ -65,3 +73,10 @@ def test_adaptive_rules_solve_the_stress_lps(name):
     obj = float(p.c @ r["x"])
     assert abs(obj - opt) <= 1e-5 * (1 + abs(opt)), (obj, opt)
     assert r["iterations"] < g["iterations"] / 5
+
+
+def test_reference_test_lp_is_unbounded():
+    from oracle import simplex
+    g = GOLD["ref_test_large_sparse"]
+    assert g["status"] == "iteration_limit" and g["iterations"] == 100000
+    assert simplex.solve(PROBS["ref_test_large_sparse"]).status == "unbounded"
