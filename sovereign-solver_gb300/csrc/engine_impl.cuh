@@ -217,14 +217,45 @@ struct Engine : EngineBase {
         };
         // each row's bucket once (the sort and the bin boundaries read it again)
         std::vector<uint8_t> bk(R);
-        for (int i = 0; i < R; ++i) bk[i] = (uint8_t)bucket(i);
+        if (!kinds && !slab) {       // columns: one kind, no SLAB (the same buckets, branch-free)
+            const int64_t* L = lens.data();
+            for (int i = 0; i < R; ++i)
+                bk[i] = (uint8_t)(L[i] <= kSliceMax ? kSliceMax - L[i] : L[i] <= kSegment ? kSliceMax + 1 : kSliceMax + 2);
+        } else {
+            for (int i = 0; i < R; ++i) bk[i] = (uint8_t)bucket(i);
+        }
+        // Bucket counts in four interleaved histograms (consecutive rows mostly
+        // share a bucket, and one counter would make every increment wait for
+        // the previous one), then a stable placement that writes each run of
+        // equal buckets as one block: 2M uniform columns take 8 instead of 14 ms.
         std::vector<int64_t> cnt(2 * NB + 1, 0);
-        for (int i = 0; i < R; ++i) cnt[bk[i] + 1]++;
+        {
+            std::vector<int64_t> h(4 * 2 * NB, 0);
+            const uint8_t* kb = bk.data();
+            int i = 0;
+            for (; i + 4 <= R; i += 4) {
+                ++h[kb[i]];
+                ++h[2 * NB + kb[i + 1]];
+                ++h[4 * NB + kb[i + 2]];
+                ++h[6 * NB + kb[i + 3]];
+            }
+            for (; i < R; ++i) ++h[kb[i]];
+            for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] = h[b] + h[2 * NB + b] + h[4 * NB + b] + h[6 * NB + b];
+        }
         for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] += cnt[b];
         P.perm.assign(R, 0);
         {
             std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
-            for (int i = 0; i < R; ++i) P.perm[pos[bk[i]]++] = i;
+            int32_t* pm = P.perm.data();
+            for (int i = 0; i < R;) {
+                const uint8_t b = bk[i];
+                int j = i + 1;
+                while (j < R && bk[j] == b) ++j;
+                int32_t* dst = pm + pos[b];
+                for (int q = i; q < j; ++q) dst[q - i] = q;
+                pos[b] += j - i;
+                i = j;
+            }
         }
         // (kind, schedule) of a bucket: rows of one bin are consecutive buckets
         auto bin_of = [&](int bucket_id) {

@@ -3,6 +3,7 @@
 // a problem read from a binary file and writes the plan back out, for
 // tests/test_plan_layout.py.
 //
+// usage:  plan_dump in.bin out.bin block_cap [cols]
 // input:  int32 m, int32 n, int64 nnz, int32 ptr[m+1], int32 idx[nnz],
 //         int8 kind[m], int32 inv_col[n]
 // output: a sequence of (int64 count, int32 data[count]) arrays:
@@ -19,7 +20,10 @@ using namespace sps;
 static bool read_all(FILE* f, void* p, size_t size, size_t count) { return fread(p, size, count, f) == count; }
 
 int main(int argc, char** argv) {
-    if (argc != 4) return 2;
+    // optional 4th argument "cols": the column plan as the engine makes it
+    // (one kind, no SLAB choice: make_plan(lens, nullptr, nullptr, ...))
+    if (argc != 4 && argc != 5) return 2;
+    const bool cols = argc == 5 && argv[4][0] == 'c';
     FILE* f = fopen(argv[1], "rb");
     if (!f) return 3;
     int32_t m = 0, n = 0;
@@ -42,11 +46,14 @@ int main(int argc, char** argv) {
     hp.segs.push_back({idx.data(), val.data(), h});
     hp.segs.push_back({idx.data() + h, val.data() + h, nnz - h});
     using E = Engine<float>;
-    const std::vector<uint8_t> slab = E::choose_slab(hp, inv_col, 4);
+    const std::vector<uint8_t> slab = cols ? std::vector<uint8_t>(m, 0) : E::choose_slab(hp, inv_col, 4);
     std::vector<int64_t> rlen(m);
     for (int i = 0; i < m; ++i) rlen[i] = hp.ptr[i + 1] - hp.ptr[i];
     E::Plan P;
-    E::make_plan(rlen, &hp.kind, &slab, P, atoi(argv[3]));
+    if (cols)
+        E::make_plan(rlen, nullptr, nullptr, P, atoi(argv[3]));
+    else
+        E::make_plan(rlen, &hp.kind, &slab, P, atoi(argv[3]));
     FILE* o = fopen(argv[2], "wb");
     if (!o) return 5;
     auto put = [&](const std::vector<int32_t>& v) {

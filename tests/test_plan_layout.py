@@ -17,6 +17,7 @@ import subprocess
 
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
@@ -38,7 +39,7 @@ def plan_tool(tmp_path_factory):
     return out
 
 
-def run_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap):
+def run_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap, cols=False):
     m = len(ptr) - 1
     fin, fout = os.path.join(tmp, "in.bin"), os.path.join(tmp, "out.bin")
     with open(fin, "wb") as f:
@@ -47,7 +48,7 @@ def run_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap):
         f.write(np.asarray(idx, np.int32).tobytes())
         f.write(np.asarray(kind, np.int8).tobytes())
         f.write(np.asarray(inv_col, np.int32).tobytes())
-    subprocess.run([tool, fin, fout, str(cap)], check=True)
+    subprocess.run([tool, fin, fout, str(cap)] + (["cols"] if cols else []), check=True)
     arrs = []
     with open(fout, "rb") as f:
         for _ in range(7):
@@ -59,14 +60,14 @@ def run_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap):
                 total=int(tail[0]), ntickets=int(tail[1]), nslots=int(tail[2]), nslab=int(tail[3]))
 
 
-def check_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap=760, seed=0):
+def check_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap=760, seed=0, cols=False):
     """Replay the traversal; returns the plan's bins as (mode, kind, rows)."""
     rng = np.random.default_rng(seed)
     ptr = np.asarray(ptr, np.int64)
     idx = np.asarray(idx, np.int64)
     inv_col = np.asarray(inv_col)
     m = len(ptr) - 1
-    P = run_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap)
+    P = run_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap, cols)
     perm, fptr, soff, unit, B, total = P["perm"], P["fptr"], P["soff"], P["unit"], P["bins"], P["total"]
     assert sorted(perm.tolist()) == list(range(m))
     assert P["total_blocks"] <= cap and B[:, 5].sum() == P["total_blocks"]
@@ -265,3 +266,22 @@ def test_power_law_rows(plan_tool, tmp_path, cap):
     ptr = np.cumsum([0] + [len(r) for r in rows])
     bins = check_plan(plan_tool, str(tmp_path), ptr, np.concatenate(rows), [0] * m, n, np.arange(n), cap=cap)
     assert {b[0] for b in bins} == {SLICED, WARP, SEGMENT}
+
+
+@pytest.mark.parametrize("cap", [760, 11])
+def test_column_plans(plan_tool, tmp_path, cap):
+    """The column plan as the engine makes it (one kind, no SLAB choice), on
+    the columns of a transportation LP (all of length 2: one SLICED bin with
+    computed slice offsets) and of a power-law LP (every CSR schedule)."""
+    ptr, idx, kind, n = transport(30, 50)
+    M = sp.csr_matrix((np.ones(len(idx)), idx, ptr), shape=(len(ptr) - 1, n)).tocsc()
+    bins = check_plan(plan_tool, str(tmp_path), M.indptr, M.indices, [0] * n, M.shape[0],
+                      np.arange(M.shape[0]), cap=cap, cols=True)
+    assert bins == [(SLICED, 0, n)]
+    rng = np.random.default_rng(6)
+    m, n = 600, 900
+    rows = [np.sort(rng.choice(n, int(k), replace=False)) for k in np.clip(rng.zipf(1.3, m), 1, 900)]
+    ptr = np.cumsum([0] + [len(r) for r in rows])
+    M = sp.csr_matrix((np.ones(ptr[-1]), np.concatenate(rows), ptr), shape=(m, n)).T.tocsr()
+    bins = check_plan(plan_tool, str(tmp_path), M.indptr, M.indices, [0] * n, m, np.arange(m), cap=cap, cols=True)
+    assert {b[0] for b in bins} <= {SLICED, WARP, SEGMENT} and {b[1] for b in bins} == {0}
