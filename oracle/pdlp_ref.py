@@ -4,7 +4,9 @@ Same rules as ``SPS_MODE_ADAPTIVE`` (box form, 10 Ruiz + 1 Pock-Chambolle
 passes, η₀ = 1/max|K̃|, ω₀ = ‖c̃‖/‖b̃‖, adaptive step, step-weighted averages,
 KKT check of average and current every 64 attempts, restart to the better one
 on 0.2 / 0.8 / 0.36 criteria, primal-weight update at restarts, termination on
-the original problem's relative KKT error), in a chosen iterate precision.
+the original problem's relative KKT error, infeasibility and unboundedness
+certificates from the change since the last restart), in a chosen iterate
+precision.
 Used to check the engine's trajectory on small problems and to study the
 effect of the iterate precision.
 
@@ -41,6 +43,35 @@ def scale(K: sp.csr_matrix, ruiz: int = 10):
         dr = np.where(rs > 0, dr / np.sqrt(np.where(rs > 0, rs, 1)), dr)
         dc = np.where(cs > 0, dc / np.sqrt(np.where(cs > 0, cs, 1)), dc)
     return dr, dc
+
+
+RAY_TOL = 1e-6   # a certificate's residual must be at most this fraction of its objective
+
+
+def ray_status(Ks, KT, c, b, lo, hi, le, dx, dy):
+    """Infeasibility / unboundedness test on the change (dx, dy) of the current
+    iterate since the last restart, in the scaled space, as the engine's check
+    takes it (``csrc/decide.cuh`` ``decide_check``): dy is a Farkas certificate
+    when b^T dy plus the bound terms of lambda = -K^T dy is positive and dy's
+    violation of the dual cone together with lambda's cone residual is at most
+    RAY_TOL of it; dx is an improving ray when c^T dx < 0 and K dx's violation
+    of the row cones together with dx's violation of the bounds' recession cone
+    is at most RAY_TOL of |c^T dx|.  Returns "infeasible", "unbounded" or None."""
+    hl, hh = np.isfinite(lo), np.isfinite(hi)
+    kdx = Ks.astype(float) @ dx
+    kdx[le] = np.maximum(kdx[le], 0.0)
+    dyv = np.where(le, np.maximum(dy, 0.0), 0.0)
+    lr = -(KT.astype(float) @ dy)
+    lp = np.where(hl & hh, lr, np.where(hl, np.maximum(lr, 0.0), np.where(hh, np.minimum(lr, 0.0), 0.0)))
+    bound = float(np.sum(np.where(hl, lo, 0.0) * np.maximum(lp, 0.0)) + np.sum(np.where(hh, hi, 0.0) * np.minimum(lp, 0.0)))
+    dual_obj = float(b.astype(float) @ dy) + bound
+    if dual_obj > 0.0 and np.sqrt(float((lr - lp) @ (lr - lp)) + float(dyv @ dyv)) <= RAY_TOL * dual_obj:
+        return "infeasible"
+    vx = np.where(hl & hh, dx, np.where(hl, np.minimum(dx, 0.0), np.where(hh, np.maximum(dx, 0.0), 0.0)))
+    cdx = float(c.astype(float) @ dx)
+    if cdx < 0.0 and np.sqrt(float(kdx @ kdx) + float(vx @ vx)) <= RAY_TOL * (-cdx):
+        return "unbounded"
+    return None
 
 
 def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="direct", check=64):
@@ -118,10 +149,13 @@ def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="di
         ea, ka, axa, atya = metrics(xa, ya)
         ec, kc_, _, _ = metrics(x, y)
         best_avg = has_avg and ea < ec
-        if min(ea if has_avg else np.inf, ec) < tol or k >= max_iters:
+        optimal = min(ea if has_avg else np.inf, ec) < tol
+        ray = None if optimal else ray_status(Ks, KT, c, b, lo, hi, le, (x - xl).astype(float),
+                                              (y - yl).astype(float))
+        if optimal or ray or k >= max_iters:
             if best_avg:
                 x, y = xa, ya
-            status = "optimal" if min(ea if has_avg else np.inf, ec) < tol else "iteration_limit"
+            status = "optimal" if optimal else ray or "iteration_limit"
             break
         cand_avg = has_avg and ka < kc_
         kc = ka if cand_avg else kc_
