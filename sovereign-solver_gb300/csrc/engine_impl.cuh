@@ -200,6 +200,41 @@ struct Engine : EngineBase {
         return slab;
     }
 
+    // Columns longer than the device insertion sort takes (kSortMax), ordered
+    // by row index on the host: idx / val hold the CSC entries of columns
+    // [j0, j1) (cptr[j0] .. cptr[j1]); shorter columns in the range are left as
+    // they are.  Columns are independent, so host threads take column ranges.
+    static void sort_long_columns(const int32_t* cptr, int32_t j0, int32_t j1, int32_t* idx, double* val) {
+        const int64_t base = cptr[j0];
+        auto work = [&](int32_t a, int32_t b) {
+            std::vector<int64_t> ord;
+            std::vector<int32_t> ri2;
+            std::vector<double> rv2;
+            for (int32_t j = a; j < b; ++j) {
+                const int64_t s = cptr[j] - base, len = (int64_t)cptr[j + 1] - cptr[j];
+                if (len <= kSortMax) continue;
+                int32_t* ri = idx + s;
+                double* rv = val + s;
+                ord.resize(len);
+                std::iota(ord.begin(), ord.end(), 0);
+                std::sort(ord.begin(), ord.end(), [&](int64_t x, int64_t y) { return ri[x] < ri[y]; });
+                ri2.resize(len);
+                rv2.resize(len);
+                for (int64_t q = 0; q < len; ++q) { ri2[q] = ri[ord[q]]; rv2[q] = rv[ord[q]]; }
+                std::copy(ri2.begin(), ri2.end(), ri);
+                std::copy(rv2.begin(), rv2.end(), rv);
+            }
+        };
+        const int64_t cols = (int64_t)j1 - j0;
+        const int nt = (int)std::min<int64_t>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())),
+                                              std::max<int64_t>(1, cols / 4096));
+        if (nt <= 1) { work(j0, j1); return; }
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t)
+            pool.emplace_back(work, (int32_t)(j0 + cols * t / nt), (int32_t)(j0 + cols * (t + 1) / nt));
+        for (auto& th : pool) th.join();
+    }
+
     // Order: per kind, SLICED rows by decreasing length, then WARP rows, then
     // SEGMENT rows, then SLAB rows (stable counting sort); one bin per (kind,
     // schedule).
@@ -634,22 +669,28 @@ struct Engine : EngineBase {
         }
         SPS_CK(cudaStreamSynchronize(st));
         cudaFreeAsync(s_ptr, st); cudaFreeAsync(s_idx, st); cudaFreeAsync(s_val, st); cudaFreeAsync(s_colcount, st); cudaFreeAsync(s_err, st);
-        // columns too long for the device insertion sort: order on the host
-        for (int j = 0; j < n; ++j) {
-            const int64_t len = cptr[j + 1] - cptr[j];
-            if (len <= kSortMax) continue;
-            std::vector<int32_t> ri(len);
-            std::vector<double> rv(len);
-            SPS_CK(cudaMemcpy(ri.data(), t_cidx + cptr[j], sizeof(int32_t) * len, cudaMemcpyDeviceToHost));
-            SPS_CK(cudaMemcpy(rv.data(), t_cval + cptr[j], sizeof(double) * len, cudaMemcpyDeviceToHost));
-            std::vector<int64_t> ord(len);
-            std::iota(ord.begin(), ord.end(), 0);
-            std::sort(ord.begin(), ord.end(), [&](int64_t a, int64_t b) { return ri[a] < ri[b]; });
-            std::vector<int32_t> ri2(len);
-            std::vector<double> rv2(len);
-            for (int64_t q = 0; q < len; ++q) { ri2[q] = ri[ord[q]]; rv2[q] = rv[ord[q]]; }
-            SPS_CK(cudaMemcpy(t_cidx + cptr[j], ri2.data(), sizeof(int32_t) * len, cudaMemcpyHostToDevice));
-            SPS_CK(cudaMemcpy(t_cval + cptr[j], rv2.data(), sizeof(double) * len, cudaMemcpyHostToDevice));
+        // columns too long for the device insertion sort: ordered on the host, with
+        // one copy each way of the CSC range that holds them (four copies per
+        // column cost seconds on the 168k long columns of a 1.1e8-nonzero LP)
+        {
+            int32_t j0 = -1, j1 = -1;
+            for (int j = 0; j < n; ++j)
+                if (cptr[j + 1] - cptr[j] > kSortMax) {
+                    if (j0 < 0) j0 = j;
+                    j1 = j + 1;
+                }
+            if (j0 >= 0) {
+                const int64_t lo = cptr[j0], len = (int64_t)cptr[j1] - cptr[j0];
+                std::vector<int32_t> ri(len);
+                std::vector<double> rv(len);
+                SPS_CK(cudaMemcpyAsync(ri.data(), t_cidx + lo, sizeof(int32_t) * len, cudaMemcpyDeviceToHost, st));
+                SPS_CK(cudaMemcpyAsync(rv.data(), t_cval + lo, sizeof(double) * len, cudaMemcpyDeviceToHost, st));
+                SPS_CK(cudaStreamSynchronize(st));
+                sort_long_columns(cptr.data(), j0, j1, ri.data(), rv.data());
+                SPS_CK(cudaMemcpyAsync(t_cidx + lo, ri.data(), sizeof(int32_t) * len, cudaMemcpyHostToDevice, st));
+                SPS_CK(cudaMemcpyAsync(t_cval + lo, rv.data(), sizeof(double) * len, cudaMemcpyHostToDevice, st));
+                SPS_CK(cudaStreamSynchronize(st));
+            }
         }
 
         // ---- scaling (adaptive) or reference diagonal steps, on the FP64 temporaries
