@@ -9,6 +9,7 @@
 #include <thread>
 
 #include "engine_impl.cuh"
+#include "nvtx.cuh"
 
 using namespace sps;
 
@@ -274,6 +275,7 @@ int sps_options_init(sps_options* o) {
 }
 
 int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_handle** out) {
+    sps::NvtxRange nvtx_range("sps_create");
     g_create_error.clear();
     if (!out) return create_fail(SPS_ERR_INVALID, "null output handle pointer");
     *out = nullptr;
@@ -324,6 +326,7 @@ int sps_set_warm_start(sps_handle* h, const double* x0, const double* y0, double
 }
 
 int sps_solve(sps_handle* h, sps_result* res) {
+    sps::NvtxRange nvtx_range("sps_solve");
     if (!h || !res) return SPS_ERR_INVALID;
     h->eng->err.clear();
     h->last_esc = false;
@@ -338,6 +341,7 @@ int sps_time_iteration_kernels(sps_handle* h, int32_t reps, double* out) {
 }
 
 int sps_get_solution(sps_handle* h, double* x, double* y) {
+    sps::NvtxRange nvtx_range("sps_get_solution");
     if (!h) return SPS_ERR_INVALID;
     if (h->last_esc) {
         const int rc = h->esc->eng->get(x, y);

@@ -25,6 +25,7 @@
 
 #include "batch.cuh"
 #include "gnn_internal.cuh"
+#include "nvtx.cuh"
 
 namespace sps {
 void set_create_error(const std::string& msg);
@@ -938,6 +939,7 @@ static int32_t half_octave(double x) { return x > 0.0 ? (int32_t)std::floor(2.0 
 
 extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, const sps_options* opt_in,
                                 sps_batch** out) {
+    sps::NvtxRange nvtx_range("sps_batch_create");
     if (!out || count <= 0 || !probs) {
         sps::set_create_error("sps_batch_create: need count > 0, problems and an output pointer");
         return SPS_ERR_INVALID;
@@ -1273,6 +1275,7 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
 }
 
 extern "C" int sps_batch_solve(sps_batch* b, sps_batch_stats* stats) {
+    sps::NvtxRange nvtx_range("sps_batch_solve");
     if (!b) return SPS_ERR_INVALID;
     SPB_CK(cudaSetDevice(b->opt.device));
     const int64_t W = b->opt.check_interval > 0 ? b->opt.check_interval : 64;
@@ -1446,6 +1449,7 @@ extern "C" int sps_batch_set_warm_starts(sps_batch* b, const double* x0, const d
 }
 
 extern "C" int sps_batch_set_warm_starts_gnn(sps_batch* b, sps_gnn* g, const double* scales) {
+    sps::NvtxRange nvtx_range("sps_batch_set_warm_starts_gnn");
     if (!b) return SPS_ERR_INVALID;
     if (!g || !scales) return b->fail(SPS_ERR_INVALID, "need a network and its four scales");
     for (int q = 0; q < 4; ++q)

@@ -19,6 +19,7 @@
 
 #include "../../include/sps_gnn.h"
 #include "gnn_internal.cuh"
+#include "nvtx.cuh"
 
 namespace {
 
@@ -916,6 +917,7 @@ int sps_gnn_create(const sps_gnn_graph* gr, const sps_gnn_options* opt_in, sps_g
 }
 
 int sps_gnn_predict(sps_gnn* g, int32_t batch, const float* vf, const float* cf, float* x0, float* y0, float* lw) {
+    sps::NvtxRange nvtx_range("sps_gnn_predict");
     if (!g) return -1;
     if (int rc = check_batch(g, batch, vf, cf)) return rc;
     GNN_CK(cudaSetDevice(g->opt.device));
@@ -948,6 +950,7 @@ int sps_gnn_loss_grad(sps_gnn* g, int32_t batch, const float* vf, const float* c
 
 int sps_gnn_train_step(sps_gnn* g, int32_t batch, const float* vf, const float* cf, const float* xt, const float* yt,
                        const float* lt, double* loss) {
+    sps::NvtxRange nvtx_range("sps_gnn_train_step");
     if (!g) return -1;
     if (int rc = check_batch(g, batch, vf, cf)) return rc;
     if (!xt || !yt || !lt) return g->fail(-1, "null targets");
