@@ -341,7 +341,8 @@ def batch_cpu_baseline(args):
                        f"0, 128, ..., 3968 of the batch ({len(ks)} LPs), {procs} single-threaded processes, "
                        f"{wall:.1f} s wall; per-LP {np.median(per):.2f} s median, "
                        f"{sum(o[1] == 'optimal' for o in out)}/{len(ks)} optimal"),
-            "serial_s_per_solve": float(np.mean(per))}
+            "serial_s_per_solve": float(np.mean(per)),
+            "one_core_value": 1.0 / float(np.mean(per))}     # solves/s of one single-threaded process
 
 
 def run_batch(args, rank, world):
