@@ -122,3 +122,22 @@ def test_get_available_device_values():
 def test_no_gpu_fails_loudly():
     with pytest.raises(RuntimeError, match="CUDA"):
         pdhg.solve_lp_pdhg(_lp())
+
+
+def test_integration_stub_matches_the_abi():
+    """The ctypes stub a maintainer would paste into the reference tree (the
+    first Python block of INTEGRATION.md's C ABI section) declares the same
+    struct layouts as the package's own binding, which the test above checks
+    against the header."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    sec = text[text.index("## 2. C ABI binding"):]
+    code = sec[sec.index("```python") + len("```python"):]
+    code = code[:code.index("```")]
+    classes = code[code.index("class Desc"):code.index("def solve_lp_pdhg")]
+    ns = {"C": C, "i32p": C.POINTER(C.c_int32), "f64p": C.POINTER(C.c_double)}
+    exec(classes, ns)
+    for stub, ours in ((ns["Desc"], N.ProblemDesc), (ns["Opts"], N.Options), (ns["Res"], N.Result)):
+        assert C.sizeof(stub) == C.sizeof(ours), stub.__name__
+        assert [f for f, _ in stub._fields_] == [f for f, _ in ours._fields_], stub.__name__
+        for f, _ in stub._fields_:
+            assert getattr(stub, f).offset == getattr(ours, f).offset, (stub.__name__, f)
