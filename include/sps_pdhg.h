@@ -57,6 +57,15 @@ extern "C" {
 #define SPS_FP32  0  /* FP32 iterates and SpMV, FP64 checks */
 #define SPS_FP64  1  /* FP64 everywhere */
 
+/* relative KKT error measure of the adaptive single-LP engine (sps_options.kkt_form) */
+#define SPS_KKT_LAGRANGIAN  0  /* dual objective = Lagrangian bound b^T y + sum_j min over
+                                  [lb_j, ub_j] of r_j x_j, r = c - K^T y: every finite bound
+                                  enters the gap (default) */
+#define SPS_KKT_PDLP        1  /* a finite bound farther from x_j than |x_j| does not enter the
+                                  dual objective; the part of r_j it would absorb counts as dual
+                                  residual instead (PDLP's default handling, OR-tools
+                                  handle_some_primal_gradients_on_finite_bounds_as_residuals) */
+
 typedef struct {
     int32_t n;                      /* variables */
     int32_t m_ub;                   /* rows of A_ub x <= b_ub */
@@ -109,7 +118,8 @@ typedef struct {
                                  from its current point.  Which instances leave depends on
                                  timing, so results are no longer bit-identical from run to run;
                                  0 (default) = never */
-    int32_t reserved[1];
+    int32_t kkt_form;         /* SPS_KKT_LAGRANGIAN (default) or SPS_KKT_PDLP; adaptive mode of
+                                 the single-LP engine only (sps_batch_create rejects PDLP) */
 } sps_options;
 
 typedef struct {
@@ -132,7 +142,9 @@ typedef struct {
                                  iteration, restart and time fields then cover both parts */
     int32_t warm_start_used;  /* 1 if the solve started from the caller's warm start (0 when none
                                  was given or the cold-start fallback rejected it) */
-    int32_t reserved[3];
+    int32_t reserved;
+    double  rel_kkt_lagrangian; /* the returned point's relative KKT error in the Lagrangian form
+                                   (SPS_KKT_LAGRANGIAN); equals rel_kkt unless kkt_form is PDLP */
 } sps_result;
 
 typedef struct sps_handle sps_handle;
@@ -249,12 +261,18 @@ typedef struct {
  * rel_kkt, rel_primal, rel_dual, rel_gap, primal objective, dual objective —
  * the same measure sps_solve reports (sps_result.rel_*).  Work is queued on
  * `stream` (a cudaStream_t, NULL = default stream); the call does not wait.
- * Scratch is a fixed ~2.1 MB device array inside the library (held by every
+ * Preconditions the call cannot check without reading device memory: every
+ * column index lies in [0, n), indptr is non-decreasing from 0.  Every array
+ * the LP needs must be non-NULL, also for rows without nonzeros (indptr,
+ * indices, values and rhs when m_ub + m_eq > 0; c, lb, ub when n > 0), else
+ * SPS_ERR_INVALID.  K^T y is summed with integer digits, so the result is
+ * bitwise reproducible from call to call.
+ * Scratch is a fixed ~6.3 MB device array inside the library (held by every
  * GPU that loads it until exit), so n is limited to 262144 columns (larger n
  * returns SPS_ERR_INVALID); rows are unlimited.  All calls share that array:
  * calls that overlap on the GPU race — order them on one stream.  The first
- * call on each device looks up the array's device address; make that first
- * call before any stream capture.  Errors: sps_last_error(NULL). */
+ * call in each CUDA context looks up the array's device address; make that
+ * first call before any stream capture.  Errors: sps_last_error(NULL). */
 int sps_kkt_noalloc(const sps_device_lp *lp, const double *x, const double *y, double *out, void *stream);
 
 /* Number of visible CUDA devices (0 when none or the driver is unusable).

@@ -14,6 +14,11 @@ cᵀx − yᵀ(Kx − rhs) (so y ≤ 0 on ≤ rows):
                  gap = |cᵀx − d(y)| / (1 + |cᵀx| + |d(y)|),
                  d(y) = rhsᵀy + Σ lb_j λ_j⁺ − Σ ub_j λ_j⁻.
 
+                 With ``form="pdlp"`` a finite bound farther from x_j than |x_j|
+                 is left out of λ's cone and of d(y), so the part of r_j it
+                 would absorb counts as dual residual (PDLP's default handling
+                 of far bounds; the engine's ``kkt_form="pdlp"``).
+
 ``ref_form_error`` the reference's own error (``solver/lp/pdhg.py:181-196``)
                  after mapping (x, y) into the reference standard form
                  (``pdhg.py:62-125``): shifted x, slacks max(b − A_ub x, 0),
@@ -36,7 +41,7 @@ def stacked(problem):
     return K, rhs
 
 
-def box_rel_kkt(problem, x, y, K=None, rhs=None) -> dict:
+def box_rel_kkt(problem, x, y, K=None, rhs=None, form="lagrangian") -> dict:
     if K is None:
         K, rhs = stacked(problem)
     x = np.asarray(x, float)
@@ -50,6 +55,12 @@ def box_rel_kkt(problem, x, y, K=None, rhs=None) -> dict:
 
     r = c - K.T @ y
     has_l, has_u = np.isfinite(lb), np.isfinite(ub)
+    if form == "pdlp":
+        with np.errstate(invalid="ignore"):
+            has_l = has_l & (np.abs(x - lb) <= np.abs(x))
+            has_u = has_u & (np.abs(x - ub) <= np.abs(x))
+    elif form != "lagrangian":
+        raise ValueError(form)
     lam = np.where(has_l & has_u, r,
           np.where(has_l, np.maximum(r, 0.0), np.where(has_u, np.minimum(r, 0.0), 0.0)))
     dres = np.concatenate([r - lam, np.maximum(y[:m_ub], 0.0)])

@@ -74,7 +74,8 @@ def ray_status(Ks, KT, c, b, lo, hi, le, dx, dy):
     return None
 
 
-def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="direct", check=64):
+def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="direct", check=64,
+          kkt_form="lagrangian"):
     K, rhs = kkt.stacked(problem)
     m_ub = problem.n_ineq
     m, n = K.shape
@@ -105,6 +106,10 @@ def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="di
         res[le] = np.maximum(res[le], 0)
         rc = c.astype(float) - KT.astype(float) @ yv.astype(float)
         hl, hh = np.isfinite(lo), np.isfinite(hi)
+        if kkt_form == "pdlp":      # far finite bounds (|x - bound| > |x|) leave the dual objective
+            xf = xv.astype(float)
+            hl = hl & (np.abs(xf - lo) <= np.abs(xf))
+            hh = hh & (np.abs(xf - hi) <= np.abs(xf))
         lam = np.where(hl & hh, rc, np.where(hl, np.maximum(rc, 0), np.where(hh, np.minimum(rc, 0), 0)))
         dres = rc - lam
         po = float(c.astype(float) @ xv)
@@ -179,4 +184,4 @@ def solve(problem, tol=1e-4, max_iters=100000, dtype=np.float32, interaction="di
     xo = x.astype(float) * dc
     yo = y.astype(float) * dr
     return {"status": status, "iterations": k, "x": xo, "y": yo, "restarts": restarts,
-            "kkt": kkt.box_rel_kkt(problem, np.clip(xo, problem.lb, problem.ub), yo)}
+            "kkt": kkt.box_rel_kkt(problem, np.clip(xo, problem.lb, problem.ub), yo, form=kkt_form)}

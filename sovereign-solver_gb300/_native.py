@@ -27,6 +27,7 @@ STATUS = {0: "optimal", 1: "iteration_limit", 2: "time_limit", 3: "numeric_error
 ESCALATE = {"off": 0, "fp64": 1, "stop": 2}
 MODES = {"reference": 0, "adaptive": 1}
 PRECISIONS = {"fp32": 0, "fp64": 1}
+KKT_FORMS = {"lagrangian": 0, "pdlp": 1}
 
 
 class ProblemDesc(C.Structure):
@@ -45,7 +46,7 @@ class Options(C.Structure):
         ("graph_mode", C.c_int32), ("device", C.c_int32), ("max_blocks", C.c_int32),
         ("batch_group", C.c_int32), ("escalate", C.c_int32), ("warm_fallback", C.c_int32),
         ("batch_team", C.c_int32), ("batch_team_nnz", C.c_int32), ("batch_handoff_nnz", C.c_int32),
-        ("reserved", C.c_int32 * 1),
+        ("kkt_form", C.c_int32),
     ]
 
 
@@ -65,7 +66,8 @@ class Result(C.Structure):
         ("rel_primal", C.c_double), ("rel_dual", C.c_double), ("rel_gap", C.c_double),
         ("primal_weight", C.c_double), ("step_size", C.c_double), ("setup_ms", C.c_double),
         ("solve_ms", C.c_double), ("kernel_launches", C.c_int64), ("returned_average", C.c_int32),
-        ("escalated", C.c_int32), ("warm_start_used", C.c_int32), ("reserved", C.c_int32 * 3),
+        ("escalated", C.c_int32), ("warm_start_used", C.c_int32), ("reserved", C.c_int32),
+        ("rel_kkt_lagrangian", C.c_double),
     ]
 
 

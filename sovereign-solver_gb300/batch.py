@@ -39,13 +39,15 @@ class PDHGBatch:
     attempts) still running leave the launch and are finished by the single-LP
     engine on the whole GPU; which ones leave depends on timing, so results are
     not bit-identical from run to run.  0 (default) = never.
+    ``kkt_form``: the batched solver measures the Lagrangian form only (the
+    PDLP form is an option of the single-LP engine).
     """
 
     def __init__(self, problems: Sequence, tol: float = 1e-4, max_iters: int = MAX_PDHG_ITERS,
                  batch_group: int = 0, time_limit: float = 0.0, check_interval: int = 0,
                  graph_mode: int = 2, device: int = 0, ruiz_iters: int = 10, escalate: str = "fp64",
                  warm_fallback: bool = True, batch_team: int = 0, batch_team_nnz: int = 0,
-                 batch_handoff_nnz: int = 0):
+                 batch_handoff_nnz: int = 0, kkt_form: str = "lagrangian"):
         self.lib = N.load()
         self.problems = list(problems)
         if not self.problems:
@@ -54,7 +56,8 @@ class PDHGBatch:
         arr = (N.ProblemDesc * len(self._descs))(*[d.desc for d in self._descs])
         o = make_options(tol=tol, max_iters=max_iters, time_limit=time_limit,
                          check_interval=check_interval, graph_mode=graph_mode, device=device,
-                         ruiz_iters=ruiz_iters, escalate=escalate, warm_fallback=warm_fallback)
+                         ruiz_iters=ruiz_iters, escalate=escalate, warm_fallback=warm_fallback,
+                         kkt_form=kkt_form)
         o.batch_group = int(batch_group)
         o.batch_team = int(batch_team)
         o.batch_team_nnz = int(batch_team_nnz)

@@ -287,6 +287,11 @@ int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_hand
         return create_fail(SPS_ERR_INVALID, "unknown precision");
     if (opt.max_iters < 0 || !(opt.tol >= 0) || opt.check_interval < 0 || opt.time_limit_s < 0)
         return create_fail(SPS_ERR_INVALID, "invalid options");
+    if (opt.kkt_form != SPS_KKT_LAGRANGIAN && opt.kkt_form != SPS_KKT_PDLP)
+        return create_fail(SPS_ERR_INVALID, "unknown kkt_form");
+    if (opt.kkt_form == SPS_KKT_PDLP && opt.mode != SPS_MODE_ADAPTIVE)
+        return create_fail(SPS_ERR_INVALID, "kkt_form PDLP needs the adaptive mode (the reference mode "
+                                            "reports the reference's own error)");
     if (int rc = validate(prob)) return rc;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= opt.device || opt.device < 0) {

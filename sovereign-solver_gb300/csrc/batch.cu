@@ -951,6 +951,10 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         sps::set_create_error("sps_batch_create: the batched solver runs the adaptive mode with FP32 iterates");
         return SPS_ERR_INVALID;
     }
+    if (opt.kkt_form != SPS_KKT_LAGRANGIAN) {
+        sps::set_create_error("sps_batch_create: the batched solver reports the Lagrangian KKT form only");
+        return SPS_ERR_INVALID;
+    }
     auto b = std::make_unique<sps_batch>();
     b->count = count;
     b->opt = opt;
@@ -1510,6 +1514,7 @@ extern "C" int sps_batch_get(sps_batch* b, int32_t k, double* x, double* y, sps_
         res->accepted_steps = c.accepted_total;
         res->objective = obj;
         res->rel_kkt = c.rel_kkt;
+        res->rel_kkt_lagrangian = c.rel_kkt;
         res->rel_primal = c.rel_p;
         res->rel_dual = c.rel_d;
         res->rel_gap = c.rel_gap;

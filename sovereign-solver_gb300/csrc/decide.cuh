@@ -21,6 +21,10 @@ constexpr double kRayTol = 1e-6;
 // Partials of a check: column pass tc[kColPartials], row pass tr[kRowPartials].
 constexpr int kColPartials = 14;
 constexpr int kRowPartials = 11;
+// With the PDLP error form the single-LP column check adds, per point q, the
+// Lagrangian form's original-scale dual residual^2 (lag[q]) and bound terms
+// (lag[2 + q]), so the returned point's Lagrangian error is reported too.
+constexpr int kLagPartials = 4;
 
 // Adaptive step (PDLP): limit = ||dz||_w^2 / (2 |dy^T K dx|); the attempt is
 // accepted if eta <= limit; next eta = min((1 - (k+1)^-0.3) limit, (1 + (k+1)^-0.6) eta).
@@ -72,10 +76,10 @@ __device__ __forceinline__ bool decide_step(Ctl& c, double dy2, double inter_sig
 // precision floor; the host continues in FP64 from the saved point).  Sets c.apply.
 __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[kColPartials],
                                              const double (&tr)[kRowPartials], double inv_nb, double inv_nc,
-                                             bool stop) {
+                                             bool stop, const double* lag = nullptr) {
     const bool has_avg = c.w_sum > 0.0;
     const double w = c.omega;
-    double rel[2], kw[2], rp[2], rd[2], gp[2], po[2], dob[2];
+    double rel[2], kw[2], rp[2], rd[2], gp[2], po[2], dob[2], rl[2];
     for (int q = 0; q < 2; ++q) {
         po[q] = tc[5 * q + 2];
         dob[q] = tr[4 * q + 2] + tc[5 * q + 3];
@@ -87,6 +91,13 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[kColPart
         kw[q] = sqrt(w * w * tr[4 * q + 0] + tc[5 * q + 0] / (w * w) + g * g);
         if (!isfinite(rel[q])) rel[q] = INFINITY;
         if (!isfinite(kw[q])) kw[q] = INFINITY;
+        rl[q] = rel[q];
+        if (lag) {
+            const double dl = tr[4 * q + 2] + lag[2 + q];
+            const double gl = fabs(po[q] - dl) / (1.0 + fabs(po[q]) + fabs(dl));
+            rl[q] = fmax(rp[q], fmax(sqrt(lag[q]) * inv_nc, gl));
+            if (!isfinite(rl[q])) rl[q] = INFINITY;
+        }
     }
     c.last_avg_kkt = rel[0];
     c.last_cur_kkt = rel[1];
@@ -98,7 +109,7 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[kColPart
         c.kkt_last = kw[1];
         c.kkt_prev_cand = kw[1];
         c.rel_kkt = rel[1]; c.rel_p = rp[1]; c.rel_d = rd[1]; c.rel_gap = gp[1];
-        c.pobj = po[1]; c.dobj = dob[1];
+        c.pobj = po[1]; c.dobj = dob[1]; c.rel_kkt_lagr = rl[1];
         c.apply = AP_CANDIDATE | AP_RESTART;   // the start point is the first restart point
         return;
     }
@@ -144,7 +155,7 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[kColPart
         c.done = 1;
         c.choice = best == 0 ? 1 : 0;
         c.rel_kkt = rel[best]; c.rel_p = rp[best]; c.rel_d = rd[best]; c.rel_gap = gp[best];
-        c.pobj = po[best]; c.dobj = dob[best];
+        c.pobj = po[best]; c.dobj = dob[best]; c.rel_kkt_lagr = rl[best];
         c.apply = (best == 0 ? AP_LOAD_AVG : 0) | save;
         return;
     }

@@ -123,6 +123,8 @@ struct Ctl {
     double omega_best;       // primal weight when the best point was taken
     uint64_t t_begin, t_end; // batched solver: device clock (ns) at the instance's start and end
     int32_t warm_used;       // batched solver: the instance started from its warm start
+    double rel_kkt_lagr;     // the returned point's error in the Lagrangian form (= rel_kkt unless
+                             // the single-LP engine measures the PDLP form)
 };
 
 enum TicketSlot { T_ROW_STEP = 0, T_COL_STEP, T_ROW_CHECK, T_COL_CHECK, T_APPLY, T_AUX0, T_AUX1, T_AUX2 };

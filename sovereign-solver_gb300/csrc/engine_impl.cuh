@@ -555,7 +555,7 @@ struct Engine : EngineBase {
         const int tail = std::min(grid_for(m), kSms * 4);
         const int apply_blocks = grid_for(std::max(n, m), kBlock, kSms * 8);
         const size_t part_row_n = (size_t)std::max(rp.bt.total_blocks, 1) * kRowPartials;
-        const size_t part_col_n = (size_t)(cp.bt.total_blocks + tail) * kColPartials;
+        const size_t part_col_n = (size_t)(cp.bt.total_blocks + tail) * (kColPartials + kLagPartials);
         const size_t part_aux_n = (size_t)std::max(apply_blocks, kSms * 16) * 3;
         const size_t nseg = (size_t)std::max(std::max(rp.units(), cp.units()), 1);
         const size_t ntk = (size_t)std::max(std::max(rp.ntickets, cp.ntickets), 1);
@@ -789,6 +789,7 @@ struct Engine : EngineBase {
         a.apply_blocks = apply_blocks;
         a.c = d_c; a.b = d_b; a.lo = d_lo; a.hi = d_hi;
         a.uniform_bounds = uniform;
+        a.far_residual = adaptive && opt.kkt_form == SPS_KKT_PDLP;
         a.lo_u = V(L0); a.hi_u = V(U0);
         a.dr = d_dr; a.dc = d_dc;
         a.idr = d_idr; a.idc = d_idc;
@@ -826,6 +827,13 @@ struct Engine : EngineBase {
     // ---------------------------------------------------------------- solve
     int nodes_per_window() const { return 2 * args.check_interval + 3; }
 
+    // column check in the error form the options ask for (the PDLP form's kernel adds
+    // the Lagrangian form's partials of the same points)
+    void launch_col_check(const Args<V>& a) {
+        if (a.far_residual) ad_col_check<V, true><<<a.cols.total_blocks, kBlock, 0, st>>>(a);
+        else ad_col_check<V, false><<<a.cols.total_blocks, kBlock, 0, st>>>(a);
+    }
+
     void launch_window(const Args<V>& a) {
         const int W = a.check_interval;
         const int gr = a.rows.total_blocks, gc = a.cols.total_blocks;
@@ -835,7 +843,7 @@ struct Engine : EngineBase {
                 ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
             }
             ad_row_check<V><<<gr, kBlock, 0, st>>>(a);
-            ad_col_check<V><<<gc, kBlock, 0, st>>>(a);
+            launch_col_check(a);
             ad_apply<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
         } else {
             for (int w = 0; w < W; ++w) {
@@ -981,7 +989,7 @@ struct Engine : EngineBase {
                 spmv_rows<V><<<gr, kBlock, 0, st>>>(args, args.X[0], args.AX[0]);
                 spmv_cols<V><<<gc, kBlock, 0, st>>>(args, args.Y[0], args.ATY[0]);
                 ad_row_check<V><<<gr, kBlock, 0, st>>>(args);
-                ad_col_check<V><<<gc, kBlock, 0, st>>>(args);
+                launch_col_check(args);
                 ad_apply<V><<<args.apply_blocks, kBlock, 0, st>>>(args);
                 launches += 6;
                 SPS_CK(cudaGetLastError());
@@ -1049,6 +1057,7 @@ struct Engine : EngineBase {
         res->rel_primal = h_ctl->rel_p;
         res->rel_dual = h_ctl->rel_d;
         res->rel_gap = h_ctl->rel_gap;
+        res->rel_kkt_lagrangian = adaptive ? h_ctl->rel_kkt_lagr : h_ctl->rel_kkt;
         res->primal_weight = h_ctl->omega;
         res->step_size = h_ctl->eta;
         res->setup_ms = setup_ms;

@@ -35,6 +35,7 @@ struct Args {
     const V* c; const V* b; const V* lo; const V* hi;
     V lo_u, hi_u;
     int32_t uniform_bounds;
+    int32_t far_residual;      // SPS_KKT_PDLP: far finite bounds leave the dual objective
     const double* dr; const double* dc;
     const double* idr; const double* idc;    // adaptive: 1 / dr, 1 / dc (the checks multiply)
     const V* tau; const V* sigma;
@@ -294,19 +295,23 @@ SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
         for (int q = 0; q < kRowPartials; ++q) a.part_row[(size_t)blockIdx.x * kRowPartials + q] = e.p[q];
 }
 
-template <class V>
+// Far = true: the PDLP error form (far finite bounds leave the dual objective),
+// with the Lagrangian form's dual residual and bound terms as kLagPartials more
+// partials; Far = false: the Lagrangian form (the default).
+template <class V, bool Far>
 struct AdColCheckEpi {
+    static constexpr int NP = kColPartials + (Far ? kLagPartials : 0);
     const Args<V>* a;
     const V *xs, *xlb, *xc, *xl;
     V* atya;
     double inv_w;
     // per point: dres_s^2, dres_o^2, c^T x, bound terms, ||x - x_last||^2; then for the
     // change since the last restart: cone residual^2 of -K^T dy, its bound terms,
-    // recession-cone violation^2 of dx, c^T dx
-    double p[kColPartials] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    // recession-cone violation^2 of dx, c^T dx; with Far, the Lagrangian form's
+    // dres_o^2 of both points, then its bound terms of both points
+    double p[NP] = {};
     bool nonneg;               // every column in [0, +inf): the bound terms vanish
     using Pre = NoPre;
-    static constexpr int NP = kColPartials;
     using R = double;
     __device__ __forceinline__ void zero() { for (int q = 0; q < NP; ++q) p[q] = 0.0; }
     __device__ __forceinline__ void export_to(double* d) const { for (int q = 0; q < NP; ++q) d[q] = p[q]; }
@@ -331,6 +336,7 @@ struct AdColCheckEpi {
             p[5 * q + 2] += cj * xv;
             const double d = xv - double(xl[j]);
             p[5 * q + 4] += d * d;
+            if constexpr (Far) p[kColPartials + q] += dor * dor;   // a zero lower bound is never far
         }
         const double lv = fmin(double(a->ATYl[j]) - acc[1], 0.0);
         p[10] += lv * lv;
@@ -347,16 +353,25 @@ struct AdColCheckEpi {
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const double rc = cj - acc[q];
-            const double lam = (hl && hh) ? rc : hl ? fmax(rc, 0.0) : hh ? fmin(rc, 0.0) : 0.0;
+            const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
+            // PDLP form: a bound farther from x than |x| (a scale-free test) takes no part of rc
+            const bool nl = hl && (!Far || fabs(xv - lo) <= fabs(xv));
+            const bool nh = hh && (!Far || fabs(xv - hi) <= fabs(xv));
+            const double lam = (nl && nh) ? rc : nl ? fmax(rc, 0.0) : nh ? fmin(rc, 0.0) : 0.0;
             const double dres = rc - lam;
             p[5 * q + 0] += dres * dres;
             const double dor = dres * idc;
             p[5 * q + 1] += dor * dor;
-            const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
             p[5 * q + 2] += cj * xv;
-            p[5 * q + 3] += (hl ? lo * fmax(lam, 0.0) : 0.0) + (hh ? hi * fmin(lam, 0.0) : 0.0);
+            p[5 * q + 3] += (nl ? lo * fmax(lam, 0.0) : 0.0) + (nh ? hi * fmin(lam, 0.0) : 0.0);
             const double d = xv - double(xl[j]);
             p[5 * q + 4] += d * d;
+            if constexpr (Far) {    // the Lagrangian form of the same point
+                const double lg = (hl && hh) ? rc : hl ? fmax(rc, 0.0) : hh ? fmin(rc, 0.0) : 0.0;
+                const double dl = (rc - lg) * idc;
+                p[kColPartials + q] += dl * dl;
+                p[kColPartials + 2 + q] += (hl ? lo * fmax(lg, 0.0) : 0.0) + (hh ? hi * fmin(lg, 0.0) : 0.0);
+            }
         }
         const double lr = -(acc[1] - double(a->ATYl[j]));
         const double lp = (hl && hh) ? lr : hl ? fmax(lr, 0.0) : hh ? fmin(lr, 0.0) : 0.0;
@@ -369,28 +384,31 @@ struct AdColCheckEpi {
     }
 };
 
-template <class V>
+template <class V, bool Far>
 SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
+    using Epi = AdColCheckEpi<V, Far>;
+    constexpr int NP = Epi::NP;
     Ctl* ctl = a.ctl;
     if (ctl->done) return;
-    __shared__ double sm[kWarps * kColPartials];
+    __shared__ double sm[kWarps * NP];
     __shared__ bool last;
     const int cur = ctl->cur;
     const bool has_avg = ctl->w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
     GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], inv_w};
-    AdColCheckEpi<V> e{&a, has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], a.xl, a.ATYa, inv_w};
+    Epi e{&a, has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], a.xl, a.ATYa, inv_w};
     e.nonneg = a.uniform_bounds && a.lo_u == V(0) && isinf(a.hi_u) && a.hi_u > V(0);
     visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e);
-    if (!publish_partials<kColPartials>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
-    double tc[kColPartials], tr[kRowPartials];
-    gather_partials<kColPartials>(tc, a.part_col, gridDim.x, sm);
+    if (!publish_partials<NP>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
+    double tc[NP], tr[kRowPartials];
+    gather_partials<NP>(tc, a.part_col, gridDim.x, sm);
     gather_partials<kRowPartials>(tr, a.part_row, a.rows.total_blocks, sm);
-    add_segment_rows<kColPartials>(tc, a.csc, sm);
+    add_segment_rows<NP>(tc, a.csc, sm);
     add_segment_rows<kRowPartials>(tr, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_CHECK] = 0;
-    decide_check(*ctl, tc, tr, a.inv_nb, a.inv_nc, stop_requested(ctl, a.abort_flag));
+    decide_check(*ctl, reinterpret_cast<const double(&)[kColPartials]>(tc), tr, a.inv_nb, a.inv_nc,
+                 stop_requested(ctl, a.abort_flag), Far ? tc + kColPartials : nullptr);
 }
 
 template <class V>

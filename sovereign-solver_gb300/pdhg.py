@@ -90,17 +90,22 @@ class _Desc:
 
 def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, tol=PDHG_TOL,
                  check_interval=0, ruiz_iters=10, time_limit=0.0, graph_mode=2, device=0,
-                 max_blocks=0, escalate="fp64", warm_fallback=True) -> N.Options:
+                 max_blocks=0, escalate="fp64", warm_fallback=True, kkt_form="lagrangian") -> N.Options:
     """Options for ``sps_create``.  ``escalate`` (adaptive FP32): "fp64" continues a
     stalled solve in FP64 from its best point, "stop" ends it with status
     "stalled", "off" keeps iterating in FP32.  ``warm_fallback``: start cold when
-    a warm start's relative KKT error is above the cold start's."""
+    a warm start's relative KKT error is above the cold start's.  ``kkt_form``
+    (adaptive mode): "lagrangian" puts every finite bound into the dual
+    objective; "pdlp" leaves out bounds farther from x_j than |x_j| and counts
+    the reduced cost they would absorb as dual residual (PDLP's default)."""
     if mode not in N.MODES:
         raise ValueError(f"Unknown mode {mode!r}. Choose 'adaptive' or 'reference'.")
     if precision not in N.PRECISIONS:
         raise ValueError(f"Unknown precision {precision!r}. Choose 'fp32' or 'fp64'.")
     if escalate not in N.ESCALATE:
         raise ValueError(f"Unknown escalate {escalate!r}. Choose 'fp64', 'stop' or 'off'.")
+    if kkt_form not in N.KKT_FORMS:
+        raise ValueError(f"Unknown kkt_form {kkt_form!r}. Choose 'lagrangian' or 'pdlp'.")
     o = N.Options()
     N.load().sps_options_init(C.byref(o))
     o.mode, o.precision = N.MODES[mode], N.PRECISIONS[precision]
@@ -110,6 +115,7 @@ def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, to
     o.max_blocks = int(max_blocks)
     o.escalate = N.ESCALATE[escalate]
     o.warm_fallback = 1 if warm_fallback else 0
+    o.kkt_form = N.KKT_FORMS[kkt_form]
     return o
 
 
@@ -190,6 +196,7 @@ def to_result(problem, r: N.Result, x, y, mode, precision) -> SolveResult:
         "setup_ms": float(r.setup_ms), "solve_ms": float(r.solve_ms),
         "kernel_launches": int(r.kernel_launches), "returned_average": bool(r.returned_average),
         "escalated": bool(r.escalated), "warm_start_used": bool(r.warm_start_used),
+        "rel_kkt_lagrangian": float(r.rel_kkt_lagrangian),
     }
     msg = f"{mode}/{precision} PDHG on GPU: rel_kkt={r.rel_kkt:.3e}"
     return SolveResult(status, x, obj, int(r.iterations), message=msg, y=y,
@@ -199,17 +206,18 @@ def to_result(problem, r: N.Result, x, y, mode, precision) -> SolveResult:
 def solve_lp_pdhg(problem, max_iters: int = MAX_PDHG_ITERS, tol: float = PDHG_TOL, *,
                   mode: str = "adaptive", precision: str = "fp32", warm_start=None,
                   time_limit: float = 0.0, graph_mode: int = 2, check_interval: int = 0,
-                  device: int = 0, escalate: str = "fp64") -> SolveResult:
+                  device: int = 0, escalate: str = "fp64", kkt_form: str = "lagrangian") -> SolveResult:
     """Solve an LP with restarted PDHG on the GPU (``solver/lp/pdhg.py:152``).
 
     ``warm_start`` = (x0, y0, omega0) starts from a given point (adaptive mode).
     Non-convergence is not an error: status ``"iteration_limit"``.  With FP32
     iterates a solve whose error stops halving continues in FP64 from its best
-    point (``escalate="fp64"``; ``stats["escalated"]`` tells).
+    point (``escalate="fp64"``; ``stats["escalated"]`` tells).  ``kkt_form`` picks
+    the measure ``tol`` applies to (``make_options``).
     """
     with PDHGEngine(problem, mode=mode, precision=precision, max_iters=max_iters, tol=tol,
                     time_limit=time_limit, graph_mode=graph_mode, check_interval=check_interval,
-                    device=device, escalate=escalate) as eng:
+                    device=device, escalate=escalate, kkt_form=kkt_form) as eng:
         if warm_start is not None:
             x0, y0, w0 = (tuple(warm_start) + (None, None, 0.0))[:3]
             eng.warm_start(x0, y0, w0 or 0.0)

@@ -114,6 +114,18 @@ def test_unknown_device_and_method():
         sps.Solver().solve(method="pdhg")
 
 
+def test_kkt_form_rejected_where_it_does_not_apply():
+    """The PDLP error form is an option of the adaptive single-LP engine: the
+    reference mode and the batched solver reject it before any device work."""
+    p = _lp()
+    with pytest.raises(ValueError, match="kkt_form"):
+        pdhg.solve_lp_pdhg(p, mode="reference", kkt_form="pdlp")
+    with pytest.raises(ValueError, match="kkt_form"):
+        pdhg.solve_lp_pdhg(p, kkt_form="strict")
+    with pytest.raises(ValueError, match="Lagrangian"):
+        sps.PDHGBatch([p, p], kkt_form="pdlp")
+
+
 def test_get_available_device_values():
     assert sps.get_available_device() in ("cuda", "cpu")
 
@@ -125,18 +137,12 @@ def test_no_gpu_fails_loudly():
 
 
 def test_integration_stub_matches_the_abi():
-    """The ctypes stub a maintainer would paste into the reference tree (the
-    first Python block of INTEGRATION.md's C ABI section) declares the same
-    struct layouts as the package's own binding, which the test above checks
-    against the header."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    sec = text[text.index("## 2. C ABI binding"):]
-    code = sec[sec.index("```python") + len("```python"):]
-    code = code[:code.index("```")]
-    classes = code[code.index("class Desc"):code.index("def solve_lp_pdhg")]
-    ns = {"C": C, "i32p": C.POINTER(C.c_int32), "f64p": C.POINTER(C.c_double)}
-    exec(classes, ns)
-    for stub, ours in ((ns["Desc"], N.ProblemDesc), (ns["Opts"], N.Options), (ns["Res"], N.Result)):
+    """The ctypes stub a maintainer would paste into the reference tree
+    (``tests/integration_stub.py`` holds its struct declarations) declares the
+    same struct layouts as the package's own binding, which the test above
+    checks against the header."""
+    import integration_stub as stub_mod
+    for stub, ours in ((stub_mod.Desc, N.ProblemDesc), (stub_mod.Opts, N.Options), (stub_mod.Res, N.Result)):
         assert C.sizeof(stub) == C.sizeof(ours), stub.__name__
         assert [f for f, _ in stub._fields_] == [f for f, _ in ours._fields_], stub.__name__
         for f, _ in stub._fields_:
