@@ -8,11 +8,20 @@ one complete solve.  ``value`` = solves/s with the problem resident in HBM
 public C-ABI call from pinned host buffers (upload + layout + solve + solution
 read-back inside the timed region).
 
+The default run adds the metric's other parts as ``subrecords`` of the same
+line, each with its own steps, clocks, roofline and CPU baseline: the power-law
+LP (1M x 2M, ~21M nonzeros; SpMV rooflines of both passes), the batch of 4096
+planted LPs (solves/s, p50/p99 attempts) and the learned warm start on 1000
+held-out transportation seeds (warm batched against cold single-instance time
+per solve).  ``--no-subrecords`` skips them.
+
 ``--impl reference`` times the reference algorithm (the oracle's C + OpenMP
-restatement of ``solver/lp/pdhg.py``, all host threads) on the same workload.
+restatement of ``solver/lp/pdhg.py``, all host threads) on the same workload;
+both arms carry the same ``config`` dict.
 
 Multi-GPU: replicas (each rank solves its own seed of the workload; no
-collective), value = total solves / slowest rank's time.
+collective), value = total solves / slowest rank's time.  ``--gpus N`` without
+a torch.distributed environment relaunches the script as N ranks.
 """
 
 from __future__ import annotations
@@ -215,8 +224,9 @@ def run_ours(args, rank, world):
 
     p, info, cfg = make_workload(args.config, seed=args.seed + rank, powerlaw_nnz=args.powerlaw_nnz)
     hbm, peak_kind = peaks()
+    form = kkt_form_of(args)
     eng = sps.PDHGEngine(p, tol=args.tol, max_iters=args.max_iters, device=args.device,
-                         graph_mode=args.graph_mode)
+                         graph_mode=args.graph_mode, kkt_form=form)
     for _ in range(args.warmup):
         r = eng.solve_raw()
     barrier(world)
@@ -244,7 +254,7 @@ def run_ours(args, rank, world):
             pinned.append(a)
             seen.add(a.ctypes.data)
     opts = pdhg.make_options(tol=args.tol, max_iters=args.max_iters, device=args.device,
-                             graph_mode=args.graph_mode)
+                             graph_mode=args.graph_mode, kkt_form=form)
     xo, yo = np.empty(d.n), np.empty(d.m_ub + d.m_eq)
     for a in (xo, yo):
         if lib.sps_pin_host(a.ctypes.data, a.nbytes) == 0:
@@ -274,10 +284,8 @@ def run_ours(args, rank, world):
     dom = "col" if kt[1] >= kt[0] else "row"
     dom_ms = kt[1] if dom == "col" else kt[0]
     achieved = ib[dom] / (dom_ms / 1e3) / 1e9
-    obj_err = None
-    if "obj_star" in info:
-        obj_err = abs(float(res.objective) - info["obj_star"]) / (1 + abs(info["obj_star"]))
     status = N.STATUS.get(res.status, str(res.status))
+    it_med = int(np.median(iters))
     line = {
         "metric": METRIC,
         "value": value, "unit": "solves/s",
@@ -285,11 +293,16 @@ def run_ours(args, rank, world):
         "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {**cfg, "tol_rel_kkt": args.tol, "mode": "adaptive", "precision": "fp32 iterates, fp64 checks",
-                   "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)"},
-        "iters_to_tol": int(np.median(iters)),
+        "config": {**cfg, "tol_rel_kkt": args.tol},
+        "mode": "adaptive", "precision": "fp32 iterates, fp64 checks (fp64 continuation if fp32 stalls)",
+        "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)",
+        "kkt_form": form,
+        "iters_to_tol": it_med,
         "sec_to_tol": t_max / args.steps,
-        "status": status, "rel_kkt": float(res.rel_kkt), "obj_error_vs_planted": obj_err,
+        "s_per_iter": t_max / args.steps / max(it_med, 1),
+        "status": status, "rel_kkt": float(res.rel_kkt), "rel_kkt_lagrangian": float(res.rel_kkt_lagrangian),
+        "escalated_fp64": bool(res.escalated),
+        "obj_error": objective_error(args.config, args.seed + rank, float(res.objective), info),
         "restarts": int(res.restarts), "setup_ms": float(res.setup_ms),
         "host_wall_s_timed": wall,
         "gpu_launches": launches,
@@ -306,10 +319,37 @@ def run_ours(args, rank, world):
                                         ((kt[0] if dom == "col" else kt[1]) / 1e3) / 1e9)},
         "clocks": clk.summary(),
     }
+    # whole solve: both passes' algorithmic bytes per attempt x attempts / solve time (the checks,
+    # one per 64 attempts, move more bytes that are not counted)
+    line["solve_avg_gbs"] = (ib["row"] + ib["col"]) * it_med / (t_max / args.steps) / 1e9
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(p, args)
-    print(json.dumps(line), flush=True)
     return line
+
+
+def kkt_form_of(args) -> str:
+    """The error form the engine terminates on: the Lagrangian form by default;
+    the PDLP form on the power-law LP, whose 10-wide bounds far from x* put the
+    Lagrangian dual bound at a relative gap that FP32 iterates cannot close."""
+    if args.kkt_form != "auto":
+        return args.kkt_form
+    return "pdlp" if args.config == 2 else "lagrangian"
+
+
+def objective_error(config: int, seed: int, objective: float, info: dict):
+    """|objective - optimum| / (1 + |optimum|) against the planted optimum or the
+    exact optimum committed with the fixtures (HiGHS dual simplex), else None."""
+    if "obj_star" in info:
+        opt, src = info["obj_star"], "planted optimum c^T x* = b^T y*"
+    else:
+        key = {1: f"transport_1000x2000_s{seed}", 4: f"transport_family_200x400_s{seed}"}.get(config)
+        try:
+            with open(os.path.join(ROOT, "tests", "golden", "optima.json")) as f:
+                entry = json.load(f)[key]
+        except (OSError, KeyError, TypeError, ValueError):
+            return None
+        opt, src = float(entry["objective"]), f"exact optimum ({entry['solver']}, tests/golden/optima.json)"
+    return {"value": abs(objective - opt) / (1 + abs(opt)), "objective": objective, "optimum": opt, "against": src}
 
 
 def _ref_solve_one(k):
@@ -422,11 +462,11 @@ def run_batch(args, rank, world):
         "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": (f"batched: {args.batch} planted LPs per GPU, m log-uniform [50,5000], "
-                                f"n = m*U[1.5,3], 10-50 nnz/column, u=2 (total nnz {sum(nnz)})"),
-                   "tol_rel_kkt": args.tol, "mode": "adaptive, one persistent launch (graph replay)",
-                   "precision": "fp32 iterates, fp64 checks, fp64 continuation of stalled instances",
-                   "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)"},
+        "config": {"workload": batch_workload(args.batch), "tol_rel_kkt": args.tol},
+        "total_nnz": int(sum(nnz)),
+        "mode": "adaptive, one persistent launch (graph replay)",
+        "precision": "fp32 iterates, fp64 checks, fp64 continuation of stalled instances",
+        "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)",
         "iters_p50": float(np.percentile(its, 50)), "iters_p99": float(np.percentile(its, 99)),
         "iters_max": int(its.max()), "optimal": int(sum(r.status == "optimal" for r in res)),
         "escalated_fp64": int(esc), "handed_off": int(hand),
@@ -443,8 +483,12 @@ def run_batch(args, rank, world):
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = batch_cpu_baseline(args)
-    print(json.dumps(line), flush=True)
     return line
+
+
+def batch_workload(count: int) -> str:
+    return (f"batched: {count} planted LPs per GPU (seeds = instance index), m log-uniform [50,5000], "
+            f"n = m*U[1.5,3], 10-50 nnz/column, u=2")
 
 
 WEIGHTS = os.path.join(ROOT, "sovereign-solver_gb300", "data", "warmstart_transport_200x400.npz")
@@ -554,11 +598,10 @@ def run_warmstart(args, rank, world):
         "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": (f"learned warm start: transportation family 200x400 (n=80k, m=600, nnz=160k), "
-                                f"{args.batch} held-out seeds per GPU, network trained on seeds 0..19999"),
-                   "tol_rel_kkt": args.tol, "mode": "GNN inference + warm-started batched PDHG (cold fallback on)",
-                   "precision": "fp32 iterates, fp64 checks; GNN bf16 weights, fp32 accumulation",
-                   "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)"},
+        "config": {"workload": warmstart_workload(args.batch), "tol_rel_kkt": args.tol},
+        "mode": "GNN inference + warm-started batched PDHG (cold fallback on)",
+        "precision": "fp32 iterates, fp64 checks; GNN bf16 weights, fp32 accumulation",
+        "parallelism": f"replicas x{world}", "l2": "working set > 129 MB L2 (inputs larger than L2)",
         "warm_iters_median": float(np.median(wi)), "cold_iters_median": float(np.median(ci)),
         "warm_iters_mean": float(wi.mean()), "cold_iters_mean": float(ci.mean()),
         "warm_used": int(sum(r.stats["warm_start_used"] for r in warm)),
@@ -583,8 +626,12 @@ def run_warmstart(args, rank, world):
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(probs[0], args, ref_key=f"4:{TEST_SEED0}")
-    print(json.dumps(line), flush=True)
     return line
+
+
+def warmstart_workload(count: int) -> str:
+    return (f"learned warm start: transportation family 200x400 (n=80k, m=600, nnz=160k), "
+            f"{count} held-out seeds per GPU from {TEST_SEED0}, network trained on seeds 0..19999")
 
 
 def branching_node(args, rank, on_cpu=False):
@@ -683,12 +730,12 @@ def run_branching(args, rank, world):
         "ms_per_step": t_max * 1e3 / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": (f"strong branching: {len(kids)} child LPs of the {len(top)} most fractional "
-                                f"variables of a set-covering node, m=200, n=2000, nnz={nz}"),
-                   "tol_rel_kkt": args.tol, "mode": "adaptive batched, warm-started from the parent LP",
-                   "precision": "fp32 iterates, fp64 checks, fp64 continuation of stalled instances",
-                   "parallelism": f"replicas x{world}",
-                   "l2": "working set < 129 MB L2 (the 40 children's matrices, 1.3 MB, stay in L2)"},
+        "config": {"workload": BRANCH_WORKLOAD, "tol_rel_kkt": args.tol},
+        "nnz": int(nz),
+        "mode": "adaptive batched, warm-started from the parent LP",
+        "precision": "fp32 iterates, fp64 checks, fp64 continuation of stalled instances",
+        "parallelism": f"replicas x{world}",
+        "l2": "working set < 129 MB L2 (the 40 children's matrices, 1.3 MB, stay in L2)",
         "iters_p50": float(np.percentile(its, 50)), "iters_max": int(its.max()),
         "statuses": {s_: int(sum(r.status == s_ for r in res)) for s_ in sorted({r.status for r in res})},
         "infinite_gains": int(np.isinf(gains).sum()), "team": int(team), "persistent_blocks": int(blocks),
@@ -704,8 +751,11 @@ def run_branching(args, rank, world):
     }
     if args.cpu_baseline:
         line["cpu_baseline"] = branching_cpu_baseline(kids, lp.objective, args.cpu_budget)
-    print(json.dumps(line), flush=True)
     return line
+
+
+BRANCH_WORKLOAD = ("strong branching: the 40 child LPs of the 20 most fractional variables of a "
+                   "set-covering node, m=200, n=2000 (seed 0)")
 
 
 def cpu_baseline(p, args, ref_key=None):
@@ -736,7 +786,7 @@ def run_reference(args, rank, world):
     if args.config == 4:
         from sovereign_solver_gb300.workloads import TransportFamily
         p = TransportFamily().problem(TEST_SEED0)
-        cfg = {"workload": "transportation family 200x400, held-out seed 10000000 (one cold solve per step)"}
+        cfg = {"workload": warmstart_workload(args.batch or 1000)}
         ref_key = f"4:{TEST_SEED0}"
     else:
         p, info, cfg = make_workload(args.config, seed=args.seed, powerlaw_nnz=args.powerlaw_nnz)
@@ -765,7 +815,13 @@ def run_reference(args, rank, world):
         "s_per_iter": s_per_iter,
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
+    if ref_iters:
+        line["reference_run"] = {
+            "value_is": ("rate of producing the reference's own answer on this LP: the timed per-iteration "
+                         "cost x the iteration count of a full reference run made once in the build "
+                         "container (tests/golden/reference_iterations.json)"),
+            "iterations": n_it, "status": ref_iters["status"], "objective": ref_iters.get("objective"),
+            "reaches_tol": ref_iters["status"] == "optimal"}
     return line
 
 
@@ -784,12 +840,10 @@ def run_reference_batch(args, world):
         "metric": METRIC, "impl": "reference", "value": value, "unit": "solves/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-        "data": "synthetic", "config": {"workload": "batched planted LPs (the 32-LP sample of the 4096)",
-                                        "tol_rel_kkt": args.tol},
+        "data": "synthetic", "config": {"workload": batch_workload(args.batch or 4096), "tol_rel_kkt": args.tol},
         "cpu_baseline": cb,
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
     return line
 
 
@@ -807,13 +861,11 @@ def run_reference_branching(args, world):
         "metric": METRIC, "impl": "reference", "value": value, "unit": "child LPs/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp64",
-        "data": "synthetic", "config": {"workload": (f"strong branching: the {len(kids)} child LPs of a "
-                                                     f"set-covering node, m=200, n=2000"),
-                                        "tol_rel_kkt": "exact (simplex)"},
+        "data": "synthetic", "config": {"workload": BRANCH_WORKLOAD, "tol_rel_kkt": args.tol},
+        "solver_tolerance": "exact (simplex, one solve per child as the reference's _lp_gain)",
         "cpu_baseline": cb,
         "e2e": {"value": value, "unit": "child LPs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
     return line
 
 
@@ -855,6 +907,51 @@ def gather(world, obj):
     return out
 
 
+def torchrun_command(argv, gpus: int, port: int):
+    """The command that relaunches this script as ``gpus`` ranks of one node
+    (one process per GPU, rendezvous on 127.0.0.1)."""
+    return [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={gpus}",
+            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__), *argv]
+
+
+def free_port() -> int:
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+SUBRECORDS = (("powerlaw_1Mx2M", 2), ("batched_4096", 3), ("learned_warm_start_1000", 4))
+
+
+def subrecords(args, rank, world):
+    """The metric's other parts, measured in the same run as the default line:
+    the power-law LP (SpMV roofline of both passes), the 4096-LP batch (solves/s,
+    p50/p99 attempts) and the learned warm start (warm batched against cold
+    single-instance wall time per solve).  Each has its own steps, clocks,
+    roofline and CPU baseline; fewer timed steps than the default line, since
+    one step of these is a whole batch or a multi-second solve."""
+    import copy
+    out = {}
+    for name, cfg in SUBRECORDS:
+        sub = copy.copy(args)
+        sub.config, sub.steps, sub.warmup = cfg, args.sub_steps, args.sub_warmup
+        sub.e2e_steps = 1
+        sub.cpu_budget = min(args.cpu_budget, 10.0)
+        sub.batch = {3: 4096, 4: 1000}.get(cfg)
+        try:
+            line = RUNNERS[cfg](sub, rank, world)
+            line.pop("metric", None)
+            out[name] = line
+        except Exception as exc:          # a failed part is reported, the default line still prints
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+        log(f"subrecord {name}: {json.dumps(out[name])[:300]}")
+    return out
+
+
+RUNNERS = {0: run_ours, 1: run_ours, 2: run_ours, 3: run_batch, 4: run_warmstart, 5: run_branching}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -871,6 +968,8 @@ def main():
     ap.add_argument("--powerlaw-nnz", type=int, default=20_000_000,
                     help="config 2: nonzeros the Zipf(1.5) row lengths are rescaled to; 0 = lengths as drawn "
                          "(about 1.1e8 nonzeros)")
+    ap.add_argument("--kkt-form", default="auto", choices=["auto", "lagrangian", "pdlp"],
+                    help="single-LP error form the solve terminates on: auto = pdlp for config 2, else lagrangian")
     ap.add_argument("--single-sample", type=int, default=32)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--tol", type=float, default=TOL)
@@ -878,24 +977,32 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-subrecords", dest="subrecords", action="store_false",
+                    help="default workload only: skip the power-law, batched and warm-start parts")
+    ap.add_argument("--sub-steps", type=int, default=1, help="timed steps of each part of the default run")
+    ap.add_argument("--sub-warmup", type=int, default=3, help="warm-up steps of each part of the default run")
     ap.add_argument("--graph-mode", type=int, default=2,
                     help="2: one graph with a device-driven loop (default); 1: replayed window graph; "
                          "0: plain launches (what a profiler's launch list can see kernel by kernel)")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        # one process per GPU: relaunch under torch.distributed.run
+        cmd = torchrun_command(sys.argv[1:], args.gpus, free_port())
+        raise SystemExit(subprocess.call(cmd))
     rank, world = init_dist()
     args.device = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
-        run_reference(args, rank, world)
-    elif args.config == 3:
-        args.batch = args.batch or 4096
-        run_batch(args, rank, world)
-    elif args.config == 4:
-        args.batch = args.batch or 1000
-        run_warmstart(args, rank, world)
-    elif args.config == 5:
-        run_branching(args, rank, world)
+        line = run_reference(args, rank, world)
     else:
-        run_ours(args, rank, world)
+        if args.config == 3:
+            args.batch = args.batch or 4096
+        elif args.config == 4:
+            args.batch = args.batch or 1000
+        line = RUNNERS[args.config](args, rank, world)
+        if args.subrecords and args.config == 1 and world == 1 and line is not None:
+            line["subrecords"] = subrecords(args, rank, world)
+    if line is not None:
+        print(json.dumps(line), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
