@@ -207,6 +207,47 @@ def reference_sample(p, budget_s: float):
             "threads": pdhg_ref_c.threads()}
 
 
+def reference_gpu_path(p, iters: int = 300):
+    """The reference's own GPU path (``solver/lp/pdhg_gpu.py:315-443``: torch-CUDA
+    FP64 sparse CSR, host KKT check every 50 iterations), unmodified, from its
+    install in baseline/_ref, on the same LP: seconds per iteration as the
+    difference of a short and a long capped run (setup excluded).  A reported
+    secondary figure; the reference arm's value stays the CPU path."""
+    ref = os.path.join(ROOT, "baseline", "_ref")
+    if not os.path.isdir(os.path.join(ref, "solver")):
+        return {"unavailable": "the reference is not installed in baseline/_ref"}
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return {"unavailable": "torch sees no CUDA device"}
+    except ImportError:
+        return {"unavailable": "torch is not importable"}
+    if ref not in sys.path:
+        sys.path.insert(0, ref)
+    from solver.lp.pdhg_gpu import DeviceEngine, solve_lp_pdhg_gpu
+    from solver.problem import Problem as RefProblem
+    rp = RefProblem(c=np.asarray(p.c, float), A_ub=p.A_ub, b_ub=np.asarray(p.b_ub, float), A_eq=p.A_eq,
+                    b_eq=np.asarray(p.b_eq, float), lb=np.asarray(p.lb, float), ub=np.asarray(p.ub, float),
+                    integer_mask=np.zeros(p.n_vars, dtype=bool))
+    backend = DeviceEngine(device="cuda").backend
+    short = max(50, iters // 3)
+
+    def timed(k):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = solve_lp_pdhg_gpu(rp, device="cuda", max_iters=k)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, r
+    timed(short)                                 # warm-up: torch / cuSPARSE initialisation
+    t_s, _ = timed(short)
+    t_l, r = timed(iters)
+    return {"s_per_iter": (t_l - t_s) / (iters - short), "backend": backend, "dtype": "fp64",
+            "sample": (f"solve_lp_pdhg_gpu(device='cuda') capped at {short} and {iters} iterations, "
+                       f"per-iteration time = difference / {iters - short} (standard form, upload and "
+                       f"setup cancel); status at the cap {r.status!r}"),
+            "torch": torch.__version__}
+
+
 def load_reference_iterations(config: int):
     path = os.path.join(ROOT, "tests", "golden", "reference_iterations.json")
     try:
@@ -815,6 +856,11 @@ def run_reference(args, rank, world):
         "s_per_iter": s_per_iter,
         "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
+    if args.config in (0, 1) and args.ref_gpu:
+        try:
+            line["reference_gpu_path"] = reference_gpu_path(p)
+        except Exception as exc:       # a secondary figure: its failure is reported, not fatal
+            line["reference_gpu_path"] = {"unavailable": f"{type(exc).__name__}: {exc}"}
     if ref_iters:
         line["reference_run"] = {
             "value_is": ("rate of producing the reference's own answer on this LP: the timed per-iteration "
@@ -977,6 +1023,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-ref-gpu", dest="ref_gpu", action="store_false",
+                    help="reference arm: skip timing the reference's own torch-CUDA path from baseline/_ref")
     ap.add_argument("--no-subrecords", dest="subrecords", action="store_false",
                     help="default workload only: skip the power-law, batched and warm-start parts")
     ap.add_argument("--sub-steps", type=int, default=1, help="timed steps of each part of the default run")
