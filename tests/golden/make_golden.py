@@ -3,7 +3,9 @@
 Run from the repository root, in a container where the reference checkout is
 mounted (it is pure Python and imports with NumPy + SciPy):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference checkout>
+
+(or with the checkout's path in SPS_REFERENCE_ROOT and no argument).
 
 Writes
 ------
@@ -158,4 +160,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPS_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit(f"usage: python {sys.argv[0]} <reference checkout> (or set SPS_REFERENCE_ROOT)")
+    main(root)

@@ -16,7 +16,9 @@ call stubbed): it is unbounded, and the reference runs it to its cap.
 Run from the repository root, in a container where the reference checkout is
 mounted (pure Python, NumPy + SciPy):
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_stress_golden.py /root/reference
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_stress_golden.py <reference checkout>
+
+(or with the checkout's path in SPS_REFERENCE_ROOT and no argument).
 
 Writes ``stress_problems.npz`` (CSR arrays, the layout of
 ``small_problems.npz``) and ``stress_golden.json`` (reference result and the
@@ -98,4 +100,7 @@ def main(ref_root: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SPS_REFERENCE_ROOT")
+    if not root:
+        raise SystemExit(f"usage: python {sys.argv[0]} <reference checkout> (or set SPS_REFERENCE_ROOT)")
+    main(root)

@@ -11,7 +11,10 @@ from sovereign_solver_gb300.mps import read_mps
 from fixtures import load_golden, load_problems
 from oracle import simplex
 
-REF_INSTANCES = "/root/reference/benchmarks/instances"
+# the reference checkout's Netlib instances, where a checkout is present (path in
+# SPS_REFERENCE_ROOT); the committed fixtures hold what its reader made of them
+REF_ROOT = os.environ.get("SPS_REFERENCE_ROOT", "")
+REF_INSTANCES = os.path.join(REF_ROOT, "benchmarks", "instances") if REF_ROOT else ""
 GOLD = load_golden()
 PROBS = load_problems()
 
@@ -24,9 +27,9 @@ def _rows(A, b):
 
 @pytest.mark.parametrize("name", ["afiro", "blending", "adlittle", "brandy"])
 def test_netlib_matches_reference_reader(name):
-    path = os.path.join(REF_INSTANCES, name + ".mps")
-    if not os.path.exists(path):
-        pytest.skip("reference instances not present")
+    path = os.path.join(REF_INSTANCES, name + ".mps") if REF_INSTANCES else ""
+    if not path or not os.path.exists(path):
+        pytest.skip("reference instances not present (set SPS_REFERENCE_ROOT to a reference checkout)")
     p, q = read_mps(path), PROBS[name]
     np.testing.assert_array_equal(p.c, q.c)
     np.testing.assert_array_equal(p.lb, q.lb)
@@ -40,9 +43,9 @@ def test_netlib_matches_reference_reader(name):
 
 @pytest.mark.parametrize("name", ["exmip1", "p0033", "p0548"])
 def test_milp_files_parse(name):
-    path = os.path.join(REF_INSTANCES, name + ".mps")
-    if not os.path.exists(path):
-        pytest.skip("reference instances not present")
+    path = os.path.join(REF_INSTANCES, name + ".mps") if REF_INSTANCES else ""
+    if not path or not os.path.exists(path):
+        pytest.skip("reference instances not present (set SPS_REFERENCE_ROOT to a reference checkout)")
     p = read_mps(path)
     p.validate()
     assert p.integer_mask.any()
