@@ -232,7 +232,12 @@ __device__ __forceinline__ uint64_t global_ns() {
 // All control flow below is warp-uniform, so full-mask shuffles are safe.
 
 constexpr int kUnroll = 8;
-constexpr int kFinishBatch = 8;      // partial loads in flight when a row's (slice's) last unit adds them
+// Partial loads in flight when a row's (slice's) last unit adds its units'
+// partials (the adds stay in unit order): 16 for one FP32 value per unit (a
+// transportation demand slice has 32 units: two round trips instead of four),
+// 8 where more registers per partial would spill at the step kernels' budget.
+template <int NV, class Acc>
+__host__ __device__ constexpr int finish_batch() { return NV * sizeof(Acc) <= 4 ? 16 : 8; }
 constexpr int kPassMinBlocks = 5;    // resident blocks per SM the iteration kernels are built for
 
 // SLICED: lane t of the warp owns row begin + 32*slice + t.  Two slices per
@@ -276,12 +281,26 @@ __device__ __forceinline__ void visit_slice_pair(const Bin& b, int s0, int s1, c
                 j[h][u] = ok ? __ldg(L.idx + p) : 0;
                 a[h][u] = ok ? Acc(__ldg(L.val + p)) : Acc(0);
             }
+        // in the two-point FP64 passes (the checks), steps past a slice's length
+        // (warp-uniform) add zeros: skip their gathers and products (half the FP64
+        // pipe time of a check on 2-nonzero slices); the sums are unchanged.  The
+        // one-point passes keep the straight-line form (their register budget).
+        if (NV < 2 || (k + 4 <= len[0] && k + 4 <= len[1])) {
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+            for (int h = 0; h < 2; ++h)
 #pragma unroll
-            for (int u = 0; u < 4; ++u)
+                for (int u = 0; u < 4; ++u)
 #pragma unroll
-                for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
+                    for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
+        } else {
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                    if (k + u < len[h])
+#pragma unroll
+                        for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
+        }
     }
     if (r[0] < b.end) e(r[0], b.kind, acc[0], pre[0]);
     if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
@@ -422,16 +441,17 @@ __device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, in
     Acc tot[NV];
 #pragma unroll
     for (int q = 0; q < NV; ++q) tot[q] = Acc(0);
-    // the row's segment partials, kFinishBatch loads in flight, added in order
-    for (int s0 = 0; s0 < nseg; s0 += kFinishBatch) {
-        Acc v[kFinishBatch][NV];
+    // the row's segment partials, finish_batch loads in flight, added in order
+    constexpr int FB = finish_batch<NV, Acc>();
+    for (int s0 = 0; s0 < nseg; s0 += FB) {
+        Acc v[FB][NV];
 #pragma unroll
-        for (int w = 0; w < kFinishBatch; ++w)
+        for (int w = 0; w < FB; ++w)
 #pragma unroll
             for (int q = 0; q < NV; ++q)
                 v[w][q] = s0 + w < nseg ? __ldcg(part + (size_t)(first + s0 + w) * NV + q) : Acc(0);
 #pragma unroll
-        for (int w = 0; w < kFinishBatch; ++w)
+        for (int w = 0; w < FB; ++w)
 #pragma unroll
             for (int q = 0; q < NV; ++q) tot[q] += v[w][q];
     }
@@ -477,6 +497,75 @@ __device__ __forceinline__ void add_segment_rows(T (&tot)[NP], const Layout<V>& 
     if (threadIdx.x == 0)
 #pragma unroll
         for (int p = 0; p < NP; ++p) tot[p] += s[p];
+}
+
+// In a kernel's last block: gather_partials followed by add_segment_rows, with
+// the first round of both's loads issued together (one L2 round trip fewer on
+// the serial tail of the pass); the same additions in the same order.
+template <int NP, class T, class V>
+__device__ __forceinline__ void gather_all_partials(T (&tot)[NP], const T* partials, int nblk,
+                                                    const Layout<V>& L, T* smem) {
+    __threadfence();
+    constexpr int B = 4;                       // as gather_partials
+    constexpr int BS = NP <= 2 ? 8 : 2;        // as add_segment_rows
+    const T* part = reinterpret_cast<const T*>(L.seg_rowpart);
+    T sv[BS][NP], bv[B][NP];
+#pragma unroll
+    for (int u = 0; u < BS; ++u) {
+        const int k = threadIdx.x + u * kBlock;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) sv[u][p] = k < L.nsegrows ? __ldcg(part + (size_t)k * NP + p) : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < B; ++u) {
+        const int b = threadIdx.x + u * kBlock;
+#pragma unroll
+        for (int p = 0; p < NP; ++p) bv[u][p] = b < nblk ? __ldcg(partials + (size_t)b * NP + p) : T(0);
+    }
+#pragma unroll
+    for (int p = 0; p < NP; ++p) tot[p] = T(0);
+#pragma unroll
+    for (int u = 0; u < B; ++u)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) tot[p] += bv[u][p];
+    for (int b0 = threadIdx.x + kBlock * B; b0 < nblk; b0 += kBlock * B) {
+        T v[B][NP];
+#pragma unroll
+        for (int u = 0; u < B; ++u) {
+            const int b = b0 + u * kBlock;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) v[u][p] = b < nblk ? __ldcg(partials + (size_t)b * NP + p) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < B; ++u)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) tot[p] += v[u][p];
+    }
+    block_sum<NP>(tot, smem);
+    T sacc[NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) sacc[p] = T(0);
+#pragma unroll
+    for (int u = 0; u < BS; ++u)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) sacc[p] += sv[u][p];
+    for (int k0 = threadIdx.x + kBlock * BS; k0 < L.nsegrows; k0 += kBlock * BS) {
+        T v[BS][NP];
+#pragma unroll
+        for (int u = 0; u < BS; ++u) {
+            const int k = k0 + u * kBlock;
+#pragma unroll
+            for (int p = 0; p < NP; ++p) v[u][p] = k < L.nsegrows ? __ldcg(part + (size_t)k * NP + p) : T(0);
+        }
+#pragma unroll
+        for (int u = 0; u < BS; ++u)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) sacc[p] += v[u][p];
+    }
+    block_sum<NP>(sacc, smem);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int p = 0; p < NP; ++p) tot[p] += sacc[p];
 }
 
 // SLAB: unit u of the bin = steps [c S, min(L, (c+1) S)) of slice s (S =
@@ -540,16 +629,17 @@ __device__ __forceinline__ void visit_slab_unit(const Bin& b, int u, const Layou
         const Acc* first = reinterpret_cast<const Acc*>(L.slab_part) + (size_t)(b.part0 + u - c) * 32 * NV;
 #pragma unroll
         for (int q = 0; q < NV; ++q) acc[q] = Acc(0);
-        // the slice's unit partials, kFinishBatch loads in flight, added in unit order
-        for (int w0 = 0; w0 < nunits; w0 += kFinishBatch) {
-            Acc v[kFinishBatch][NV];
+        // the slice's unit partials, finish_batch loads in flight, added in unit order
+        constexpr int FB = finish_batch<NV, Acc>();
+        for (int w0 = 0; w0 < nunits; w0 += FB) {
+            Acc v[FB][NV];
 #pragma unroll
-            for (int w = 0; w < kFinishBatch; ++w)
+            for (int w = 0; w < FB; ++w)
 #pragma unroll
                 for (int q = 0; q < NV; ++q)
                     v[w][q] = w0 + w < nunits ? __ldcg(first + (size_t)(w0 + w) * 32 * NV + lane * NV + q) : Acc(0);
 #pragma unroll
-            for (int w = 0; w < kFinishBatch; ++w)
+            for (int w = 0; w < FB; ++w)
 #pragma unroll
                 for (int q = 0; q < NV; ++q) acc[q] += v[w][q];
         }

@@ -128,6 +128,7 @@ struct Engine : EngineBase {
         int32_t ntickets = 0;           // SEGMENT rows and SLAB slices
         int32_t nslots = 0;             // epilogue partial slots: SEGMENT rows, SLAB slices
         int32_t nslab_units = 0;
+        std::vector<int64_t> bin_store; // stored entries per bin (the block shares' work measure)
     };
 
     // Blocks that give every warp of the bin work for its first step (warps
@@ -233,6 +234,67 @@ struct Engine : EngineBase {
         for (int t = 0; t < nt; ++t)
             pool.emplace_back(work, (int32_t)(j0 + cols * t / nt), (int32_t)(j0 + cols * (t + 1) / nt));
         for (auto& th : pool) th.join();
+    }
+
+    // Blocks of one launch over the bins: one resident wave (block_cap) shared by
+    // the bins in proportion to their work (stored entries plus a per-unit
+    // overhead of one 32-entry step), never more than one warp per unit.  The
+    // pass kernels and the check kernels (fewer resident blocks: more registers)
+    // each get their own shares of the same layout.
+    static void share_blocks(BinTable& bt, const std::vector<int64_t>& bin_store, int block_cap) {
+        int64_t need_total = 0;
+        double work_total = 0.0;
+        std::vector<double> work(bt.nbins);
+        for (int i = 0; i < bt.nbins; ++i) {
+            const Bin& b = bt.bin[i];
+            need_total += blocks_needed(b);
+            work[i] = double(bin_store[i]) + 32.0 * b.units;
+            work_total += work[i];
+        }
+        // When every bin's need fits the wave, every bin gets it (one step per
+        // warp); a proportional share here left a few warps two units in a row
+        // and the pass waited for them.
+        // Otherwise the shares are rounded down (at least one block, at most the
+        // need) and the blocks left go to the largest remainders, so the bins
+        // add up to the wave: rounding every share up put up to one block per
+        // bin past it, and those blocks waited for a free slot.
+        const int64_t budget = std::min<int64_t>(block_cap, need_total);
+        const int nb = bt.nbins;
+        std::vector<int64_t> share(nb), need(nb);
+        std::vector<double> raw(nb);
+        int64_t sum = 0;
+        for (int i = 0; i < nb; ++i) {
+            need[i] = blocks_needed(bt.bin[i]);
+            raw[i] = budget * work[i] / std::max(work_total, 1.0);
+            share[i] = need_total <= block_cap
+                           ? need[i]
+                           : std::max<int64_t>(1, std::min<int64_t>(need[i], (int64_t)std::floor(raw[i])));
+            sum += share[i];
+        }
+        while (sum < budget) {
+            int best = -1;
+            for (int i = 0; i < nb; ++i)
+                if (share[i] < need[i] && (best < 0 || raw[i] - share[i] > raw[best] - share[best])) best = i;
+            if (best < 0) break;
+            ++share[best];
+            ++sum;
+        }
+        while (sum > budget) {            // one-block floors of small bins: take from the largest share
+            int best = -1;
+            for (int i = 0; i < nb; ++i)
+                if (share[i] > 1 && (best < 0 || share[i] > share[best])) best = i;
+            if (best < 0) break;
+            --share[best];
+            --sum;
+        }
+        int blocks = 0;
+        for (int i = 0; i < nb; ++i) {
+            Bin& b = bt.bin[i];
+            b.nblocks = (int)share[i];
+            b.block_begin = blocks;
+            blocks += b.nblocks;
+        }
+        bt.total_blocks = blocks;
     }
 
     // Order: per kind, SLICED rows by decreasing length, then WARP rows, then
@@ -382,63 +444,11 @@ struct Engine : EngineBase {
         }
         P.fptr[R] = (int32_t)std::min<int64_t>(off, INT32_MAX);
         P.total = off;
-        // Blocks: one resident wave shared by the bins in proportion to their
-        // work (stored entries plus a per-unit overhead of one 32-entry step),
-        // never more than one warp per unit.
-        int64_t need_total = 0;
-        double work_total = 0.0;
-        std::vector<double> work(P.bt.nbins);
-        for (int i = 0; i < P.bt.nbins; ++i) {
-            const Bin& b = P.bt.bin[i];
-            need_total += blocks_needed(b);
-            work[i] = double(bin_store[i]) + 32.0 * b.units;
-            work_total += work[i];
-        }
-        // When every bin's need fits the wave, every bin gets it (one step per
-        // warp); a proportional share here left a few warps two units in a row
-        // and the pass waited for them.
-        // Otherwise the shares are rounded down (at least one block, at most the
-        // need) and the blocks left go to the largest remainders, so the bins
-        // add up to the wave: rounding every share up put up to one block per
-        // bin past it, and those blocks waited for a free slot.
-        const int64_t budget = std::min<int64_t>(block_cap, need_total);
-        const int nb = P.bt.nbins;
-        std::vector<int64_t> share(nb), need(nb);
-        std::vector<double> raw(nb);
-        int64_t sum = 0;
-        for (int i = 0; i < nb; ++i) {
-            need[i] = blocks_needed(P.bt.bin[i]);
-            raw[i] = budget * work[i] / std::max(work_total, 1.0);
-            share[i] = need_total <= block_cap
-                           ? need[i]
-                           : std::max<int64_t>(1, std::min<int64_t>(need[i], (int64_t)std::floor(raw[i])));
-            sum += share[i];
-        }
-        while (sum < budget) {
-            int best = -1;
-            for (int i = 0; i < nb; ++i)
-                if (share[i] < need[i] && (best < 0 || raw[i] - share[i] > raw[best] - share[best])) best = i;
-            if (best < 0) break;
-            ++share[best];
-            ++sum;
-        }
-        while (sum > budget) {            // one-block floors of small bins: take from the largest share
-            int best = -1;
-            for (int i = 0; i < nb; ++i)
-                if (share[i] > 1 && (best < 0 || share[i] > share[best])) best = i;
-            if (best < 0) break;
-            --share[best];
-            --sum;
-        }
-        int blocks = 0;
-        for (int i = 0; i < nb; ++i) {
-            Bin& b = P.bt.bin[i];
-            b.nblocks = (int)share[i];
-            b.block_begin = blocks;
-            blocks += b.nblocks;
-        }
-        P.bt.total_blocks = blocks;
+        P.bin_store = bin_store;
+        share_blocks(P.bt, P.bin_store, block_cap);
     }
+
+
 
     // Final device layout of one orientation from the internal CSR temporaries.
     int build_layout(const Plan& P, int R, const int32_t* tptr, const int32_t* tidx, const V* tval,
@@ -785,6 +795,23 @@ struct Engine : EngineBase {
         a.csr = Lr;
         a.csc = Lc;
         a.rows = rp.bt; a.cols = cp.bt;
+        {   // the check kernels' shares: one wave at their own occupancy
+            int nr = 0, nc = 0;
+            if (adaptive) {
+                SPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nr, ad_row_check<V>, kBlock, 0));
+                if (opt.kkt_form == SPS_KKT_PDLP)
+                    SPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nc, ad_col_check<V, true>, kBlock, 0));
+                else
+                    SPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nc, ad_col_check<V, false>, kBlock, 0));
+            } else {
+                SPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nr, rf_row_check<V>, kBlock, 0));
+                SPS_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nc, rf_col_check<V>, kBlock, 0));
+            }
+            a.rows_chk = rp.bt;
+            a.cols_chk = cp.bt;
+            share_blocks(a.rows_chk, rp.bin_store, std::min(block_cap, kSms * std::max(nr, 1)));
+            share_blocks(a.cols_chk, cp.bin_store, std::min(block_cap, kSms * std::max(nc, 1)));
+        }
         a.col_tail_blocks = tail;
         a.apply_blocks = apply_blocks;
         a.c = d_c; a.b = d_b; a.lo = d_lo; a.hi = d_hi;
@@ -830,8 +857,8 @@ struct Engine : EngineBase {
     // column check in the error form the options ask for (the PDLP form's kernel adds
     // the Lagrangian form's partials of the same points)
     void launch_col_check(const Args<V>& a) {
-        if (a.far_residual) ad_col_check<V, true><<<a.cols.total_blocks, kBlock, 0, st>>>(a);
-        else ad_col_check<V, false><<<a.cols.total_blocks, kBlock, 0, st>>>(a);
+        if (a.far_residual) ad_col_check<V, true><<<a.cols_chk.total_blocks, kBlock, 0, st>>>(a);
+        else ad_col_check<V, false><<<a.cols_chk.total_blocks, kBlock, 0, st>>>(a);
     }
 
     void launch_window(const Args<V>& a) {
@@ -842,7 +869,7 @@ struct Engine : EngineBase {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
                 ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
             }
-            ad_row_check<V><<<gr, kBlock, 0, st>>>(a);
+            ad_row_check<V><<<a.rows_chk.total_blocks, kBlock, 0, st>>>(a);
             launch_col_check(a);
             ad_apply<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
         } else {
@@ -850,8 +877,8 @@ struct Engine : EngineBase {
                 rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
                 rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
             }
-            rf_row_check<V><<<gr, kBlock, 0, st>>>(a, 0);
-            rf_col_check<V><<<gc, kBlock, 0, st>>>(a, 0);
+            rf_row_check<V><<<a.rows_chk.total_blocks, kBlock, 0, st>>>(a, 0);
+            rf_col_check<V><<<a.cols_chk.total_blocks, kBlock, 0, st>>>(a, 0);
             rf_apply<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
         }
     }
@@ -988,7 +1015,7 @@ struct Engine : EngineBase {
                                                                    d_perm_col, d_perm_row, d_rkind, tl_ns);
                 spmv_rows<V><<<gr, kBlock, 0, st>>>(args, args.X[0], args.AX[0]);
                 spmv_cols<V><<<gc, kBlock, 0, st>>>(args, args.Y[0], args.ATY[0]);
-                ad_row_check<V><<<gr, kBlock, 0, st>>>(args);
+                ad_row_check<V><<<args.rows_chk.total_blocks, kBlock, 0, st>>>(args);
                 launch_col_check(args);
                 ad_apply<V><<<args.apply_blocks, kBlock, 0, st>>>(args);
                 launches += 6;
@@ -1018,8 +1045,8 @@ struct Engine : EngineBase {
             }
         } else {
             k_rf_start<V><<<args.apply_blocks, kBlock, 0, st>>>(args, tl_ns);
-            rf_row_check<V><<<gr, kBlock, 0, st>>>(args, 1);
-            rf_col_check<V><<<gc, kBlock, 0, st>>>(args, 1);
+            rf_row_check<V><<<args.rows_chk.total_blocks, kBlock, 0, st>>>(args, 1);
+            rf_col_check<V><<<args.cols_chk.total_blocks, kBlock, 0, st>>>(args, 1);
             launches += 3;
         }
         SPS_CK(cudaGetLastError());
@@ -1031,8 +1058,8 @@ struct Engine : EngineBase {
         if (!h_ctl->done) status = SPS_STATUS_ITERATION_LIMIT;
         if (!adaptive && status != SPS_STATUS_OPTIMAL) {
             // report the error of the returned (current) point
-            rf_row_check<V><<<gr, kBlock, 0, st>>>(args, 1);
-            rf_col_check<V><<<gc, kBlock, 0, st>>>(args, 1);
+            rf_row_check<V><<<args.rows_chk.total_blocks, kBlock, 0, st>>>(args, 1);
+            rf_col_check<V><<<args.cols_chk.total_blocks, kBlock, 0, st>>>(args, 1);
             launches += 2;
         }
         const int cur = adaptive ? h_ctl->cur : 0;

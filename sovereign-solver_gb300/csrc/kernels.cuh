@@ -30,6 +30,8 @@ struct Args {
     int32_t n, m;
     Layout<V> csr, csc;
     BinTable rows, cols;
+    BinTable rows_chk, cols_chk;   // the same bins with the check kernels' block shares (one wave
+                                   // at their own occupancy: they hold more registers)
     int32_t col_tail_blocks;   // extra blocks of ad_col_step that sweep the rows
     int32_t apply_blocks;
     const V* c; const V* b; const V* lo; const V* hi;
@@ -139,8 +141,7 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     V* part = reinterpret_cast<V*>(a.part_row);
     if (!publish_partials<2>(v, part, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
     V t[2];
-    gather_partials<2>(t, part, gridDim.x, sm);
-    add_segment_rows<2>(t, a.csr, sm);
+    gather_all_partials<2>(t, part, gridDim.x, a.csr, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_ROW_STEP] = 0;
     decide_step(*ctl, double(t[0]), double(t[1]));
@@ -208,8 +209,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     V* part = reinterpret_cast<V*>(a.part_col);
     if (!publish_partials<1>(v, part, &ctl->ticket[T_COL_STEP], sm, &last)) return;
     V t[1];
-    gather_partials<1>(t, part, gridDim.x, sm);
-    add_segment_rows<1>(t, a.csc, sm);
+    gather_all_partials<1>(t, part, gridDim.x, a.csc, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_STEP] = 0;
     ctl->dx2 = double(t[0]);
@@ -289,7 +289,7 @@ SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
     GatherTwo<V> g{has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], inv_w};
     AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], a.yl, a.AXa, inv_w};
-    visit_bins<2, double>(a.rows, blockIdx.x, a.csr, g, e);
+    visit_bins<2, double>(a.rows_chk, blockIdx.x, a.csr, g, e);
     block_sum<kRowPartials>(e.p, sm);
     if (threadIdx.x == 0)
         for (int q = 0; q < kRowPartials; ++q) a.part_row[(size_t)blockIdx.x * kRowPartials + q] = e.p[q];
@@ -398,11 +398,11 @@ SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], inv_w};
     Epi e{&a, has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], a.xl, a.ATYa, inv_w};
     e.nonneg = a.uniform_bounds && a.lo_u == V(0) && isinf(a.hi_u) && a.hi_u > V(0);
-    visit_bins<2, double>(a.cols, blockIdx.x, a.csc, g, e);
+    visit_bins<2, double>(a.cols_chk, blockIdx.x, a.csc, g, e);
     if (!publish_partials<NP>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
     double tc[NP], tr[kRowPartials];
     gather_partials<NP>(tc, a.part_col, gridDim.x, sm);
-    gather_partials<kRowPartials>(tr, a.part_row, a.rows.total_blocks, sm);
+    gather_partials<kRowPartials>(tr, a.part_row, a.rows_chk.total_blocks, sm);
     add_segment_rows<NP>(tc, a.csc, sm);
     add_segment_rows<kRowPartials>(tr, a.csr, sm);
     if (threadIdx.x != 0) return;
@@ -609,7 +609,7 @@ SPS_CHECK_KERNEL rf_row_check(Args<V> a, int mode) {
     const V win = V(ctl->window);
     RfGather<V> g{avg ? a.xs : a.X[0], win, avg};
     RfRowCheckEpi<V> e{a.b, avg ? a.ys : a.Y[0], win, avg};
-    visit_bins<1, double>(a.rows, blockIdx.x, a.csr, g, e);
+    visit_bins<1, double>(a.rows_chk, blockIdx.x, a.csr, g, e);
     block_sum<2>(e.p, sm);
     if (threadIdx.x == 0) {
         a.part_row[(size_t)blockIdx.x * 2 + 0] = e.p[0];
@@ -648,11 +648,11 @@ SPS_CHECK_KERNEL rf_col_check(Args<V> a, int mode) {
     const V win = V(ctl->window);
     RfGather<V> g{avg ? a.ys : a.Y[0], win, avg};
     RfColCheckEpi<V> e{a.c, avg ? a.xs : a.X[0], win, avg};
-    visit_bins<1, double>(a.cols, blockIdx.x, a.csc, g, e);
+    visit_bins<1, double>(a.cols_chk, blockIdx.x, a.csc, g, e);
     if (!publish_partials<2>(e.p, a.part_col, &ctl->ticket[T_COL_CHECK], sm, &last)) return;
     double tc[2], tr[2];
     gather_partials<2>(tc, a.part_col, gridDim.x, sm);
-    gather_partials<2>(tr, a.part_row, a.rows.total_blocks, sm);
+    gather_partials<2>(tr, a.part_row, a.rows_chk.total_blocks, sm);
     add_segment_rows<2>(tc, a.csc, sm);
     add_segment_rows<2>(tr, a.csr, sm);
     if (threadIdx.x != 0) return;
