@@ -580,6 +580,7 @@ struct Engine : EngineBase {
         V *X0, *X1, *Y0, *Y1, *AX0 = nullptr, *AX1 = nullptr, *ATY0 = nullptr, *ATY1 = nullptr;
         V *xs, *ys, *xl = nullptr, *yl = nullptr, *AXa = nullptr, *ATYa = nullptr, *xbar = nullptr;
         V *xb = nullptr, *yb = nullptr, *AXl = nullptr, *ATYl = nullptr;
+        double *d_px = nullptr, *d_py = nullptr;   // FP64 copies of the check's two points
 
         // uniform bounds: every column [L, U] with L in {0, -inf}, U = +inf
         bool uniform = true;
@@ -626,6 +627,7 @@ struct Engine : EngineBase {
             add(&d_idr, sizeof(double) * m); add(&d_idc, sizeof(double) * n);
             add(&AXl, sizeof(V) * m); add(&ATYl, sizeof(V) * n);
             if (stall_test()) { add(&xb, sizeof(V) * n); add(&yb, sizeof(V) * m); }
+            add(&d_px, sizeof(double) * 2 * n); add(&d_py, sizeof(double) * 2 * m);
         } else {
             add(&xbar, sizeof(V) * n);
             add(&d_tau, sizeof(V) * n);
@@ -833,6 +835,8 @@ struct Engine : EngineBase {
         a.xs = xs; a.ys = ys; a.xl = xl; a.yl = yl; a.AXa = AXa; a.ATYa = ATYa; a.xbar = xbar;
         a.xb = xb; a.yb = yb;
         a.AXl = AXl; a.ATYl = ATYl;
+        a.px[0] = d_px; a.px[1] = d_px ? d_px + n : nullptr;
+        a.py[0] = d_py; a.py[1] = d_py ? d_py + m : nullptr;
         a.part_row = d_pr; a.part_col = d_pc; a.part_aux = d_pa;
         a.ctl = d_ctl;
         a.abort_flag = d_abort;
@@ -852,7 +856,7 @@ struct Engine : EngineBase {
     }
 
     // ---------------------------------------------------------------- solve
-    int nodes_per_window() const { return 2 * args.check_interval + 3; }
+    int nodes_per_window() const { return 2 * args.check_interval + (mode == SPS_MODE_ADAPTIVE ? 4 : 3); }
 
     // column check in the error form the options ask for (the PDLP form's kernel adds
     // the Lagrangian form's partials of the same points)
@@ -869,6 +873,7 @@ struct Engine : EngineBase {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
                 ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
             }
+            ad_check_prep<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
             ad_row_check<V><<<a.rows_chk.total_blocks, kBlock, 0, st>>>(a);
             launch_col_check(a);
             ad_apply<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
@@ -1015,10 +1020,11 @@ struct Engine : EngineBase {
                                                                    d_perm_col, d_perm_row, d_rkind, tl_ns);
                 spmv_rows<V><<<gr, kBlock, 0, st>>>(args, args.X[0], args.AX[0]);
                 spmv_cols<V><<<gc, kBlock, 0, st>>>(args, args.Y[0], args.ATY[0]);
+                ad_check_prep<V><<<args.apply_blocks, kBlock, 0, st>>>(args);
                 ad_row_check<V><<<args.rows_chk.total_blocks, kBlock, 0, st>>>(args);
                 launch_col_check(args);
                 ad_apply<V><<<args.apply_blocks, kBlock, 0, st>>>(args);
-                launches += 6;
+                launches += 7;
                 SPS_CK(cudaGetLastError());
                 return SPS_OK;
             };

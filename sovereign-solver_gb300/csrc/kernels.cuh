@@ -46,6 +46,7 @@ struct Args {
     V* xs; V* ys; V* xl; V* yl; V* AXa; V* ATYa; V* xbar;
     V* xb; V* yb;              // best point of the stall test (null unless it is on)
     V* AXl; V* ATYl;           // adaptive: K x_last, K^T y_last (infeasibility tests)
+    double* px[2]; double* py[2];   // adaptive: the check's two points (average, current) in FP64
     double* part_row; double* part_col; double* part_aux;
     Ctl* ctl;
     const volatile int32_t* abort_flag;
@@ -230,13 +231,10 @@ __device__ __forceinline__ double avg_at(const V* s, const V* l, double inv_w, i
     return l ? v + double(__ldg(l + j)) : v;
 }
 
-template <class V>
-struct GatherTwo {
-    const V *s, *l, *x;
-    double inv_w;
-    __device__ __forceinline__ double operator()(int q, int j) const {
-        return q == 0 ? avg_at(s, l, inv_w, j) : double(__ldg(x + j));
-    }
+// The check's two points in FP64 (written by ad_check_prep), gathered as is.
+struct GatherPts {
+    const double *p0, *p1;
+    __device__ __forceinline__ double operator()(int q, int j) const { return __ldg((q == 0 ? p0 : p1) + j); }
 };
 
 template <class V>
@@ -264,7 +262,7 @@ struct AdRowCheckEpi {
             p[4 * q + 0] += res * res;
             const double ro = res * idr;
             p[4 * q + 1] += ro * ro;
-            const double yv = q == 0 ? avg_at(ys, ylb, inv_w, r) : double(yc[r]);
+            const double yv = __ldg(a->py[q] + r);
             p[4 * q + 2] += br * yv;
             const double d = yv - double(yl[r]);
             p[4 * q + 3] += d * d;
@@ -272,11 +270,36 @@ struct AdRowCheckEpi {
         double kdx = acc[1] - double(a->AXl[r]);
         if (kind) kdx = fmax(kdx, 0.0);
         p[8] += kdx * kdx;
-        const double dy = double(yc[r]) - double(yl[r]);
+        const double dy = __ldg(a->py[1] + r) - double(yl[r]);
         p[9] += br * dy;
         if (kind) p[10] += fmax(dy, 0.0) * fmax(dy, 0.0);
     }
 };
+
+// The check's two points as FP64 vectors, once per check: the average
+// x_last + x_sum / w_sum (the current iterate while there is no average yet) and
+// the current iterate, for x and y.  The checks then gather and read doubles
+// (no conversion or average per nonzero on GB300's slow FP64 pipe); the values
+// are the ones the checks computed per nonzero before, so every sum is unchanged.
+template <class V>
+__global__ void __launch_bounds__(kBlock) ad_check_prep(Args<V> a) {
+    const Ctl* ctl = a.ctl;
+    if (ctl->done) return;
+    const int cur = ctl->cur;
+    const bool has_avg = ctl->w_sum > 0.0;
+    const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
+    const int stride = gridDim.x * kBlock;
+    for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += stride) {
+        const double xc = double(a.X[cur][j]);
+        a.px[0][j] = has_avg ? avg_at(a.xs, a.xl, inv_w, j) : xc;
+        a.px[1][j] = xc;
+    }
+    for (int i = blockIdx.x * kBlock + threadIdx.x; i < a.m; i += stride) {
+        const double yc = double(a.Y[cur][i]);
+        a.py[0][i] = has_avg ? avg_at(a.ys, a.yl, inv_w, i) : yc;
+        a.py[1][i] = yc;
+    }
+}
 
 template <class V>
 SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
@@ -287,7 +310,7 @@ SPS_CHECK_KERNEL ad_row_check(Args<V> a) {
     // with no average yet, point 0 aliases the current iterate
     const bool has_avg = ctl->w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
-    GatherTwo<V> g{has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], inv_w};
+    GatherPts g{a.px[0], a.px[1]};
     AdRowCheckEpi<V> e{&a, has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], a.yl, a.AXa, inv_w};
     visit_bins<2, double>(a.rows_chk, blockIdx.x, a.csr, g, e);
     block_sum<kRowPartials>(e.p, sm);
@@ -332,7 +355,7 @@ struct AdColCheckEpi {
             p[5 * q + 0] += dres * dres;
             const double dor = dres * idc;
             p[5 * q + 1] += dor * dor;
-            const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
+            const double xv = __ldg(a->px[q] + j);
             p[5 * q + 2] += cj * xv;
             const double d = xv - double(xl[j]);
             p[5 * q + 4] += d * d;
@@ -340,7 +363,7 @@ struct AdColCheckEpi {
         }
         const double lv = fmin(double(a->ATYl[j]) - acc[1], 0.0);
         p[10] += lv * lv;
-        const double dx = double(xc[j]) - double(xl[j]);
+        const double dx = __ldg(a->px[1] + j) - double(xl[j]);
         const double vx = fmin(dx, 0.0);
         p[12] += vx * vx;
         p[13] += cj * dx;
@@ -353,7 +376,7 @@ struct AdColCheckEpi {
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
             const double rc = cj - acc[q];
-            const double xv = q == 0 ? avg_at(xs, xlb, inv_w, j) : double(xc[j]);
+            const double xv = __ldg(a->px[q] + j);
             // PDLP form: a bound farther from x than |x| (a scale-free test) takes no part of rc
             const bool nl = hl && (!Far || fabs(xv - lo) <= fabs(xv));
             const bool nh = hh && (!Far || fabs(xv - hi) <= fabs(xv));
@@ -377,7 +400,7 @@ struct AdColCheckEpi {
         const double lp = (hl && hh) ? lr : hl ? fmax(lr, 0.0) : hh ? fmin(lr, 0.0) : 0.0;
         p[10] += (lr - lp) * (lr - lp);
         p[11] += (hl ? lo * fmax(lp, 0.0) : 0.0) + (hh ? hi * fmin(lp, 0.0) : 0.0);
-        const double dx = double(xc[j]) - double(xl[j]);
+        const double dx = __ldg(a->px[1] + j) - double(xl[j]);
         const double vx = (hl && hh) ? dx : hl ? fmin(dx, 0.0) : hh ? fmax(dx, 0.0) : 0.0;
         p[12] += vx * vx;
         p[13] += cj * dx;
@@ -395,7 +418,7 @@ SPS_CHECK_KERNEL ad_col_check(Args<V> a) {
     const int cur = ctl->cur;
     const bool has_avg = ctl->w_sum > 0.0;
     const double inv_w = has_avg ? 1.0 / ctl->w_sum : 1.0;
-    GatherTwo<V> g{has_avg ? a.ys : a.Y[cur], has_avg ? a.yl : nullptr, a.Y[cur], inv_w};
+    GatherPts g{a.py[0], a.py[1]};
     Epi e{&a, has_avg ? a.xs : a.X[cur], has_avg ? a.xl : nullptr, a.X[cur], a.xl, a.ATYa, inv_w};
     e.nonneg = a.uniform_bounds && a.lo_u == V(0) && isinf(a.hi_u) && a.hi_u > V(0);
     visit_bins<2, double>(a.cols_chk, blockIdx.x, a.csc, g, e);
