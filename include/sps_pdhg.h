@@ -105,7 +105,7 @@ typedef struct {
                                  the cold start's (x = clip(0, lb, ub), y = 0) is dropped and the
                                  solve starts cold; 0: always start from the warm point */
     int32_t batch_team;       /* batched solver: blocks (one thread-block cluster) per large
-                                 instance, 1..8; 1 = one block per instance; 0 = 2, or in a
+                                 instance, 1..8; 1 = one block per instance; 0 = 4, or in a
                                  batch of fewer instances than half the resident blocks the
                                  largest of 2, 4, 8 that keeps every instance resident */
     int32_t batch_team_nnz;   /* batched solver: instances with at least this many nonzeros are

@@ -28,7 +28,7 @@ class PDHGBatch:
     16, 32); 0 lets the library time the candidates on a sample of the batch.
     The lanes per row of the row pass (4, 8, 16, 32) are always timed.
     ``batch_team``: blocks (a thread-block cluster) per large instance, 1 = one
-    block per instance, 0 = 2 (or, in a batch of fewer instances than half the
+    block per instance, 0 = 4 (or, in a batch of fewer instances than half the
     resident blocks, the largest of 2, 4, 8 that keeps them all resident);
     ``batch_team_nnz``: nonzeros from which an instance is large (0 = 65 536 in
     such a small batch, else the larger of 65 536 and twice the median).

@@ -1,12 +1,14 @@
 // api.cu — extern "C" entry points of libsps_gb300.so (declared in
 // include/sps_pdhg.h): input validation, the reference standard-form
 // conversion for SPS_MODE_REFERENCE, and handle management.
+#include <algorithm>
 #include <cmath>
 #include <chrono>
 #include <cstring>
 #include <memory>
 #include <string>
 #include <thread>
+#include <vector>
 
 #include "engine_impl.cuh"
 #include "nvtx.cuh"
@@ -52,10 +54,30 @@ bool check_csr(const int32_t* ptr, const int32_t* idx, const double* val, int32_
     return true;
 }
 
+// Index of the first item in [0, len) that bad() flags, or len: on host threads
+// over contiguous chunks when len is large.
+template <class F>
+int64_t first_bad(int64_t len, F bad) {
+    const int64_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(hw, len >> 17));
+    std::vector<int64_t> first(nt, len);
+    auto scan = [&](int t) {
+        const int64_t lo = len * t / nt, hi = len * (t + 1) / nt;
+        for (int64_t i = lo; i < hi; ++i)
+            if (bad(i)) { first[t] = i; return; }
+    };
+    if (nt == 1) {
+        scan(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t) pool.emplace_back(scan, t);
+        for (auto& th : pool) th.join();
+    }
+    return *std::min_element(first.begin(), first.end());
+}
+
 bool finite_all(const double* v, int64_t len) {
-    for (int64_t i = 0; i < len; ++i)
-        if (!std::isfinite(v[i])) return false;
-    return true;
+    return first_bad(len, [&](int64_t i) { return !std::isfinite(v[i]); }) == len;
 }
 
 // Validation shared by both modes (solver/problem.py:103-142 plus the engine's
@@ -74,11 +96,11 @@ int validate(const sps_problem_desc* d) {
     if (!finite_all(d->c, d->n)) return create_fail(SPS_ERR_INVALID, "non-finite objective coefficient");
     if (!finite_all(d->b_ub, d->m_ub) || !finite_all(d->b_eq, d->m_eq))
         return create_fail(SPS_ERR_INVALID, "non-finite right-hand side");
-    for (int32_t j = 0; j < d->n; ++j) {
+    const int64_t bad = first_bad(d->n, [&](int64_t j) {
         const double l = d->lb[j], u = d->ub[j];
-        if (std::isnan(l) || std::isnan(u) || l == INFINITY || u == -INFINITY || l > u + 1e-12)
-            return create_fail(SPS_ERR_INVALID, "invalid bounds at variable " + std::to_string(j));
-    }
+        return std::isnan(l) || std::isnan(u) || l == INFINITY || u == -INFINITY || l > u + 1e-12;
+    });
+    if (bad < d->n) return create_fail(SPS_ERR_INVALID, "invalid bounds at variable " + std::to_string(bad));
     return SPS_OK;
 }
 
@@ -292,7 +314,9 @@ int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_hand
     if (opt.kkt_form == SPS_KKT_PDLP && opt.mode != SPS_MODE_ADAPTIVE)
         return create_fail(SPS_ERR_INVALID, "kkt_form PDLP needs the adaptive mode (the reference mode "
                                             "reports the reference's own error)");
+    const CreateTrace trace;
     if (int rc = validate(prob)) return rc;
+    trace.mark("host validation");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= opt.device || opt.device < 0) {
         cudaGetLastError();
@@ -309,12 +333,22 @@ int sps_create(const sps_problem_desc* prob, const sps_options* opt_in, sps_hand
     EngineBase* e = h->eng;
     e->n_user = prob->n;
     e->m_user = prob->m_ub + prob->m_eq;
-    e->c_user.assign(prob->c, prob->c + prob->n);
-    e->lb_user.assign(prob->lb, prob->lb + prob->n);
-    e->ub_user.assign(prob->ub, prob->ub + prob->n);
-    if (opt.mode == SPS_MODE_ADAPTIVE && opt.precision == SPS_FP32 && opt.escalate == 1) h->copy = copy_problem(prob, e);
     e->smap = sm;
+    e->trace = &trace;
+    // the host copies the engine keeps (c and bounds for extraction, the whole problem
+    // when a stalled FP32 solve may continue in FP64) on a thread of their own, while
+    // the device set-up runs; set-up reads only the caller's arrays and hp
+    std::thread copies([&] {
+        e->c_user.assign(prob->c, prob->c + prob->n);
+        e->lb_user.assign(prob->lb, prob->lb + prob->n);
+        e->ub_user.assign(prob->ub, prob->ub + prob->n);
+        if (opt.mode == SPS_MODE_ADAPTIVE && opt.precision == SPS_FP32 && opt.escalate == 1)
+            h->copy = copy_problem(prob, e);
+    });
     const int rc = opt.precision == SPS_FP32 ? setup_f32(e, hp, opt, opt.mode) : setup_f64(e, hp, opt, opt.mode);
+    copies.join();
+    trace.mark("host copies joined");
+    e->trace = nullptr;
     if (rc != SPS_OK) {
         g_create_error = e->err;
         delete e;

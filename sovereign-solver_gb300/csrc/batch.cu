@@ -745,6 +745,22 @@ __global__ void __launch_bounds__(kBlock) k_batch_extract(const Inst* inst, cons
 using sps::Ctl;
 using sps::batch::Inst;
 
+// A host array that is not value-initialised on allocation (the batch packing
+// writes every element on its own threads).
+template <class T>
+struct HostBuf {
+    std::unique_ptr<T[]> p;
+    size_t n = 0;
+    HostBuf() = default;
+    explicit HostBuf(int64_t count) : p(new T[(size_t)std::max<int64_t>(count, 1)]), n((size_t)std::max<int64_t>(count, 0)) {}
+    T* data() { return p.get(); }
+    const T* data() const { return p.get(); }
+    T& operator[](size_t i) { return p[i]; }
+    const T& operator[](size_t i) const { return p[i]; }
+    size_t size() const { return n; }
+    bool empty() const { return n == 0; }
+};
+
 struct sps_batch {
     int32_t count = 0;
     sps_options opt{};
@@ -769,11 +785,11 @@ struct sps_batch {
     double *d_xo = nullptr, *d_yo = nullptr;
     sps::batch::Arrays arr{};
     int64_t sum_n = 0, sum_m = 0;
-    std::vector<double> c_all, lb_all, ub_all;   // original data, packed like the column vectors
+    HostBuf<double> c_all, lb_all, ub_all;       // original data, packed like the column vectors
     // original rows (local CSR offsets, columns, values) and right-hand sides,
     // kept for the FP64 continuation of stalled instances
-    std::vector<int32_t> h_rptr, h_ridx;
-    std::vector<double> h_rv, h_b;
+    HostBuf<int32_t> h_rptr, h_ridx;
+    HostBuf<double> h_rv, h_b;
     std::vector<double> xo, yo;
     std::vector<Ctl> out;
     std::vector<int8_t> escalated;
@@ -985,9 +1001,11 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
     b->sum_n = vc;
     b->sum_m = vr;
     // ---- host packing (CSR of [A_ub; A_eq] and a CSC by counting sort), spread over host threads
-    std::vector<int32_t> rptr(rp), ridx(NNZ), cptr(cp), cidx(NNZ);
-    std::vector<double> rv(NNZ), cv(NNZ), c64(vc), lo64(vc), hi64(vc), b64(vr);
-    std::vector<int8_t> kind(vr);
+    // not zero-filled: every element is written by the packing threads (gigabytes on
+    // large batches, which a value-initialising std::vector cleared on one thread)
+    HostBuf<int32_t> rptr(rp), ridx(NNZ), cptr(cp), cidx(NNZ);
+    HostBuf<double> rv(NNZ), cv(NNZ), c64(vc), lo64(vc), hi64(vc), b64(vr);
+    HostBuf<int8_t> kind(vr);
     std::vector<std::string> errs(count);
     auto pack = [&](int32_t k) {
         const sps_problem_desc& d = probs[k];
@@ -1053,9 +1071,9 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
             sps::set_create_error("instance " + std::to_string(k) + ": " + errs[k]);
             return SPS_ERR_INVALID;
         }
-    b->c_all = c64;
-    b->lb_all = lo64;
-    b->ub_all = hi64;
+    b->c_all = std::move(c64);
+    b->lb_all = std::move(lo64);
+    b->ub_all = std::move(hi64);
     // hand-out order: largest instances (nonzeros + rows + columns) first
     std::vector<int64_t> work(count);
     for (int32_t k = 0; k < count; ++k)
@@ -1114,8 +1132,8 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         SPB_CK(up(d_rptr, rptr.data(), 4 * rp)); SPB_CK(up(d_ridx, ridx.data(), 4 * NNZ));
         SPB_CK(up(d_cptr, cptr.data(), 4 * cp)); SPB_CK(up(d_cidx, cidx.data(), 4 * NNZ));
         SPB_CK(up(t_rv, rv.data(), 8 * NNZ)); SPB_CK(up(t_cv, cv.data(), 8 * NNZ));
-        SPB_CK(up(t_c, c64.data(), 8 * vc)); SPB_CK(up(t_lo, lo64.data(), 8 * vc));
-        SPB_CK(up(t_hi, hi64.data(), 8 * vc)); SPB_CK(up(t_b, b64.data(), 8 * vr));
+        SPB_CK(up(t_c, b->c_all.data(), 8 * vc)); SPB_CK(up(t_lo, b->lb_all.data(), 8 * vc));
+        SPB_CK(up(t_hi, b->ub_all.data(), 8 * vc)); SPB_CK(up(t_b, b64.data(), 8 * vr));
         SPB_CK(up(d_kind, kind.data(), vr));
         SPB_CK(up(b->d_inst, b->inst.data(), sizeof(Inst) * count));
         SPB_CK(up(b->d_order, b->order.data(), 4 * (size_t)count));
@@ -1160,13 +1178,17 @@ extern "C" int sps_batch_create(int32_t count, const sps_problem_desc* probs, co
         // instances as resident blocks (strong branching's children) leaves SMs
         // idle instead: there every instance of 65536 nonzeros or more gets a
         // team, 2, 4 or 8 blocks, the largest that still fits the resident wave.
-        int want = opt.batch_team > 0 ? std::min(opt.batch_team, 8) : 2;
+        // Default team in a batch that fills the GPU: 4 blocks (4096 planted LPs of
+        // 50-5000 rows: 2.90 s per batch against 3.19 s with 2 and 3.26 s with 8).
+        int want = opt.batch_team > 0 ? std::min(opt.batch_team, 8) : 4;
         if (opt.batch_team_nnz > 0) {
             b->team_nnz = opt.batch_team_nnz;
         } else if ((int64_t)count * 2 <= slots) {
             b->team_nnz = sps::batch::kTeamNnz;
-            if (opt.batch_team <= 0)
+            if (opt.batch_team <= 0) {
+                want = 2;
                 while (want < 8 && (int64_t)count * want * 2 <= slots) want *= 2;
+            }
         } else {
             const int32_t med = b->inst[b->order[count / 2]].nnz;
             b->team_nnz = (int32_t)std::max<int64_t>(sps::batch::kTeamNnz, 2LL * med);

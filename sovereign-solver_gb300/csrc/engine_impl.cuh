@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -38,7 +40,20 @@ struct StdMap {
     std::vector<double> lb_shift;
 };
 
+// Phase times of sps_create on stderr when the environment sets
+// SPS_TRACE_CREATE (a diagnostic: which part of set-up a large LP waits on).
+struct CreateTrace {
+    bool on = std::getenv("SPS_TRACE_CREATE") != nullptr;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    void mark(const char* what) const {
+        if (!on) return;
+        const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        std::fprintf(stderr, "sps_create %-26s %9.2f ms\n", what, ms);
+    }
+};
+
 struct EngineBase {
+    const CreateTrace* trace = nullptr;   // set during sps_create
     // caller problem (for extraction)
     int32_t n_user = 0, m_user = 0;
     std::vector<double> c_user, lb_user, ub_user;
@@ -84,6 +99,10 @@ struct Engine : EngineBase {
     int32_t *d_perm_row = nullptr, *d_perm_col = nullptr;
     int8_t* d_rkind = nullptr;
     double *d_xout = nullptr, *d_yout = nullptr, *d_wx = nullptr, *d_wy = nullptr;
+    // adaptive mode: the caller's c (and bounds unless uniform) in FP64, caller order, for the
+    // solution extracted on the device; the solution then stays there until sps_get_solution
+    double *d_cuser = nullptr, *d_lbuser = nullptr, *d_ubuser = nullptr, *d_obj = nullptr;
+    bool sol_on_device = false;
     bool have_warm_x = false, have_warm_y = false;
     double warm_omega = 0.0;
     bool warm_used = false;
@@ -297,6 +316,39 @@ struct Engine : EngineBase {
         bt.total_blocks = blocks;
     }
 
+    // Host threads for a loop over R items (one below 2^17 items), and the loop over
+    // nt contiguous chunks, chunk t on thread t.
+    static int host_threads(int64_t R) {
+        const int64_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        return (int)std::max<int64_t>(1, std::min<int64_t>(hw, R >> 17));
+    }
+    template <class F>
+    static void for_chunks(int64_t R, int nt, F f) {
+        if (nt <= 1) { f(0, 0, (int)R); return; }
+        std::vector<std::thread> pool;
+        for (int t = 0; t < nt; ++t) pool.emplace_back(f, t, (int)(R * t / nt), (int)(R * (t + 1) / nt));
+        for (auto& th : pool) th.join();
+    }
+
+    // out[0] = 0, out[i + 1] = out[i] + len(i): chunk sums on host threads, then
+    // each chunk fills its part from its offset.
+    template <class F>
+    static void prefix_lengths(int R, F len, std::vector<int32_t>& out) {
+        const int nt = host_threads(R);
+        std::vector<int64_t> part(nt + 1, 0);
+        for_chunks(R, nt, [&](int t, int lo, int hi) {
+            int64_t acc = 0;
+            for (int i = lo; i < hi; ++i) acc += len(i);
+            part[t + 1] = acc;
+        });
+        for (int t = 0; t < nt; ++t) part[t + 1] += part[t];
+        out[0] = 0;
+        for_chunks(R, nt, [&](int t, int lo, int hi) {
+            int64_t acc = part[t];
+            for (int i = lo; i < hi; ++i) { acc += len(i); out[i + 1] = (int32_t)acc; }
+        });
+    }
+
     // Order: per kind, SLICED rows by decreasing length, then WARP rows, then
     // SEGMENT rows, then SLAB rows (stable counting sort); one bin per (kind,
     // schedule).
@@ -312,47 +364,59 @@ struct Engine : EngineBase {
                                             : kSliceMax + (md == BM_WARP ? 1 : md == BM_SEGMENT ? 2 : 3);
             return kind_of(i) * NB + sub;
         };
-        // each row's bucket once (the sort and the bin boundaries read it again)
+        // each row's bucket once (the sort and the bin boundaries read it again);
+        // large plans on host threads over contiguous chunks (a 2M-column plan
+        // took 12 ms of a 29 ms sps_create on one thread)
         std::vector<uint8_t> bk(R);
-        if (!kinds && !slab) {       // columns: one kind, no SLAB (the same buckets, branch-free)
-            const int64_t* L = lens.data();
-            for (int i = 0; i < R; ++i)
-                bk[i] = (uint8_t)(L[i] <= kSliceMax ? kSliceMax - L[i] : L[i] <= kSegment ? kSliceMax + 1 : kSliceMax + 2);
-        } else {
-            for (int i = 0; i < R; ++i) bk[i] = (uint8_t)bucket(i);
-        }
-        // Bucket counts in four interleaved histograms (consecutive rows mostly
-        // share a bucket, and one counter would make every increment wait for
-        // the previous one), then a stable placement that writes each run of
-        // equal buckets as one block: 2M uniform columns take 8 instead of 14 ms.
-        std::vector<int64_t> cnt(2 * NB + 1, 0);
-        {
+        const int nt = host_threads(R);
+        std::vector<std::vector<int64_t>> hist(nt, std::vector<int64_t>(2 * NB, 0));
+        for_chunks(R, nt, [&](int t, int lo, int hi) {
+            if (!kinds && !slab) {   // columns: one kind, no SLAB (the same buckets, branch-free)
+                const int64_t* L = lens.data();
+                for (int i = lo; i < hi; ++i)
+                    bk[i] = (uint8_t)(L[i] <= kSliceMax ? kSliceMax - L[i] : L[i] <= kSegment ? kSliceMax + 1 : kSliceMax + 2);
+            } else {
+                for (int i = lo; i < hi; ++i) bk[i] = (uint8_t)bucket(i);
+            }
+            // bucket counts in four interleaved histograms (consecutive rows mostly
+            // share a bucket, and one counter would make every increment wait for
+            // the previous one)
             std::vector<int64_t> h(4 * 2 * NB, 0);
             const uint8_t* kb = bk.data();
-            int i = 0;
-            for (; i + 4 <= R; i += 4) {
+            int i = lo;
+            for (; i + 4 <= hi; i += 4) {
                 ++h[kb[i]];
                 ++h[2 * NB + kb[i + 1]];
                 ++h[4 * NB + kb[i + 2]];
                 ++h[6 * NB + kb[i + 3]];
             }
-            for (; i < R; ++i) ++h[kb[i]];
-            for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] = h[b] + h[2 * NB + b] + h[4 * NB + b] + h[6 * NB + b];
-        }
+            for (; i < hi; ++i) ++h[kb[i]];
+            for (int b = 0; b < 2 * NB; ++b) hist[t][b] = h[b] + h[2 * NB + b] + h[4 * NB + b] + h[6 * NB + b];
+        });
+        std::vector<int64_t> cnt(2 * NB + 1, 0);
+        for (int t = 0; t < nt; ++t)
+            for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] += hist[t][b];
         for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] += cnt[b];
+        // stable placement: chunk t starts each bucket after the earlier chunks' rows of
+        // it, and writes each run of equal buckets as one block
         P.perm.assign(R, 0);
         {
-            std::vector<int64_t> pos(cnt.begin(), cnt.end() - 1);
+            std::vector<std::vector<int64_t>> pos(nt, std::vector<int64_t>(cnt.begin(), cnt.end() - 1));
+            for (int t = 1; t < nt; ++t)
+                for (int b = 0; b < 2 * NB; ++b) pos[t][b] = pos[t - 1][b] + hist[t - 1][b];
             int32_t* pm = P.perm.data();
-            for (int i = 0; i < R;) {
-                const uint8_t b = bk[i];
-                int j = i + 1;
-                while (j < R && bk[j] == b) ++j;
-                int32_t* dst = pm + pos[b];
-                for (int q = i; q < j; ++q) dst[q - i] = q;
-                pos[b] += j - i;
-                i = j;
-            }
+            for_chunks(R, nt, [&](int t, int lo, int hi) {
+                std::vector<int64_t>& ps = pos[t];
+                for (int i = lo; i < hi;) {
+                    const uint8_t b = bk[i];
+                    int j = i + 1;
+                    while (j < hi && bk[j] == b) ++j;
+                    int32_t* dst = pm + ps[b];
+                    for (int q = i; q < j; ++q) dst[q - i] = q;
+                    ps[b] += j - i;
+                    i = j;
+                }
+            });
         }
         // (kind, schedule) of a bucket: rows of one bin are consecutive buckets
         auto bin_of = [&](int bucket_id) {
@@ -537,6 +601,7 @@ struct Engine : EngineBase {
                                                            : "non-finite constraint matrix value");
         }
 
+        if (trace) trace->mark("upload + validate");
         // ---- column plan
         std::vector<int64_t> clen(n);
         for (int j = 0; j < n; ++j) clen[j] = colcount[j];
@@ -544,7 +609,9 @@ struct Engine : EngineBase {
         make_plan(clen, nullptr, nullptr, cp, block_cap);
         const std::vector<int32_t>& perm_col = cp.perm;
         std::vector<int32_t> inv_col(n);
-        for (int j = 0; j < n; ++j) inv_col[perm_col[j]] = j;
+        for_chunks(n, host_threads(n), [&](int, int lo, int hi) {
+            for (int j = lo; j < hi; ++j) inv_col[perm_col[j]] = j;
+        });
 
         // ---- row plan: bins by row kind, length and gather locality (SLAB groups)
         Plan rp;
@@ -558,9 +625,10 @@ struct Engine : EngineBase {
             return fail(SPS_ERR_INVALID, "padded matrix layout exceeds 2^31-1 entries");
         }
         std::vector<int32_t> nptr(m + 1, 0), cptr(n + 1, 0);
-        for (int r = 0; r < m; ++r) nptr[r + 1] = nptr[r] + (int32_t)rlen[perm_row[r]];
-        for (int j = 0; j < n; ++j) cptr[j + 1] = cptr[j] + colcount[perm_col[j]];
+        prefix_lengths(m, [&](int r) { return (int32_t)rlen[perm_row[r]]; }, nptr);
+        prefix_lengths(n, [&](int j) { return colcount[perm_col[j]]; }, cptr);
 
+        if (trace) trace->mark("host plans");
         // ---- persistent arena
         const int tail = std::min(grid_for(m), kSms * 4);
         const int apply_blocks = grid_for(std::max(n, m), kBlock, kSms * 8);
@@ -636,6 +704,11 @@ struct Engine : EngineBase {
         add(&d_ctl, sizeof(Ctl));
         add(&d_xout, sizeof(double) * n);
         add(&d_yout, sizeof(double) * m);
+        if (adaptive) {
+            add(&d_cuser, sizeof(double) * n);
+            add(&d_obj, sizeof(double) * 2);
+            if (!uniform) { add(&d_lbuser, sizeof(double) * n); add(&d_ubuser, sizeof(double) * n); }
+        }
         add(&d_wx, sizeof(double) * n);
         add(&d_wy, sizeof(double) * m);
         size_t total = 0;
@@ -647,6 +720,7 @@ struct Engine : EngineBase {
         }
         SPS_CK(cudaMemsetAsync(d_tickets, 0, sizeof(uint32_t) * ntk, st));
 
+        if (trace) trace->mark("arena");
         // ---- internal CSR and CSC temporaries (FP64 values)
         int32_t *t_inv_col, *t_fill, *t_ptr, *t_idx, *t_cptr, *t_cidx;
         double *t_rval, *t_cval, *t_stat;
@@ -705,6 +779,7 @@ struct Engine : EngineBase {
             }
         }
 
+        if (trace) trace->mark("CSR/CSC build + sort");
         // ---- scaling (adaptive) or reference diagonal steps, on the FP64 temporaries
         double *rmax = t_stat, *rsum = t_stat + m, *cmax = t_stat + 2 * m, *csum = t_stat + 2 * m + n;
         {
@@ -741,6 +816,7 @@ struct Engine : EngineBase {
         k_finish_values<V><<<warp_grid_n, kBlock, 0, st>>>(t_cptr, t_cidx, t_cval, d_dc, d_dr, t_cvV, n);
         SPS_CK(cudaGetLastError());
 
+        if (trace) trace->mark("scaling");
         // ---- final binned layouts
         Layout<V> Lr{}, Lc{};
         if (int rc = build_layout(rp, m, t_ptr, t_idx, t_rvV, Lr, d_rptr, d_rsoff, d_runit, d_ridx, d_rval)) return rc;
@@ -753,6 +829,7 @@ struct Engine : EngineBase {
         Lr.nsegrows = rp.nslots;
         Lc.nsegrows = cp.nslots;
 
+        if (trace) trace->mark("binned layouts");
         // ---- vectors in internal order (uploaded in the caller's order, permuted on the device)
         {
             double *t_c, *t_l, *t_u, *t_b;
@@ -765,6 +842,9 @@ struct Engine : EngineBase {
             k_scale_vectors<V><<<grid_for(std::max(n, m)), kBlock, 0, st>>>(t_c, t_l, t_u, t_b, d_perm_col, d_perm_row,
                                                                            d_dc, d_dr, d_c, d_lo, d_hi, d_b, n, m);
             if (d_idc) k_reciprocals<<<grid_for(std::max(n, m)), kBlock, 0, st>>>(d_dc, d_dr, d_idc, d_idr, n, m);
+            if (d_cuser) SPS_CK(cudaMemcpyAsync(d_cuser, t_c, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            if (d_lbuser) SPS_CK(cudaMemcpyAsync(d_lbuser, t_l, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
+            if (d_ubuser) SPS_CK(cudaMemcpyAsync(d_ubuser, t_u, sizeof(double) * n, cudaMemcpyDeviceToDevice, st));
             SPS_CK(cudaGetLastError());
             SPS_CK(cudaStreamSynchronize(st));
             cudaFreeAsync(t_c, st);
@@ -772,6 +852,7 @@ struct Engine : EngineBase {
         cudaFreeAsync(t_inv_col, st); cudaFreeAsync(t_fill, st); cudaFreeAsync(t_ptr, st); cudaFreeAsync(t_cptr, st); cudaFreeAsync(t_idx, st);
         cudaFreeAsync(t_cidx, st); cudaFreeAsync(t_rval, st); cudaFreeAsync(t_cval, st); cudaFreeAsync(t_rvV, st); cudaFreeAsync(t_cvV, st);
 
+        if (trace) trace->mark("vectors");
         // ---- start-up constants: eta0 = 1 / max|K~|, omega0 = ||c~|| / ||b~||
         {
             const int g = kSms * 2;
@@ -852,6 +933,7 @@ struct Engine : EngineBase {
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0, ev1);
         setup_ms = ms;
+        if (trace) trace->mark("device set-up done");
         return SPS_OK;
     }
 
@@ -1069,19 +1151,40 @@ struct Engine : EngineBase {
             launches += 2;
         }
         const int cur = adaptive ? h_ctl->cur : 0;
-        k_extract<V><<<args.apply_blocks, kBlock, 0, st>>>(args.X[cur], args.Y[cur], args.dc, args.dr, d_perm_col,
-                                                           d_perm_row, d_xout, d_yout, n, m);
+        double obj = 0;
+        if (adaptive) {
+            // the solution in the caller's order, clipped to the caller's bounds, and c^T x,
+            // on the device: it stays there until sps_get_solution asks for it
+            SPS_CK(cudaMemsetAsync(d_obj, 0, sizeof(double) * 2, st));
+            k_extract_user<V><<<args.apply_blocks, kBlock, 0, st>>>(
+                args.X[cur], args.Y[cur], args.dc, args.dr, d_perm_col, d_perm_row, d_cuser, d_lbuser, d_ubuser,
+                lb_user.empty() ? 0.0 : lb_user[0], ub_user.empty() ? 0.0 : ub_user[0], d_xout, d_yout, n, m,
+                args.part_aux, reinterpret_cast<uint32_t*>(d_obj + 1), d_obj);
+        } else {
+            k_extract<V><<<args.apply_blocks, kBlock, 0, st>>>(args.X[cur], args.Y[cur], args.dc, args.dr, d_perm_col,
+                                                               d_perm_row, d_xout, d_yout, n, m);
+        }
         launches += 1;
         SPS_CK(cudaGetLastError());
         SPS_CK(cudaEventRecord(ev1, st));
-        std::vector<double> xo(n), yo(m);
         SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
-        SPS_CK(cudaMemcpyAsync(xo.data(), d_xout, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
-        SPS_CK(cudaMemcpyAsync(yo.data(), d_yout, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        std::vector<double> xo, yo;
+        if (adaptive) {
+            SPS_CK(cudaMemcpyAsync(&obj, d_obj, sizeof(double), cudaMemcpyDeviceToHost, st));
+        } else {
+            xo.resize(n);
+            yo.resize(m);
+            SPS_CK(cudaMemcpyAsync(xo.data(), d_xout, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+            SPS_CK(cudaMemcpyAsync(yo.data(), d_yout, sizeof(double) * m, cudaMemcpyDeviceToHost, st));
+        }
         SPS_CK(cudaStreamSynchronize(st));
         float ms = 0;
         cudaEventElapsedTime(&ms, ev0, ev1);
-        to_user(xo, yo);
+        sol_on_device = adaptive;
+        if (!adaptive) {
+            to_user(xo, yo);
+            for (int j = 0; j < n_user; ++j) obj += c_user[j] * x_sol[j];
+        }
         res->status = status;
         res->restarts = h_ctl->restarts;
         res->iterations = h_ctl->iters;
@@ -1098,8 +1201,6 @@ struct Engine : EngineBase {
         res->kernel_launches = launches;
         res->returned_average = h_ctl->choice;
         res->warm_start_used = warm_used ? 1 : 0;
-        double obj = 0;
-        for (int j = 0; j < n_user; ++j) obj += c_user[j] * x_sol[j];
         res->objective = obj;
         solved = true;
         return SPS_OK;
@@ -1107,6 +1208,7 @@ struct Engine : EngineBase {
 
     // Problems with no rows or no columns: nothing runs on the device.
     int solve_trivial(sps_result* res) {
+        sol_on_device = false;
         x_sol.assign(n_user, 0.0);
         y_sol.assign(m_user, 0.0);
         res->status = SPS_STATUS_OPTIMAL;
@@ -1242,6 +1344,13 @@ struct Engine : EngineBase {
 
     int get(double* x, double* y) override {
         if (!solved) return fail(SPS_ERR_STATE, "no solution: call sps_solve first");
+        if (sol_on_device) {
+            SPS_CK(cudaSetDevice(opt.device));
+            if (x) SPS_CK(cudaMemcpyAsync(x, d_xout, sizeof(double) * n_user, cudaMemcpyDeviceToHost, st));
+            if (y) SPS_CK(cudaMemcpyAsync(y, d_yout, sizeof(double) * m_user, cudaMemcpyDeviceToHost, st));
+            SPS_CK(cudaStreamSynchronize(st));
+            return SPS_OK;
+        }
         if (x) std::memcpy(x, x_sol.data(), sizeof(double) * n_user);
         if (y) std::memcpy(y, y_sol.data(), sizeof(double) * m_user);
         return SPS_OK;

@@ -296,4 +296,50 @@ __global__ void k_extract(const V* __restrict__ x, const V* __restrict__ y, cons
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) yo[perm_row[i]] = double(y[i]) * dr[i];
 }
 
+// Adaptive mode's solution in the caller's space, on the device: x in the
+// caller's column order, unscaled and clipped to the caller's bounds (as
+// FP64 arrays, or the uniform scalars lo_u / hi_u when lb and ub are null;
+// infinite bounds clip at +-1e30), y unscaled in the caller's row order, and
+// c^T x: per-block partials in part, summed in block order by the last block
+// (ticket) into *obj.
+template <class V>
+__global__ void k_extract_user(const V* __restrict__ x, const V* __restrict__ y, const double* __restrict__ dc,
+                               const double* __restrict__ dr, const int32_t* __restrict__ perm_col,
+                               const int32_t* __restrict__ perm_row, const double* __restrict__ c,
+                               const double* __restrict__ lb, const double* __restrict__ ub, double lo_u,
+                               double hi_u, double* __restrict__ xo, double* __restrict__ yo, int32_t n, int32_t m,
+                               double* __restrict__ part, uint32_t* ticket, double* obj) {
+    __shared__ double sm[256 / 32];
+    __shared__ bool last;
+    const int stride = gridDim.x * blockDim.x;
+    double acc = 0.0;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += stride) {
+        const int o = perm_col[j];
+        double lo = lb ? lb[o] : lo_u, hi = ub ? ub[o] : hi_u;
+        lo = isfinite(lo) ? lo : -1e30;
+        hi = isfinite(hi) ? hi : 1e30;
+        const double v = fmin(fmax(double(x[j]) * dc[j], lo), hi);
+        xo[o] = v;
+        acc += c[o] * v;
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) yo[perm_row[i]] = double(y[i]) * dr[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) b += sm[w];
+        part[blockIdx.x] = b;
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    double t = 0.0;
+    for (int b = 0; b < (int)gridDim.x; ++b) t += __ldcg(part + b);
+    *obj = t;
+    *ticket = 0u;
+}
+
 }  // namespace sps
