@@ -360,6 +360,16 @@ def run_ours(args, rank, world):
                                         ((kt[0] if dom == "col" else kt[1]) / 1e3) / 1e9)},
         "clocks": clk.summary(),
     }
+    if args.config == 2:
+        # the row pass's random gathers against the floor of a pass with random indices
+        # over a vector of n entries (same nonzeros, nothing else in the kernel)
+        gf = np.zeros(2)
+        N.check(N.load().sps_time_gather_floor(int(ib["nnz"]), int(p.n_vars), 20, args.device, N.f64p(gf)), None)
+        line["gather_floor"] = {
+            "random_ms": gf[0], "in_order_ms": gf[1], "nnz": int(ib["nnz"]), "vector": int(p.n_vars),
+            "row_pass_over_random_floor": kt[0] / gf[0],
+            "what": ("sps_time_gather_floor: 16-byte index and value loads, 4 gathers per thread, nothing else; "
+                     "random = uniform column indices, in_order = the same bytes with indices walking x")}
     # whole solve: both passes' algorithmic bytes per attempt x attempts / solve time (the checks,
     # one per 64 attempts, move more bytes that are not counted)
     line["solve_avg_gbs"] = (ib["row"] + ib["col"]) * it_med / (t_max / args.steps) / 1e9

@@ -184,6 +184,16 @@ int sps_get_solution(sps_handle *h, double *x, double *y);
  * solution returned by sps_get_solution is not affected. */
 int sps_time_iteration_kernels(sps_handle *h, int32_t reps, double *out);
 
+/* Benchmark support (no reference counterpart): the floor of a sparse pass over
+ * nnz nonzeros whose column indices are uniform random over a vector of
+ * vec_len FP32 entries — each thread reads four consecutive int32 indices and
+ * FP32 values as 16-byte loads and gathers x at them, nothing else — timed with
+ * CUDA events on device `device`, `reps` passes after one warm-up, one
+ * resident wave of blocks.  out[0] = mean ms with random indices, out[1] = mean
+ * ms with indices walking x in order (the same bytes streamed).  Allocates and
+ * frees its own device memory.  Errors: sps_last_error(NULL). */
+int sps_time_gather_floor(int64_t nnz, int32_t vec_len, int32_t reps, int32_t device, double *out);
+
 /* Message of the last error on this handle (or of the last failed sps_create when h is NULL). */
 const char *sps_last_error(const sps_handle *h);
 

@@ -36,8 +36,14 @@ constexpr int kBlock = 256;          // threads per block of every pass kernel
 constexpr int kWarps = kBlock / 32;
 constexpr int kMaxBins = 8;
 constexpr int kSliceMax = 32;        // rows up to this length are SLICED
-constexpr int kSegment = 512;        // WARP rows up to this length; SEGMENT size above it
-constexpr int kSlabSteps = 32;       // steps (32-entry columns of a slice) per SLAB unit
+#ifndef SPS_SEGMENT_NNZ
+#define SPS_SEGMENT_NNZ 512
+#endif
+#ifndef SPS_SLAB_STEPS
+#define SPS_SLAB_STEPS 32
+#endif
+constexpr int kSegment = SPS_SEGMENT_NNZ;   // WARP rows up to this length; SEGMENT size above it
+constexpr int kSlabSteps = SPS_SLAB_STEPS;  // steps (32-entry columns of a slice) per SLAB unit
 
 enum BinMode { BM_SLICED = 0, BM_WARP = 1, BM_SEGMENT = 2, BM_SLAB = 3 };
 
@@ -231,7 +237,10 @@ __device__ __forceinline__ uint64_t global_ns() {
 // and the gather functor g(q, j) returns vector q at column j (as Acc).
 // All control flow below is warp-uniform, so full-mask shuffles are safe.
 
-constexpr int kUnroll = 8;
+#ifndef SPS_UNROLL
+#define SPS_UNROLL 8
+#endif
+constexpr int kUnroll = SPS_UNROLL;
 // Partial loads in flight when a row's (slice's) last unit adds its units'
 // partials (the adds stay in unit order): 16 for one FP32 value per unit (a
 // transportation demand slice has 32 units: two round trips instead of four),

@@ -147,3 +147,12 @@ def test_integration_stub_matches_the_abi():
         assert [f for f, _ in stub._fields_] == [f for f, _ in ours._fields_], stub.__name__
         for f, _ in stub._fields_:
             assert getattr(stub, f).offset == getattr(ours, f).offset, (stub.__name__, f)
+
+
+def test_gather_floor_rejects_bad_arguments():
+    """The gather-floor benchmark checks its arguments before any device work."""
+    lib = N.load()
+    out = np.zeros(2)
+    for args in ((0, 10, 1), (100, 0, 1), (100, 10, 0)):
+        assert lib.sps_time_gather_floor(args[0], args[1], args[2], 0, N.f64p(out)) == -1
+    assert lib.sps_time_gather_floor(100, 10, 1, 0, None) == -1
