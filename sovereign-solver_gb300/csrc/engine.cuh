@@ -315,6 +315,51 @@ __device__ __forceinline__ void visit_slice_pair(const Bin& b, int s0, int s1, c
     if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
 }
 
+// SLICED bin whose rows all have LEN nonzeros (slice offsets computed
+// from the bin's start): exactly LEN steps, no predicated or padding work —
+// the generic loop above runs four steps per iteration and gathers for the
+// padded ones too (half the gathers of 2-nonzero columns).  The same additions
+// in the same order as the generic loop (its padded steps add zeros).
+template <int NV, int LEN, class Acc, class V, class Gather, class Epi>
+__device__ __forceinline__ void visit_slice_pair_fixed(const Bin& b, int s0, int s1, const Layout<V>& L,
+                                                       const Gather& g, Epi& e) {
+    const int lane = threadIdx.x & 31;
+    const bool has1 = s1 < b.units;
+    const int S[2] = {s0, has1 ? s1 : s0};
+    int r[2];
+    typename Epi::Pre pre[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        r[h] = b.begin + S[h] * 32 + lane;
+        if (r[h] < b.end && (h == 0 || has1)) pre[h] = e.pre(r[h]);
+    }
+    int j[2][LEN];
+    Acc a[2][LEN];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int u = 0; u < LEN; ++u) {
+            const int p = b.slice0 + S[h] * 32 * LEN + lane + 32 * u;
+            const bool ok = h == 0 || has1;                   // warp-uniform
+            j[h][u] = ok ? __ldg(L.idx + p) : 0;
+            a[h][u] = ok ? Acc(__ldg(L.val + p)) : Acc(0);
+        }
+    Acc acc[2][NV];
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) acc[h][q] = Acc(0);
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+        if (h == 0 || has1)
+#pragma unroll
+            for (int u = 0; u < LEN; ++u)
+#pragma unroll
+                for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
+    if (r[0] < b.end) e(r[0], b.kind, acc[0], pre[0]);
+    if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
+}
+
 // Dot products of nonzeros [s, t) with the warp (lane-strided, predicated).
 template <int NV, class Acc, class V, class Gather>
 __device__ __forceinline__ void warp_dot(int s, int t, const Layout<V>& L, const Gather& g, Acc (&acc)[NV]) {
@@ -689,7 +734,19 @@ __device__ __forceinline__ void visit_bins(const BinTable& bt, int block, const 
     const int stride = b.nblocks * kWarps;
     const int w0 = (block - b.block_begin) * kWarps + (threadIdx.x >> 5);
     if (b.mode == BM_SLICED) {
-        for (int u = w0; u < b.units; u += 2 * stride) visit_slice_pair<NV, Acc>(b, u, u + stride, L, g, e);
+        // rows of one or two nonzeros each (the columns of transportation and assignment
+        // LPs): the exact-length loop (FP32 iterates; in the FP64 engine its extra code
+        // spills at the step kernels' register budget)
+        switch (sizeof(V) == 4 ? b.part0 : 0) {
+        case 1:
+            for (int u = w0; u < b.units; u += 2 * stride) visit_slice_pair_fixed<NV, 1, Acc>(b, u, u + stride, L, g, e);
+            break;
+        case 2:
+            for (int u = w0; u < b.units; u += 2 * stride) visit_slice_pair_fixed<NV, 2, Acc>(b, u, u + stride, L, g, e);
+            break;
+        default:
+            for (int u = w0; u < b.units; u += 2 * stride) visit_slice_pair<NV, Acc>(b, u, u + stride, L, g, e);
+        }
     } else if (b.mode == BM_WARP) {
         for (int u = w0; u < b.units; u += 2 * stride) visit_warp_row_pair<NV, Acc>(b, u, u + stride, L, g, e);
     } else if (b.mode == BM_SEGMENT) {
