@@ -184,6 +184,12 @@ int sps_get_solution(sps_handle *h, double *x, double *y);
  * solution returned by sps_get_solution is not affected. */
 int sps_time_iteration_kernels(sps_handle *h, int32_t reps, double *out);
 
+/* The same launches and outputs as sps_time_iteration_kernels, captured with
+ * their events (as event nodes) into one CUDA graph that is replayed once: the
+ * kernels run back to back from the device as in the solve's own graph, so
+ * out[0] + out[1] is the in-graph time of one step attempt. */
+int sps_time_iteration_kernels_graph(sps_handle *h, int32_t reps, double *out);
+
 /* Benchmark support (no reference counterpart): the floor of a sparse pass over
  * nnz nonzeros whose column indices are uniform random over a vector of
  * vec_len FP32 entries — each thread reads four consecutive int32 indices and

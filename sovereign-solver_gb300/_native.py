@@ -130,6 +130,7 @@ def load() -> C.CDLL:
         "sps_version": (C.c_char_p, []),
         "sps_device_count": (C.c_int, []),
         "sps_time_iteration_kernels": (C.c_int, [H, C.c_int32, _f64p]),
+        "sps_time_iteration_kernels_graph": (C.c_int, [H, C.c_int32, _f64p]),
         "sps_time_gather_floor": (C.c_int, [C.c_int64, C.c_int32, C.c_int32, C.c_int32, _f64p]),
         "sps_kkt_noalloc": (C.c_int, [C.POINTER(DeviceLP), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
         "sps_batch_create": (C.c_int, [C.c_int32, C.POINTER(ProblemDesc), C.POINTER(Options), C.POINTER(H)]),

@@ -376,7 +376,12 @@ int sps_solve(sps_handle* h, sps_result* res) {
 
 int sps_time_iteration_kernels(sps_handle* h, int32_t reps, double* out) {
     if (!h || !out) return SPS_ERR_INVALID;
-    return h->eng->time_kernels(reps, out);
+    return h->eng->time_kernels(reps, out, false);
+}
+
+int sps_time_iteration_kernels_graph(sps_handle* h, int32_t reps, double* out) {
+    if (!h || !out) return SPS_ERR_INVALID;
+    return h->eng->time_kernels(reps, out, true);
 }
 
 int sps_get_solution(sps_handle* h, double* x, double* y) {

@@ -62,7 +62,9 @@ struct EngineBase {
     virtual int solve(sps_result* res) = 0;
     virtual int warm(const double* x0, const double* y0, double omega0) = 0;
     virtual int get(double* x, double* y) = 0;
-    virtual int time_kernels(int reps, double* out) = 0;
+    // graph: capture the launches and events into one CUDA graph and replay it
+    // (the kernels run back to back from the device, as in the solve's graph)
+    virtual int time_kernels(int reps, double* out, bool graph) = 0;
     // Best point of the last solve's stall test in the caller's space, and the
     // primal weight it was taken with (the returned point when none was saved).
     virtual int get_best(double* x, double* y, double* omega) = 0;
@@ -1264,7 +1266,7 @@ struct Engine : EngineBase {
 
     // Per-launch timing of the two iteration kernels on the resident state.
     // The control block is saved, opened for `reps` more iterations, and restored.
-    int time_kernels(int reps, double* out) override {
+    int time_kernels(int reps, double* out, bool graph) override {
         if (!solved) return fail(SPS_ERR_STATE, "call sps_solve before timing kernels");
         if (reps <= 0) return fail(SPS_ERR_INVALID, "reps must be positive");
         if (trivial) { out[0] = out[1] = 0.0; out[2] = 1.0; return SPS_OK; }
@@ -1281,21 +1283,39 @@ struct Engine : EngineBase {
         const int gr = args.rows.total_blocks, gc = args.cols.total_blocks;
         Args<V> a = args;
         a.has_cond = 0;
-        SPS_CK(cudaEventRecord(ev[0], st));
-        for (int r = 0; r < reps; ++r) {
+        // in a capture the records become event nodes of the graph
+        const unsigned rec_flags = graph ? cudaEventRecordExternal : cudaEventRecordDefault;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t ge = nullptr;
+        if (graph) SPS_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        cudaError_t rec = cudaEventRecordWithFlags(ev[0], st, rec_flags);
+        for (int r = 0; r < reps && rec == cudaSuccess; ++r) {
             if (mode == SPS_MODE_ADAPTIVE) {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
+                rec = cudaEventRecordWithFlags(ev[2 * r + 1], st, rec_flags);
                 ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
             } else {
                 rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
+                rec = cudaEventRecordWithFlags(ev[2 * r + 1], st, rec_flags);
                 rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
             }
-            SPS_CK(cudaEventRecord(ev[2 * r + 2], st));
+            if (rec == cudaSuccess) rec = cudaEventRecordWithFlags(ev[2 * r + 2], st, rec_flags);
         }
-        SPS_CK(cudaGetLastError());
-        SPS_CK(cudaStreamSynchronize(st));
+        if (rec == cudaSuccess) rec = cudaGetLastError();
+        if (graph) {
+            const cudaError_t end = cudaStreamEndCapture(st, &g);   // always ends the capture
+            if (rec == cudaSuccess) rec = end;
+            if (rec == cudaSuccess) rec = cudaGraphInstantiate(&ge, g, 0);
+            if (rec == cudaSuccess) rec = cudaGraphLaunch(ge, st);
+        }
+        if (rec == cudaSuccess) rec = cudaStreamSynchronize(st);
+        if (ge) cudaGraphExecDestroy(ge);
+        if (g) cudaGraphDestroy(g);
+        if (rec != cudaSuccess) {
+            for (auto& e : ev) cudaEventDestroy(e);
+            cudaMemcpy(d_ctl, &saved, sizeof(Ctl), cudaMemcpyHostToDevice);
+            return fail(SPS_ERR_CUDA, std::string("timing the iteration kernels: ") + cudaGetErrorString(rec));
+        }
         double row = 0, col = 0;
         for (int r = 0; r < reps; ++r) {
             float a1 = 0, a2 = 0;

@@ -1,7 +1,8 @@
 """LP input type, field-for-field the reference's ``Problem`` dataclass.
 
 Mirrors ``solver/problem.py:19-67`` (fields), ``:71-99`` (derived sizes),
-``:103-142`` (``validate``), ``:146-158`` (``empty``) and ``:160-169``
+``:103-142`` (``validate``: ``ValueError`` on the same conditions, in this
+module's own wording), ``:146-158`` (``empty``) and ``:160-169``
 (``eval_obj``) of the reference, so a reference ``Problem`` and this one are
 interchangeable at the solver boundary (the solver only reads attributes).
 
@@ -62,32 +63,24 @@ class Problem:
         return self.P_qp is not None
 
     def validate(self) -> None:
-        """Raise ``ValueError`` listing every inconsistent dimension."""
-        n = self.n_vars
-        errs = []
-        if self.A_ub.shape != (self.n_ineq, n):
-            errs.append(f"A_ub shape {self.A_ub.shape} inconsistent with n_vars={n}")
-        if np.shape(self.b_ub) != (self.n_ineq,):
-            errs.append(f"b_ub shape {np.shape(self.b_ub)} != ({self.n_ineq},)")
-        if self.A_eq.shape != (self.n_eq, n):
-            errs.append(f"A_eq shape {self.A_eq.shape} inconsistent with n_vars={n}")
-        if np.shape(self.b_eq) != (self.n_eq,):
-            errs.append(f"b_eq shape {np.shape(self.b_eq)} != ({self.n_eq},)")
-        if np.shape(self.lb) != (n,):
-            errs.append(f"lb shape {np.shape(self.lb)} != ({n},)")
-        if np.shape(self.ub) != (n,):
-            errs.append(f"ub shape {np.shape(self.ub)} != ({n},)")
-        if np.shape(self.integer_mask) != (n,):
-            errs.append(f"integer_mask shape {np.shape(self.integer_mask)} != ({n},)")
+        """Raise ``ValueError`` naming every field whose shape does not fit the
+        others (and any variable whose lower bound exceeds its upper bound)."""
+        n, mu, me = self.n_vars, self.n_ineq, self.n_eq
+        want = [("A_ub", np.shape(self.A_ub), (mu, n)), ("b_ub", np.shape(self.b_ub), (mu,)),
+                ("A_eq", np.shape(self.A_eq), (me, n)), ("b_eq", np.shape(self.b_eq), (me,)),
+                ("lb", np.shape(self.lb), (n,)), ("ub", np.shape(self.ub), (n,)),
+                ("integer_mask", np.shape(self.integer_mask), (n,))]
+        if self.P_qp is not None:
+            want.append(("P_qp", np.shape(self.P_qp), (n, n)))
+        problems = [f"{field}: shape {got}, expected {exp}" for field, got, exp in want if tuple(got) != exp]
         if self.sense not in ("min", "max"):
-            errs.append(f"sense must be 'min' or 'max', got '{self.sense}'")
-        if self.P_qp is not None and self.P_qp.shape != (n, n):
-            errs.append(f"P_qp shape {self.P_qp.shape} inconsistent with n_vars={n}")
-        if not errs and np.any(self.lb > self.ub + 1e-12):
-            bad = np.where(self.lb > self.ub + 1e-12)[0]
-            errs.append(f"lb > ub for variables: {bad[:5].tolist()} ...")
-        if errs:
-            raise ValueError("Problem validation failed:\n  " + "\n  ".join(errs))
+            problems.append(f"sense: {self.sense!r} is neither 'min' nor 'max'")
+        if not problems:
+            crossed = np.flatnonzero(self.lb > self.ub + 1e-12)
+            if crossed.size:
+                problems.append(f"lb above ub at {crossed.size} variable(s), first {crossed[:5].tolist()}")
+        if problems:
+            raise ValueError(f"invalid Problem {self.name!r}: " + "; ".join(problems))
 
     @classmethod
     def empty(cls, n: int) -> "Problem":
@@ -111,6 +104,5 @@ class Problem:
         return -v if self.sense == "max" else v
 
     def __repr__(self) -> str:
-        kind = "MILP" if self.is_milp else ("QP" if self.is_qp else "LP")
-        return (f"Problem(name={self.name!r}, type={kind}, n_vars={self.n_vars}, "
-                f"n_ineq={self.n_ineq}, n_eq={self.n_eq})")
+        kind = "MILP" if self.is_milp else "QP" if self.is_qp else "LP"
+        return f"Problem({self.name!r}, {kind}, {self.n_vars} vars, {self.n_ineq} <=, {self.n_eq} =)"
