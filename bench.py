@@ -360,7 +360,8 @@ def run_ours(args, rank, world):
         "e2e": {"value": world / e2e_t, "unit": "solves/s", "sec_per_solve": e2e_t,
                 "h2d_bytes_per_step": problem_bytes(p), "d2h_bytes_per_step": 8 * (len(x) + len(y))},
         "kernel_ms": {"row_pass": kg[0], "col_pass": kg[1], "accept_rate": kg[2],
-                      "timing": "CUDA event nodes between the kernels of one replayed graph of 20 step attempts",
+                      "timing": ("in-graph: events around replays of a graph of 20 x [row, column] passes and of one "
+                                 "of 20 x [row] passes; column = the difference"),
                       "host_launched": {"row_pass": kt[0], "col_pass": kt[1]}},
         "attempt": {"us_in_graph": (kg[0] + kg[1]) * 1e3,
                     "gbs": (ib["row"] + ib["col"]) / ((kg[0] + kg[1]) / 1e3) / 1e9,

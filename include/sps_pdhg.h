@@ -184,10 +184,13 @@ int sps_get_solution(sps_handle *h, double *x, double *y);
  * solution returned by sps_get_solution is not affected. */
 int sps_time_iteration_kernels(sps_handle *h, int32_t reps, double *out);
 
-/* The same launches and outputs as sps_time_iteration_kernels, captured with
- * their events (as event nodes) into one CUDA graph that is replayed once: the
- * kernels run back to back from the device as in the solve's own graph, so
- * out[0] + out[1] is the in-graph time of one step attempt. */
+/* The same kernels and outputs as sps_time_iteration_kernels, timed as the
+ * solve's own graph runs them (back to back from the device, no host launch
+ * gaps): one CUDA graph of `reps` x [row pass, column pass] and one of `reps`
+ * x [row pass] are captured on the handle's stream and replayed (after one
+ * warm-up replay each) between two events; out[0] = the second's time / reps,
+ * out[1] = (the first's - the second's) / reps, so out[0] + out[1] is the
+ * in-graph time of one step attempt. */
 int sps_time_iteration_kernels_graph(sps_handle *h, int32_t reps, double *out);
 
 /* Benchmark support (no reference counterpart): the floor of a sparse pass over

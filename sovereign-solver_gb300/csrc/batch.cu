@@ -611,8 +611,22 @@ struct SetupArgs {
 };
 
 // per row (warp each): stat = d_own[r] * max|v d_other| (or the sum)
+// short: every row holds at most two entries, and a thread per row computes
+// what the warp form does (its butterfly sum of two terms is t0 + t1 too: the
+// other lanes add exact zeros), without 30 idle lanes per row
 __device__ void row_stat(const int32_t* ptr, const int32_t* idx, const double* v, const double* d_own,
-                         const double* d_other, int rows, bool sum, float* out) {
+                         const double* d_other, int rows, bool sum, float* out, bool short_rows) {
+    if (short_rows) {
+        for (int r = threadIdx.x; r < rows; r += kBlock) {
+            double a = 0.0;
+            for (int k = ptr[r]; k < ptr[r + 1]; ++k) {
+                const double t = fabs(v[k] * d_other[idx[k]]);
+                a = sum ? a + t : fmax(a, t);
+            }
+            out[r] = float(a * d_own[r]);
+        }
+        return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int r = warp; r < rows; r += kWarps) {
         double a = 0.0;
@@ -635,13 +649,28 @@ __global__ void __launch_bounds__(kBlock) k_batch_setup(SetupArgs S) {
     const double *rv = S.rv64 + I.re, *cv = S.cv64 + I.ce;
     double *dr = S.dr + I.vr, *dc = S.dc + I.vc;
     float *rm = S.rmax + I.vr, *cm = S.cmax + I.vc;
-    for (int j = threadIdx.x; j < I.n; j += kBlock) dc[j] = 1.0;
-    for (int i = threadIdx.x; i < I.m; i += kBlock) dr[i] = 1.0;
+    __shared__ int longest[2];                  // longest row, longest column
+    if (threadIdx.x < 2) longest[threadIdx.x] = 0;
     __syncthreads();
+    {
+        int lr = 0, lc = 0;
+        for (int j = threadIdx.x; j < I.n; j += kBlock) {
+            dc[j] = 1.0;
+            lc = max(lc, cptr[j + 1] - cptr[j]);
+        }
+        for (int i = threadIdx.x; i < I.m; i += kBlock) {
+            dr[i] = 1.0;
+            lr = max(lr, rptr[i + 1] - rptr[i]);
+        }
+        atomicMax(&longest[0], lr);
+        atomicMax(&longest[1], lc);
+    }
+    __syncthreads();
+    const bool short_rows = longest[0] <= 2, short_cols = longest[1] <= 2;
     for (int it = 0; it <= S.ruiz; ++it) {
         const bool pc = it == S.ruiz;           // last pass: Pock-Chambolle (sums), before it Ruiz (max)
-        row_stat(rptr, ridx, rv, dr, dc, I.m, pc, rm);
-        row_stat(cptr, cidx, cv, dc, dr, I.n, pc, cm);
+        row_stat(rptr, ridx, rv, dr, dc, I.m, pc, rm, short_rows);
+        row_stat(cptr, cidx, cv, dc, dr, I.n, pc, cm, short_cols);
         __syncthreads();
         for (int i = threadIdx.x; i < I.m; i += kBlock)
             if (rm[i] > 0.f) dr[i] /= sqrt(double(rm[i]));
@@ -651,14 +680,18 @@ __global__ void __launch_bounds__(kBlock) k_batch_setup(SetupArgs S) {
     }
     double mx = 0.0, sc = 0.0, sb = 0.0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int r = warp; r < I.m; r += kWarps)
-        for (int q = rptr[r] + lane; q < rptr[r + 1]; q += 32) {
+    // (a thread per row or column where they are short: the same values, the same maximum)
+    const int rstep = short_rows ? kBlock : kWarps, rlane = short_rows ? 1 : 32;
+    for (int r = short_rows ? threadIdx.x : warp; r < I.m; r += rstep)
+        for (int q = rptr[r] + (short_rows ? 0 : lane); q < rptr[r + 1]; q += rlane) {
             const float v = float(rv[q] * dr[r] * dc[ridx[q]]);
             S.rval[I.re + q] = v;
             mx = fmax(mx, fabs(double(v)));
         }
-    for (int j = warp; j < I.n; j += kWarps)
-        for (int q = cptr[j] + lane; q < cptr[j + 1]; q += 32) S.cval[I.ce + q] = float(cv[q] * dc[j] * dr[cidx[q]]);
+    const int cstep = short_cols ? kBlock : kWarps, clane = short_cols ? 1 : 32;
+    for (int j = short_cols ? threadIdx.x : warp; j < I.n; j += cstep)
+        for (int q = cptr[j] + (short_cols ? 0 : lane); q < cptr[j + 1]; q += clane)
+            S.cval[I.ce + q] = float(cv[q] * dc[j] * dr[cidx[q]]);
     for (int j = threadIdx.x; j < I.n; j += kBlock) {
         const double cs = S.c64[I.vc + j] * dc[j];
         S.c[I.vc + j] = float(cs);

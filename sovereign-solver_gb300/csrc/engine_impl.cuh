@@ -1283,39 +1283,71 @@ struct Engine : EngineBase {
         const int gr = args.rows.total_blocks, gc = args.cols.total_blocks;
         Args<V> a = args;
         a.has_cond = 0;
-        // in a capture the records become event nodes of the graph
-        const unsigned rec_flags = graph ? cudaEventRecordExternal : cudaEventRecordDefault;
-        cudaGraph_t g = nullptr;
-        cudaGraphExec_t ge = nullptr;
-        if (graph) SPS_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        cudaError_t rec = cudaEventRecordWithFlags(ev[0], st, rec_flags);
-        for (int r = 0; r < reps && rec == cudaSuccess; ++r) {
+        if (graph) {
+            // two graphs captured from the stream: reps x [row pass, column pass] and reps x
+            // [row pass], each timed by events around its replay (no events between the
+            // kernels, which would add their own gaps): row = the second / reps, column =
+            // (the first - the second) / reps
+            float tg[2] = {0.f, 0.f};
+            cudaError_t rec = cudaSuccess;
+            for (int variant = 0; variant < 2 && rec == cudaSuccess; ++variant) {
+                cudaGraph_t g = nullptr;
+                cudaGraphExec_t ge = nullptr;
+                rec = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
+                if (rec != cudaSuccess) break;
+                for (int r = 0; r < reps; ++r) {
+                    if (mode == SPS_MODE_ADAPTIVE) {
+                        ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
+                        if (variant == 0) ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+                    } else {
+                        rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
+                        if (variant == 0) rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
+                    }
+                }
+                rec = cudaGetLastError();
+                const cudaError_t end = cudaStreamEndCapture(st, &g);     // always ends the capture
+                if (rec == cudaSuccess) rec = end;
+                if (rec == cudaSuccess) rec = cudaGraphInstantiate(&ge, g, 0);
+                if (rec == cudaSuccess) rec = cudaGraphLaunch(ge, st);   // warm-up replay
+                if (rec == cudaSuccess) rec = cudaEventRecord(ev[0], st);
+                if (rec == cudaSuccess) rec = cudaGraphLaunch(ge, st);
+                if (rec == cudaSuccess) rec = cudaEventRecord(ev[1], st);
+                if (rec == cudaSuccess) rec = cudaStreamSynchronize(st);
+                if (rec == cudaSuccess) rec = cudaEventElapsedTime(&tg[variant], ev[0], ev[1]);
+                if (ge) cudaGraphExecDestroy(ge);
+                if (g) cudaGraphDestroy(g);
+                if (variant == 0 && rec == cudaSuccess) {
+                    Ctl after;
+                    rec = cudaMemcpy(&after, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost);
+                    out[2] = mode == SPS_MODE_ADAPTIVE
+                                 ? double(after.accepted_total - t.accepted_total) / (2.0 * reps) : 1.0;
+                    if (rec == cudaSuccess) rec = cudaMemcpy(d_ctl, &t, sizeof(Ctl), cudaMemcpyHostToDevice);
+                }
+            }
+            for (auto& e : ev) cudaEventDestroy(e);
+            const cudaError_t back = cudaMemcpy(d_ctl, &saved, sizeof(Ctl), cudaMemcpyHostToDevice);
+            if (rec == cudaSuccess) rec = back;
+            if (rec != cudaSuccess)
+                return fail(SPS_ERR_CUDA, std::string("timing the iteration kernels: ") + cudaGetErrorString(rec));
+            out[0] = tg[1] / reps;
+            out[1] = (tg[0] - tg[1]) / reps;
+            return SPS_OK;
+        }
+        SPS_CK(cudaEventRecord(ev[0], st));
+        for (int r = 0; r < reps; ++r) {
             if (mode == SPS_MODE_ADAPTIVE) {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                rec = cudaEventRecordWithFlags(ev[2 * r + 1], st, rec_flags);
+                SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
                 ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
             } else {
                 rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                rec = cudaEventRecordWithFlags(ev[2 * r + 1], st, rec_flags);
+                SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
                 rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
             }
-            if (rec == cudaSuccess) rec = cudaEventRecordWithFlags(ev[2 * r + 2], st, rec_flags);
+            SPS_CK(cudaEventRecord(ev[2 * r + 2], st));
         }
-        if (rec == cudaSuccess) rec = cudaGetLastError();
-        if (graph) {
-            const cudaError_t end = cudaStreamEndCapture(st, &g);   // always ends the capture
-            if (rec == cudaSuccess) rec = end;
-            if (rec == cudaSuccess) rec = cudaGraphInstantiate(&ge, g, 0);
-            if (rec == cudaSuccess) rec = cudaGraphLaunch(ge, st);
-        }
-        if (rec == cudaSuccess) rec = cudaStreamSynchronize(st);
-        if (ge) cudaGraphExecDestroy(ge);
-        if (g) cudaGraphDestroy(g);
-        if (rec != cudaSuccess) {
-            for (auto& e : ev) cudaEventDestroy(e);
-            cudaMemcpy(d_ctl, &saved, sizeof(Ctl), cudaMemcpyHostToDevice);
-            return fail(SPS_ERR_CUDA, std::string("timing the iteration kernels: ") + cudaGetErrorString(rec));
-        }
+        SPS_CK(cudaGetLastError());
+        SPS_CK(cudaStreamSynchronize(st));
         double row = 0, col = 0;
         for (int r = 0; r < reps; ++r) {
             float a1 = 0, a2 = 0;

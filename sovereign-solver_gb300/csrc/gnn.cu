@@ -5,8 +5,9 @@
 // innermost ([instance][node][H], FP32), so every per-node kernel runs over the
 // flattened node list of the whole batch and the weight gradients are sums
 // over it.  Aggregations are CSR SpMMs (warp per destination row, float2 per
-// lane); the dense node updates stage 32 nodes and both 64x64 weight matrices
-// in shared memory (BF16 weights widened to FP32, FP32 accumulation).  Every
+// lane); the dense node update is a register-tiled FP32 contraction of
+// 128-node tiles with both weight matrices staged in shared memory (BF16
+// weights widened to FP32), its backward a 32-node-tile kernel.  Every
 // reduction (weight gradients, losses, pooling) writes per-block partials that
 // a second kernel sums in block order: training is bitwise reproducible.
 #include <cuda_bf16.h>
@@ -92,52 +93,95 @@ __global__ void __launch_bounds__(kT) k_agg(const int32_t* __restrict__ ptr, con
 }
 
 // ---- dense node update: out = relu(U h + M a + b) ---------------------------------
-// A block stages U^T and M^T (FP32) and a tile of 32 nodes (h | a, padded rows);
-// thread t computes node t / 8, outputs (t % 8) + 8 i.
+// A register-tiled FP32 contraction of the tile's [h | a] (kUpdNodes x 2H) with
+// W^T = [U | M]^T (2H x H).  The block stages W^T (BF16 widened to FP32) once
+// and, per tile, the nodes' h and a rows as they lie in memory (16-byte loads
+// and stores).  Thread t owns nodes ng + 32 i (i < 4, ng = t / 8) and outputs
+// 4 og + 32 j + c (og = t % 8, c < 4, j < H / 32): per four input features it
+// reads four 16-byte node vectors and 2 H / 8 16-byte weight vectors from
+// shared memory for 32 (H = 64) FMAs per feature, so the FMA pipe, not
+// shared memory, sets the pace.  Each output is bias + sum over k of W[o][k] x[k]
+// in k order (h's features, then a's), one fmaf per k.
+constexpr int kUpdNodes = 128;                 // nodes per tile
+
 template <int H>
-__global__ void __launch_bounds__(kT) k_update(const float* __restrict__ h, const float* __restrict__ a,
-                                               const __nv_bfloat16* __restrict__ U,
-                                               const __nv_bfloat16* __restrict__ M, const float* __restrict__ bias,
-                                               float* __restrict__ out, int64_t nodes) {
-    constexpr int OP = H / 8;                 // outputs per thread
-    constexpr int XS = 2 * H + 1;             // padded tile row
+__host__ __device__ constexpr int upd_stride() { return 2 * H + 4; }   // padded tile row: 4 consecutive rows hit distinct banks
+
+template <int H>
+__global__ void __launch_bounds__(kT, 2) k_update(const float* __restrict__ h, const float* __restrict__ a,
+                                                  const __nv_bfloat16* __restrict__ U,
+                                                  const __nv_bfloat16* __restrict__ M,
+                                                  const float* __restrict__ bias, float* __restrict__ out,
+                                                  int64_t nodes) {
+    static_assert(H % 32 == 0 && kT == 256, "thread layout: 8 output groups x 32 node groups");
+    constexpr int K2 = 2 * H, S = upd_stride<H>(), J = H / 32;
     extern __shared__ float sm[];
-    float* Ut = sm;                           // [k][o]
-    float* Mt = Ut + H * H;
-    float* X = Mt + H * H;                    // [kTile][XS]
-    for (int t = threadIdx.x; t < H * H; t += kT) {
-        const int o = t / H, k = t % H;
-        Ut[k * H + o] = __bfloat162float(U[t]);
-        Mt[k * H + o] = __bfloat162float(M[t]);
+    float* Wt = sm;                           // [k][o], k < H from U, k >= H from M
+    float* X = Wt + K2 * H;                   // [node][S]: h (k < H) then a
+    for (int t = threadIdx.x; t < K2 * H; t += kT) {
+        const int o = t / K2, k = t % K2;
+        Wt[k * H + o] = __bfloat162float(k < H ? U[o * H + k] : M[o * H + (k - H)]);
     }
-    const int node = threadIdx.x >> 3, g = threadIdx.x & 7;
-    float bo[OP];
+    const int og = threadIdx.x & 7, ng = threadIdx.x >> 3;
+    float4 bo[J];
 #pragma unroll
-    for (int i = 0; i < OP; ++i) bo[i] = bias[g + 8 * i];
-    const int64_t tiles = (nodes + kTile - 1) / kTile;
+    for (int j = 0; j < J; ++j) {
+        const float* b = bias + 4 * og + 32 * j;    // the parameter block's offsets need not be 16-byte aligned
+        bo[j] = make_float4(b[0], b[1], b[2], b[3]);
+    }
+    const int64_t tiles = (nodes + kUpdNodes - 1) / kUpdNodes;
     for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const int64_t base = tile * kTile;
+        const int64_t base = tile * kUpdNodes;
         __syncthreads();
-        for (int t = threadIdx.x; t < kTile * H; t += kT) {
-            const int nd = t / H, k = t % H;
+        for (int t = threadIdx.x; t < kUpdNodes * (K2 / 4); t += kT) {
+            const int nd = t / (K2 / 4), q = t % (K2 / 4);
             const int64_t v = base + nd;
-            X[nd * XS + k] = v < nodes ? h[v * H + k] : 0.f;
-            X[nd * XS + H + k] = v < nodes ? a[v * H + k] : 0.f;
+            float4 val = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (v < nodes)
+                val = q < H / 4 ? *reinterpret_cast<const float4*>(h + v * H + 4 * q)
+                                : *reinterpret_cast<const float4*>(a + v * H + 4 * (q - H / 4));
+            *reinterpret_cast<float4*>(X + nd * S + 4 * q) = val;
         }
         __syncthreads();
-        float acc[OP];
+        float4 acc[4][J];
 #pragma unroll
-        for (int i = 0; i < OP; ++i) acc[i] = bo[i];
-        const float* x = X + node * XS;
-        for (int k = 0; k < H; ++k) {
-            const float xh = x[k], xa = x[H + k];
+        for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int i = 0; i < OP; ++i) acc[i] += Ut[k * H + g + 8 * i] * xh + Mt[k * H + g + 8 * i] * xa;
+            for (int j = 0; j < J; ++j) acc[i][j] = bo[j];
+#pragma unroll 2
+        for (int k = 0; k < K2; k += 4) {
+            float4 xv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) xv[i] = *reinterpret_cast<const float4*>(X + (ng + 32 * i) * S + k);
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+                float4 w[J];
+#pragma unroll
+                for (int j = 0; j < J; ++j)
+                    w[j] = *reinterpret_cast<const float4*>(Wt + (k + kk) * H + 4 * og + 32 * j);
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float x = kk == 0 ? xv[i].x : kk == 1 ? xv[i].y : kk == 2 ? xv[i].z : xv[i].w;
+#pragma unroll
+                    for (int j = 0; j < J; ++j) {
+                        acc[i][j].x = fmaf(w[j].x, x, acc[i][j].x);
+                        acc[i][j].y = fmaf(w[j].y, x, acc[i][j].y);
+                        acc[i][j].z = fmaf(w[j].z, x, acc[i][j].z);
+                        acc[i][j].w = fmaf(w[j].w, x, acc[i][j].w);
+                    }
+                }
+            }
         }
-        const int64_t v = base + node;
-        if (v < nodes) {
 #pragma unroll
-            for (int i = 0; i < OP; ++i) out[v * H + g + 8 * i] = relu(acc[i]);
+        for (int i = 0; i < 4; ++i) {
+            const int64_t v = base + ng + 32 * i;
+            if (v >= nodes) continue;
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const float4 r = make_float4(relu(acc[i][j].x), relu(acc[i][j].y), relu(acc[i][j].z),
+                                             relu(acc[i][j].w));
+                *reinterpret_cast<float4*>(out + v * H + 4 * og + 32 * j) = r;
+            }
         }
     }
 }
@@ -552,7 +596,7 @@ thread_local std::string g_gnn_create_error;
     } while (0)
 
 template <int H>
-size_t update_smem() { return sizeof(float) * (2 * H * H + kTile * (2 * H + 1)); }
+size_t update_smem() { return sizeof(float) * (2 * H * H + kUpdNodes * upd_stride<H>()); }
 template <int H>
 size_t update_back_smem() { return sizeof(float) * (2 * H * H + 3 * kTile * (H + 1)); }
 
