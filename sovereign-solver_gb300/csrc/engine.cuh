@@ -131,6 +131,16 @@ struct Ctl {
     int32_t warm_used;       // batched solver: the instance started from its warm start
     double rel_kkt_lagr;     // the returned point's error in the Lagrangian form (= rel_kkt unless
                              // the single-LP engine measures the PDLP form)
+    // adaptive single-LP step hand-off: the row pass opens an attempt (pend_seq, the state
+    // index it read), the column pass's first block decides it and publishes decided_seq
+    int64_t pend_seq;        // sequence number of the attempt the last row pass opened
+    int64_t decided_seq;     // sequence number of the last decided attempt
+    double tau_next;         // eta / omega after the decision (the primal step of the column pass)
+    double wgt_next;         // eta_used after the decision (the averaging weight)
+    int32_t pend_cur;        // cur when the attempt was opened
+    int32_t step_ok;         // the decided attempt is applied (0 after a non-finite step)
+    int32_t wait_fail;       // a block of the column pass gave up waiting for the decision
+    uint32_t col_role;       // arrival counter of the column pass's blocks (block roles)
 };
 
 enum TicketSlot { T_ROW_STEP = 0, T_COL_STEP, T_ROW_CHECK, T_COL_CHECK, T_APPLY, T_AUX0, T_AUX1, T_AUX2 };
@@ -220,6 +230,16 @@ __device__ __forceinline__ T block_scalar(F f) {
     if (threadIdx.x == 0) s = T(f());
     __syncthreads();
     return s;
+}
+
+__device__ __forceinline__ int64_t ld_acquire_gpu(const int64_t* p) {
+    int64_t v;
+    asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(int64_t* p, int64_t v) {
+    asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 __device__ __forceinline__ uint64_t global_ns() {

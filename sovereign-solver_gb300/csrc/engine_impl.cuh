@@ -955,7 +955,7 @@ struct Engine : EngineBase {
         if (mode == SPS_MODE_ADAPTIVE) {
             for (int w = 0; w < W; ++w) {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+                ad_col_step<V><<<1 + gc + a.col_tail_blocks, kBlock, 0, st>>>(a);   // + the decision block
             }
             ad_check_prep<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
             ad_row_check<V><<<a.rows_chk.total_blocks, kBlock, 0, st>>>(a);
@@ -1144,6 +1144,8 @@ struct Engine : EngineBase {
         if (rc) return rc;
         SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
         SPS_CK(cudaStreamSynchronize(st));
+        if (h_ctl->wait_fail)
+            return fail(SPS_ERR_CUDA, "internal error: a column-pass block stopped waiting for the step decision");
         int status = h_ctl->status;
         if (!h_ctl->done) status = SPS_STATUS_ITERATION_LIMIT;
         if (!adaptive && status != SPS_STATUS_OPTIMAL) {
@@ -1298,7 +1300,7 @@ struct Engine : EngineBase {
                 for (int r = 0; r < reps; ++r) {
                     if (mode == SPS_MODE_ADAPTIVE) {
                         ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                        if (variant == 0) ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+                        if (variant == 0) ad_col_step<V><<<1 + gc + a.col_tail_blocks, kBlock, 0, st>>>(a);   // + the decision block
                     } else {
                         rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
                         if (variant == 0) rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
@@ -1338,7 +1340,7 @@ struct Engine : EngineBase {
             if (mode == SPS_MODE_ADAPTIVE) {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
                 SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
-                ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+                ad_col_step<V><<<1 + gc + a.col_tail_blocks, kBlock, 0, st>>>(a);   // + the decision block
             } else {
                 rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
                 SPS_CK(cudaEventRecord(ev[2 * r + 1], st));

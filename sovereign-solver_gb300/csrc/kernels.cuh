@@ -127,35 +127,52 @@ struct AdRowStepEpi {
     }
 };
 
+// The row pass ends without a serial tail: each block writes its partials of
+// ||dy||^2 and dy^T K dx, and the step decision they feed is taken by the first
+// block to reach the column pass, while the other blocks of that pass run
+// their K^T y' gathers (speculatively: y' is the new dual if the attempt is
+// accepted, as nearly all are) and wait for it only at their first update.
 template <class V>
 SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
     __shared__ V sm[kWarps * 2];
-    __shared__ bool last;
     const int cur = ctl->cur;
     const V sigma = block_scalar<V>([&] { return ctl->eta * ctl->omega; });
+    if (blockIdx.x == 0 && threadIdx.x == 0) {      // open the attempt (no block of this pass reads these)
+        ctl->pend_seq = ctl->decided_seq + 1;
+        ctl->pend_cur = cur;
+        ctl->apply = AP_STEP_PENDING;
+    }
     AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], sigma};
     visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e);
     // reductions in V: FP32 sums in the FP32 engine (the step rule's inputs)
     V v[2] = {e.dy2, e.inter};
-    V* part = reinterpret_cast<V*>(a.part_row);
-    if (!publish_partials<2>(v, part, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
-    V t[2];
-    gather_all_partials<2>(t, part, gridDim.x, a.csr, sm);
-    if (threadIdx.x != 0) return;
-    ctl->ticket[T_ROW_STEP] = 0;
-    decide_step(*ctl, double(t[0]), double(t[1]));
+    block_sum<2>(v, sm);
+    if (threadIdx.x == 0) {
+        V* part = reinterpret_cast<V*>(a.part_row);
+        part[(size_t)blockIdx.x * 2] = v[0];
+        part[(size_t)blockIdx.x * 2 + 1] = v[1];
+    }
 }
 
+// Polls of the step decision before a block of the column pass gives up (each
+// poll an L2 round trip plus a short sleep: well over 10 ms in all).
+constexpr int kDecisionPolls = 1 << 16;
+
+// Column-pass epilogue.  The speculative operands (the state the attempt makes
+// current if accepted) are loaded with the gathers; the decision is read at the
+// first update of each thread.  With pc = cur when the attempt was opened, an
+// accepted attempt makes X[1 - pc] current, writes K^T y' to ATY[1 - pc] and the
+// next candidate to X[pc].
 template <class V>
 struct AdColStepEpi {
     const Args<V>* a;
-    const V *xc, *cc, *atyo;
-    const V* xl;
-    V *aty, *xn, *xs;
-    V tau, wgt;
-    bool accepted;
+    const V* xspec;            // X[1 - pc]
+    V* xnext;                  // X[pc]
+    V* aty;                    // ATY[1 - pc]
+    int verdict = 2;           // 2 not read yet, 1 accepted, 0 rejected, -1 not applied
+    V tau = V(0), wgt = V(0);
     V dx2 = V(0);
     struct Pre { V xj, cj, lo, hi, s, l; };
     static constexpr int NP = 1;
@@ -164,55 +181,128 @@ struct AdColStepEpi {
     __device__ __forceinline__ void export_to(R* d) const { d[0] = dx2; }
     __device__ __forceinline__ Pre pre(int j) const {
         Pre p;
-        p.xj = xc[j];
-        p.cj = cc[j];
+        p.xj = xspec[j];
+        p.cj = a->c[j];
         p.lo = lo_at(*a, j);
         p.hi = hi_at(*a, j);
-        p.s = accepted ? xs[j] : V(0);
-        p.l = accepted ? xl[j] : V(0);
+        if constexpr (sizeof(V) == 4) {   // (the FP64 engine loads them at the update: registers)
+            p.s = a->xs[j];
+            p.l = a->xl[j];
+        }
         return p;
     }
-    __device__ __forceinline__ void finish(int j, V atyj, const Pre& p) {
-        if (accepted) { aty[j] = atyj; xs[j] = p.s + wgt * (p.xj - p.l); }
+    // Wait (bounded) for the decision of the open attempt; returns 1 accepted, 0 rejected,
+    // -1 not applied (non-finite step, or the wait gave up)
+    __device__ __forceinline__ int decide() {
+        verdict = -1;
+        Ctl* ctl = a->ctl;
+        const int64_t pend = __ldcg(&ctl->pend_seq);
+        int polls = 0;
+        while (ld_acquire_gpu(&ctl->decided_seq) != pend) {
+            if (++polls > kDecisionPolls) {
+                atomicExch(&ctl->wait_fail, 1);
+                ctl->status = SPS_STATUS_NUMERIC_ERROR;
+                ctl->done = 1;
+                return -1;
+            }
+            __nanosleep(64);
+        }
+        if (!__ldcg(&ctl->step_ok)) return -1;
+        tau = V(__ldcg(&ctl->tau_next));
+        wgt = V(__ldcg(&ctl->wgt_next));
+        verdict = __ldcg(&ctl->accepted) != 0 ? 1 : 0;
+        return verdict;
+    }
+    __device__ __forceinline__ void finish(int j, V atyj, const Pre& p, bool acc, V* xn) {
+        if (acc) {
+            aty[j] = atyj;
+            if constexpr (sizeof(V) == 4) a->xs[j] = p.s + wgt * (p.xj - p.l);
+            else a->xs[j] = a->xs[j] + wgt * (p.xj - a->xl[j]);
+        }
         const V x2 = clampv(p.xj - tau * (p.cj - atyj), p.lo, p.hi);
         xn[j] = x2;
         const V d = x2 - p.xj;
         dx2 += d * d;
     }
-    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) { finish(j, acc[0], p); }
+    // accepted: the gathered K^T y' and the speculative point; otherwise nothing here (a
+    // rejected attempt's columns are redone from the kept state after the block's sweep)
+    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) {
+        if (verdict == 2) decide();
+        if (verdict == 1) finish(j, acc[0], p, true, xnext);
+    }
 };
 
+// Blocks take roles in arrival order: role 0 takes the step decision (the row
+// pass's partials, then decide_step) and publishes it; roles 1 .. colblocks
+// sweep the column bins (virtual block role - 1); the rest update the dual
+// average.  The first block to arrive is running by definition, so the waits of
+// the others on its decision always end.  Partials and the last-block ticket use
+// role - 1, the grouping of a launch without the decision block.
 template <class V>
 SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->apply != AP_STEP_PENDING) return;
-    __shared__ V sm[kWarps];
+    __shared__ V sm[kWarps * 2];
     __shared__ bool last;
-    const int cur = ctl->cur;
-    const bool acc = ctl->accepted;
-    const V tau = block_scalar<V>([&] { return ctl->eta / ctl->omega; });
-    const V wgt = block_scalar<V>([&] { return ctl->eta_used; });
-    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.xl, a.ATY[cur], a.X[1 - cur], a.xs, tau, wgt, acc};
-    const int colblocks = a.cols.total_blocks;
-    if ((int)blockIdx.x < colblocks) {
-        if (acc) {
-            visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[cur]}, e);
-        } else {
-            for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock)
-                e.finish(j, e.atyo[j], e.pre(j));
+    __shared__ uint32_t role_s;
+    if (threadIdx.x == 0) role_s = atomicAdd(&ctl->col_role, 1u);
+    __syncthreads();
+    const int role = (int)role_s;
+    if (role == 0) {
+        V t[2];
+        gather_all_partials<2>(t, reinterpret_cast<const V*>(a.part_row), a.rows.total_blocks, a.csr, sm);
+        if (threadIdx.x == 0) {
+            const bool ok = decide_step(*ctl, double(t[0]), double(t[1]));
+            ctl->step_ok = ok;
+            ctl->tau_next = ctl->eta / ctl->omega;
+            ctl->wgt_next = ctl->eta_used;
+            __threadfence();
+            st_release_gpu(&ctl->decided_seq, ctl->pend_seq);
         }
-    } else if (acc) {
-        const V* yc = a.Y[cur];
-        for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
-            a.ys[i] += wgt * (yc[i] - a.yl[i]);
+        return;
+    }
+    const int vb = role - 1;
+    const int pc = ctl->pend_cur;
+    AdColStepEpi<V> e{&a, a.X[1 - pc], a.X[pc], a.ATY[1 - pc]};
+    const int colblocks = a.cols.total_blocks;
+    if (vb < colblocks) {
+        visit_bins<1, V>(a.cols, vb, a.csc, GatherOne<V>{a.Y[1 - pc]}, e);
+        // a thread that updated no column reads the decision here; rejected: the new
+        // candidate from the kept state X[pc] and its K^T y, ATY[pc]
+        if (e.verdict == 2) e.decide();
+        if (e.verdict == 0) {
+            const V* xk = a.X[pc];
+            const V* atyk = a.ATY[pc];
+            V* xn = a.X[1 - pc];
+            for (int j = vb * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock) {
+                typename AdColStepEpi<V>::Pre p;
+                p.xj = xk[j];
+                p.cj = a.c[j];
+                p.lo = lo_at(a, j);
+                p.hi = hi_at(a, j);
+                e.finish(j, atyk[j], p, false, xn);
+            }
+        }
+    } else if (e.decide() == 1) {
+        const V* yc = a.Y[1 - pc];
+        for (int i = (vb - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
+            a.ys[i] += e.wgt * (yc[i] - a.yl[i]);
     }
     V v[1] = {e.dx2};
+    block_sum<1>(v, sm);
     V* part = reinterpret_cast<V*>(a.part_col);
-    if (!publish_partials<1>(v, part, &ctl->ticket[T_COL_STEP], sm, &last)) return;
+    if (threadIdx.x == 0) {
+        part[vb] = v[0];
+        __threadfence();
+        last = atomicAdd(&ctl->ticket[T_COL_STEP], 1u) == gridDim.x - 2;
+    }
+    __syncthreads();
+    if (!last) return;
     V t[1];
-    gather_all_partials<1>(t, part, gridDim.x, a.csc, sm);
+    gather_all_partials<1>(t, part, gridDim.x - 1, a.csc, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_STEP] = 0;
+    ctl->col_role = 0;
     ctl->dx2 = double(t[0]);
     ctl->apply = 0;
 }
