@@ -232,10 +232,18 @@ __device__ __forceinline__ T block_scalar(F f) {
     return s;
 }
 
-__device__ __forceinline__ int64_t ld_acquire_gpu(const int64_t* p) {
+__device__ __forceinline__ int64_t ld_relaxed_gpu(const int64_t* p) {
     int64_t v;
-    asm volatile("ld.acquire.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
     return v;
+}
+
+// A zero the compiler cannot see through: offsets a load's address by (v - w) so
+// that the load is issued only after v is known.
+__device__ __forceinline__ int64_t opaque_diff(int64_t v, int64_t w) {
+    int64_t z;
+    asm volatile("sub.s64 %0, %1, %2;" : "=l"(z) : "l"(v), "l"(w));
+    return z;
 }
 
 __device__ __forceinline__ void st_release_gpu(int64_t* p, int64_t v) {

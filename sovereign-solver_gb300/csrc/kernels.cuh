@@ -192,26 +192,44 @@ struct AdColStepEpi {
         return p;
     }
     // Wait (bounded) for the decision of the open attempt; returns 1 accepted, 0 rejected,
-    // -1 not applied (non-finite step, or the wait gave up)
+    // -1 not applied (non-finite step, or the wait gave up).  One lane of the calling
+    // lanes polls with relaxed L2 loads (an acquire load would also drop the SM's L1,
+    // where the gathered vector lives) and reads the decision with loads whose
+    // addresses depend on the value it saw (so they are issued after it: the decision
+    // block stores the values, fences, then releases the sequence number); the other
+    // lanes take them by shuffle.
     __device__ __forceinline__ int decide() {
-        verdict = -1;
         Ctl* ctl = a->ctl;
-        const int64_t pend = __ldcg(&ctl->pend_seq);
-        int polls = 0;
-        while (ld_acquire_gpu(&ctl->decided_seq) != pend) {
-            if (++polls > kDecisionPolls) {
+        const unsigned mask = __activemask();
+        const int leader = __ffs(mask) - 1;
+        int v = -1;
+        double t = 0.0, w = 0.0;
+        if ((int)(threadIdx.x & 31) == leader) {
+            const int64_t pend = __ldcg(&ctl->pend_seq);
+            int64_t seen = ld_relaxed_gpu(&ctl->decided_seq);
+            int polls = 0;
+            while (seen != pend && ++polls <= kDecisionPolls) {
+                __nanosleep(64);
+                seen = ld_relaxed_gpu(&ctl->decided_seq);
+            }
+            if (seen != pend) {
                 atomicExch(&ctl->wait_fail, 1);
                 ctl->status = SPS_STATUS_NUMERIC_ERROR;
                 ctl->done = 1;
-                return -1;
+            } else {
+                const int64_t z = opaque_diff(seen, pend);      // 0
+                if (__ldcg(&ctl->step_ok + z)) {
+                    t = __ldcg(&ctl->tau_next + z);
+                    w = __ldcg(&ctl->wgt_next + z);
+                    v = __ldcg(&ctl->accepted + z) != 0 ? 1 : 0;
+                }
             }
-            __nanosleep(64);
         }
-        if (!__ldcg(&ctl->step_ok)) return -1;
-        tau = V(__ldcg(&ctl->tau_next));
-        wgt = V(__ldcg(&ctl->wgt_next));
-        verdict = __ldcg(&ctl->accepted) != 0 ? 1 : 0;
-        return verdict;
+        v = __shfl_sync(mask, v, leader);
+        tau = V(__shfl_sync(mask, t, leader));
+        wgt = V(__shfl_sync(mask, w, leader));
+        verdict = v;
+        return v;
     }
     __device__ __forceinline__ void finish(int j, V atyj, const Pre& p, bool acc, V* xn) {
         if (acc) {
