@@ -262,8 +262,16 @@ __device__ __forceinline__ uint64_t global_ns() {
 //   e.pre(r)                  loads the row's own operands (issued before the
 //                             row's dot product, so they overlap its gathers)
 //   e(r, kind, acc[NV], pre)  consumes them; called once per row by one thread
+//   e.ready()                 (optional) called by the whole warp before its
+//                             epilogues of a unit: where a functor waits for
+//                             data another block publishes during the pass
 // and the gather functor g(q, j) returns vector q at column j (as Acc).
 // All control flow below is warp-uniform, so full-mask shuffles are safe.
+
+template <class E>
+__device__ __forceinline__ auto epi_ready(E& e, int) -> decltype(e.ready(), void()) { e.ready(); }
+template <class E>
+__device__ __forceinline__ void epi_ready(E&, long) {}
 
 #ifndef SPS_UNROLL
 #define SPS_UNROLL 8
@@ -339,6 +347,7 @@ __device__ __forceinline__ void visit_slice_pair(const Bin& b, int s0, int s1, c
                         for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
         }
     }
+    epi_ready(e, 0);
     if (r[0] < b.end) e(r[0], b.kind, acc[0], pre[0]);
     if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
 }
@@ -384,6 +393,7 @@ __device__ __forceinline__ void visit_slice_pair_fixed(const Bin& b, int s0, int
             for (int u = 0; u < LEN; ++u)
 #pragma unroll
                 for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
+    epi_ready(e, 0);
     if (r[0] < b.end) e(r[0], b.kind, acc[0], pre[0]);
     if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
 }
@@ -480,6 +490,7 @@ __device__ __forceinline__ void visit_warp_row_pair(const Bin& b, int u0, int u1
     const int s1 = __ldg(L.ptr + r1), t1 = has1 ? __ldg(L.ptr + r1 + 1) : s1;
     Acc acc[2][NV];
     warp_dot2<NV, Acc>(s0, t0, s1, t1, L, g, acc);
+    epi_ready(e, 0);
     if (lead) {
         e(r0, b.kind, acc[0], pre0);
         if (has1) e(r1, b.kind, acc[1], pre1);
@@ -501,6 +512,7 @@ __device__ __forceinline__ void visit_segment_pair(const Bin& b, int u0, int u1,
     const int k0 = __ldg(&L.unit[2 * gs0 + 1].x), k1 = __ldg(&L.unit[2 * gs1 + 1].x);
     Acc acc[2][NV];
     warp_dot2<NV, Acc>(a0.x, a0.y, a1.x, has1 ? a1.y : a1.x, L, g, acc);
+    epi_ready(e, 0);
     if ((threadIdx.x & 31) != 0) return;
     finish_segment<NV, Acc>(b, gs0, a0.z, k0, a0.w, acc[0], L, e);
     if (has1) finish_segment<NV, Acc>(b, gs1, a1.z, k1, a1.w, acc[1], L, e);

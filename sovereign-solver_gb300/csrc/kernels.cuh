@@ -160,18 +160,61 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
 // poll an L2 round trip plus a short sleep: well over 10 ms in all).
 constexpr int kDecisionPolls = 1 << 16;
 
+template <class V>
+struct StepDecision {
+    int verdict;        // 1 accepted, 0 rejected, -1 not applied (non-finite step, or the wait gave up)
+    V tau, wgt;
+};
+
+// The decision of the open attempt, for the whole calling warp.  Lane 0 waits
+// (bounded) for it, polling with relaxed L2 loads (an acquire load would also
+// drop the SM's L1, where the gathered vector lives), and reads it with loads
+// whose addresses depend on the sequence number it saw, so they are issued
+// after it (the decision block stores the values, fences, then releases the
+// number); the warp takes the result by shuffle.
+template <class V>
+__device__ __noinline__ StepDecision<V> wait_step_decision(Ctl* ctl) {
+    int v = -1;
+    V t = V(0), w = V(0);
+    if ((threadIdx.x & 31) == 0) {
+        const int64_t pend = __ldcg(&ctl->pend_seq);
+        int64_t seen = ld_relaxed_gpu(&ctl->decided_seq);
+        int polls = 0;
+        while (seen != pend && ++polls <= kDecisionPolls) {
+            __nanosleep(64);
+            seen = ld_relaxed_gpu(&ctl->decided_seq);
+        }
+        if (seen != pend) {
+            atomicExch(&ctl->wait_fail, 1);
+            ctl->status = SPS_STATUS_NUMERIC_ERROR;
+            ctl->done = 1;
+        } else {
+            const int64_t z = opaque_diff(seen, pend);      // 0
+            if (__ldcg(&ctl->step_ok + z)) {
+                t = V(__ldcg(&ctl->tau_next + z));
+                w = V(__ldcg(&ctl->wgt_next + z));
+                v = __ldcg(&ctl->accepted + z) != 0 ? 1 : 0;
+            }
+        }
+    }
+    StepDecision<V> d;
+    d.verdict = __shfl_sync(0xffffffffu, v, 0);
+    d.tau = __shfl_sync(0xffffffffu, t, 0);
+    d.wgt = __shfl_sync(0xffffffffu, w, 0);
+    return d;
+}
+
 // Column-pass epilogue.  The speculative operands (the state the attempt makes
-// current if accepted) are loaded with the gathers; the decision is read at the
-// first update of each thread.  With pc = cur when the attempt was opened, an
-// accepted attempt makes X[1 - pc] current, writes K^T y' to ATY[1 - pc] and the
-// next candidate to X[pc].
+// current if accepted) are loaded with the gathers; the warp reads the decision
+// in ready(), before the epilogues of its first unit.  With pc = cur when the
+// attempt was opened, an accepted attempt makes X[1 - pc] current, writes K^T y'
+// to ATY[1 - pc] and the next candidate to X[pc].
 template <class V>
 struct AdColStepEpi {
     const Args<V>* a;
-    const V* xspec;            // X[1 - pc]
-    V* xnext;                  // X[pc]
-    V* aty;                    // ATY[1 - pc]
-    int verdict = 2;           // 2 not read yet, 1 accepted, 0 rejected, -1 not applied
+    const V* xspec;             // X[1 - pc]
+    V *xnext, *aty;             // X[pc], ATY[1 - pc]
+    int verdict = 2;            // warp-uniform: 2 not read yet, 1 accepted, 0 rejected, -1 not applied
     V tau = V(0), wgt = V(0);
     V dx2 = V(0);
     struct Pre { V xj, cj, lo, hi, s, l; };
@@ -191,45 +234,14 @@ struct AdColStepEpi {
         }
         return p;
     }
-    // Wait (bounded) for the decision of the open attempt; returns 1 accepted, 0 rejected,
-    // -1 not applied (non-finite step, or the wait gave up).  One lane of the calling
-    // lanes polls with relaxed L2 loads (an acquire load would also drop the SM's L1,
-    // where the gathered vector lives) and reads the decision with loads whose
-    // addresses depend on the value it saw (so they are issued after it: the decision
-    // block stores the values, fences, then releases the sequence number); the other
-    // lanes take them by shuffle.
-    __device__ __forceinline__ int decide() {
-        Ctl* ctl = a->ctl;
-        const unsigned mask = __activemask();
-        const int leader = __ffs(mask) - 1;
-        int v = -1;
-        double t = 0.0, w = 0.0;
-        if ((int)(threadIdx.x & 31) == leader) {
-            const int64_t pend = __ldcg(&ctl->pend_seq);
-            int64_t seen = ld_relaxed_gpu(&ctl->decided_seq);
-            int polls = 0;
-            while (seen != pend && ++polls <= kDecisionPolls) {
-                __nanosleep(64);
-                seen = ld_relaxed_gpu(&ctl->decided_seq);
-            }
-            if (seen != pend) {
-                atomicExch(&ctl->wait_fail, 1);
-                ctl->status = SPS_STATUS_NUMERIC_ERROR;
-                ctl->done = 1;
-            } else {
-                const int64_t z = opaque_diff(seen, pend);      // 0
-                if (__ldcg(&ctl->step_ok + z)) {
-                    t = __ldcg(&ctl->tau_next + z);
-                    w = __ldcg(&ctl->wgt_next + z);
-                    v = __ldcg(&ctl->accepted + z) != 0 ? 1 : 0;
-                }
-            }
-        }
-        v = __shfl_sync(mask, v, leader);
-        tau = V(__shfl_sync(mask, t, leader));
-        wgt = V(__shfl_sync(mask, w, leader));
-        verdict = v;
-        return v;
+    // Called by the whole warp (the wait itself is out of line: it runs once per warp,
+    // and inlined at every traversal's epilogue it cost the pass registers).
+    __device__ __forceinline__ void ready() {
+        if (verdict != 2) return;
+        const StepDecision<V> d = wait_step_decision<V>(a->ctl);
+        verdict = d.verdict;
+        tau = d.tau;
+        wgt = d.wgt;
     }
     __device__ __forceinline__ void finish(int j, V atyj, const Pre& p, bool acc, V* xn) {
         if (acc) {
@@ -245,8 +257,8 @@ struct AdColStepEpi {
     // accepted: the gathered K^T y' and the speculative point; otherwise nothing here (a
     // rejected attempt's columns are redone from the kept state after the block's sweep)
     __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) {
-        if (verdict == 2) decide();
         if (verdict == 1) finish(j, acc[0], p, true, xnext);
+        else if (verdict == 2) atomicExch(&a->ctl->wait_fail, 1);   // a traversal without ready(): a bug
     }
 };
 
@@ -285,9 +297,9 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     const int colblocks = a.cols.total_blocks;
     if (vb < colblocks) {
         visit_bins<1, V>(a.cols, vb, a.csc, GatherOne<V>{a.Y[1 - pc]}, e);
-        // a thread that updated no column reads the decision here; rejected: the new
+        // a warp that updated no column reads the decision here; rejected: the new
         // candidate from the kept state X[pc] and its K^T y, ATY[pc]
-        if (e.verdict == 2) e.decide();
+        e.ready();
         if (e.verdict == 0) {
             const V* xk = a.X[pc];
             const V* atyk = a.ATY[pc];
@@ -301,7 +313,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
                 e.finish(j, atyk[j], p, false, xn);
             }
         }
-    } else if (e.decide() == 1) {
+    } else if (e.ready(), e.verdict == 1) {
         const V* yc = a.Y[1 - pc];
         for (int i = (vb - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
             a.ys[i] += e.wgt * (yc[i] - a.yl[i]);
