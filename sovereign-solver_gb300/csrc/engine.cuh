@@ -131,16 +131,26 @@ struct Ctl {
     int32_t warm_used;       // batched solver: the instance started from its warm start
     double rel_kkt_lagr;     // the returned point's error in the Lagrangian form (= rel_kkt unless
                              // the single-LP engine measures the PDLP form)
-    // adaptive single-LP step hand-off: the row pass opens an attempt (pend_seq, the state
-    // index it read), the column pass's first block decides it and publishes decided_seq
-    int64_t pend_seq;        // sequence number of the attempt the last row pass opened
-    int64_t decided_seq;     // sequence number of the last decided attempt
-    double tau_next;         // eta / omega after the decision (the primal step of the column pass)
-    double wgt_next;         // eta_used after the decision (the averaging weight)
-    int32_t pend_cur;        // cur when the attempt was opened
-    int32_t step_ok;         // the decided attempt is applied (0 after a non-finite step)
-    int32_t wait_fail;       // a block of the column pass gave up waiting for the decision
-    uint32_t col_role;       // arrival counter of the column pass's blocks (block roles)
+    int32_t wait_fail;       // a block of the adaptive column pass gave up waiting for the step decision
+};
+
+// Step hand-off between the adaptive single-LP row and column passes.  The row
+// pass opens an attempt (pend_seq, and the state index it read); the column
+// pass's first block decides it and publishes the decision, then the sequence
+// number in kSeqCopies copies, one per 128-byte line: each block of the column
+// pass polls the copy of its role, so the polls spread over L2 slices instead
+// of queueing on one line.  The role counter's atomics have a line of their own.
+constexpr int kSeqCopies = 16;
+struct StepHandoff {
+    struct alignas(128) Seq { int64_t v; };
+    Seq decided[kSeqCopies];         // sequence number of the last decided attempt (copies)
+    alignas(128) int64_t pend_seq;   // sequence number of the attempt the last row pass opened
+    double tau_next;                 // eta / omega after the decision (the column pass's primal step)
+    double wgt_next;                 // eta_used after the decision (the averaging weight)
+    int32_t pend_cur;                // cur when the attempt was opened
+    int32_t accepted;                // the decided attempt was accepted
+    int32_t step_ok;                 // the decided attempt is applied (0 after a non-finite step)
+    alignas(128) uint32_t col_role;  // arrival counter of the column pass's blocks (block roles)
 };
 
 enum TicketSlot { T_ROW_STEP = 0, T_COL_STEP, T_ROW_CHECK, T_COL_CHECK, T_APPLY, T_AUX0, T_AUX1, T_AUX2 };

@@ -49,6 +49,7 @@ struct Args {
     double* px[2]; double* py[2];   // adaptive: the check's two points (average, current) in FP64
     double* part_row; double* part_col; double* part_aux;
     Ctl* ctl;
+    StepHandoff* ho;               // adaptive step hand-off (row pass -> column pass)
     const volatile int32_t* abort_flag;
     cudaGraphConditionalHandle cond;
     int32_t has_cond;
@@ -140,8 +141,8 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     const int cur = ctl->cur;
     const V sigma = block_scalar<V>([&] { return ctl->eta * ctl->omega; });
     if (blockIdx.x == 0 && threadIdx.x == 0) {      // open the attempt (no block of this pass reads these)
-        ctl->pend_seq = ctl->decided_seq + 1;
-        ctl->pend_cur = cur;
+        a.ho->pend_seq = a.ho->decided[0].v + 1;
+        a.ho->pend_cur = cur;
         ctl->apply = AP_STEP_PENDING;
     }
     AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], sigma};
@@ -166,34 +167,69 @@ struct StepDecision {
     V tau, wgt;
 };
 
-// The decision of the open attempt, for the whole calling warp.  Lane 0 waits
-// (bounded) for it, polling with relaxed L2 loads (an acquire load would also
-// drop the SM's L1, where the gathered vector lives), and reads it with loads
-// whose addresses depend on the sequence number it saw, so they are issued
-// after it (the decision block stores the values, fences, then releases the
-// number); the warp takes the result by shuffle.
+// The column pass's dynamic shared memory: the block's copy of the decision.
 template <class V>
-__device__ __noinline__ StepDecision<V> wait_step_decision(Ctl* ctl) {
+struct BlockDecision {
+    int state;          // 0 nobody waiting yet, 1 one warp polling for the block, 2 ready
+    int verdict;
+    V tau, wgt;
+};
+
+// The decision of the open attempt, for the whole calling warp.  The first warp
+// of the block to get here polls for the block (lane 0, relaxed L2 loads of the
+// block's copy of the sequence number, backing off to 256 ns; an acquire load
+// would also drop the SM's L1, where the gathered vector lives), reads the
+// decision with loads whose addresses depend on the number it saw (so they are
+// issued after it: the decision block stores the values, fences, then the
+// numbers) and leaves it in shared memory; later warps read it there.  Every
+// wait is bounded.
+template <class V>
+__device__ __noinline__ StepDecision<V> wait_step_decision(const StepHandoff* ho, Ctl* ctl, int role) {
+    extern __shared__ __align__(16) unsigned char step_smem[];
+    BlockDecision<V>* bd = reinterpret_cast<BlockDecision<V>*>(step_smem);
+    volatile BlockDecision<V>* vbd = bd;
     int v = -1;
     V t = V(0), w = V(0);
     if ((threadIdx.x & 31) == 0) {
-        const int64_t pend = __ldcg(&ctl->pend_seq);
-        int64_t seen = ld_relaxed_gpu(&ctl->decided_seq);
-        int polls = 0;
-        while (seen != pend && ++polls <= kDecisionPolls) {
-            __nanosleep(64);
-            seen = ld_relaxed_gpu(&ctl->decided_seq);
-        }
-        if (seen != pend) {
-            atomicExch(&ctl->wait_fail, 1);
-            ctl->status = SPS_STATUS_NUMERIC_ERROR;
-            ctl->done = 1;
+        if (atomicCAS(&bd->state, 0, 1) == 0) {
+            const int64_t pend = __ldcg(&ho->pend_seq);
+            const int64_t* seq = &ho->decided[role % kSeqCopies].v;
+            int64_t seen = ld_relaxed_gpu(seq);
+            int polls = 0;
+            unsigned ns = 32;
+            while (seen != pend && ++polls <= kDecisionPolls) {
+                __nanosleep(ns);
+                ns = ns < 256 ? 2 * ns : 256;
+                seen = ld_relaxed_gpu(seq);
+            }
+            if (seen == pend) {
+                const int64_t z = opaque_diff(seen, pend);      // 0
+                if (__ldcg(&ho->step_ok + z)) {
+                    t = V(__ldcg(&ho->tau_next + z));
+                    w = V(__ldcg(&ho->wgt_next + z));
+                    v = __ldcg(&ho->accepted + z) != 0 ? 1 : 0;
+                }
+            } else {
+                atomicExch(&ctl->wait_fail, 1);
+                ctl->status = SPS_STATUS_NUMERIC_ERROR;
+                ctl->done = 1;
+            }
+            vbd->verdict = v;
+            vbd->tau = t;
+            vbd->wgt = w;
+            __threadfence_block();
+            vbd->state = 2;
         } else {
-            const int64_t z = opaque_diff(seen, pend);      // 0
-            if (__ldcg(&ctl->step_ok + z)) {
-                t = V(__ldcg(&ctl->tau_next + z));
-                w = V(__ldcg(&ctl->wgt_next + z));
-                v = __ldcg(&ctl->accepted + z) != 0 ? 1 : 0;
+            int spins = 0;
+            while (vbd->state != 2 && ++spins <= 4 * kDecisionPolls) __nanosleep(32);
+            __threadfence_block();
+            if (vbd->state == 2) {
+                v = vbd->verdict;
+                t = vbd->tau;
+                w = vbd->wgt;
+            } else {
+                atomicExch(&ctl->wait_fail, 1);
+                ctl->done = 1;
             }
         }
     }
@@ -214,6 +250,7 @@ struct AdColStepEpi {
     const Args<V>* a;
     const V* xspec;             // X[1 - pc]
     V *xnext, *aty;             // X[pc], ATY[1 - pc]
+    int role;
     int verdict = 2;            // warp-uniform: 2 not read yet, 1 accepted, 0 rejected, -1 not applied
     V tau = V(0), wgt = V(0);
     V dx2 = V(0);
@@ -238,7 +275,7 @@ struct AdColStepEpi {
     // and inlined at every traversal's epilogue it cost the pass registers).
     __device__ __forceinline__ void ready() {
         if (verdict != 2) return;
-        const StepDecision<V> d = wait_step_decision<V>(a->ctl);
+        const StepDecision<V> d = wait_step_decision<V>(a->ho, a->ctl, role);
         verdict = d.verdict;
         tau = d.tau;
         wgt = d.wgt;
@@ -275,7 +312,12 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     __shared__ V sm[kWarps * 2];
     __shared__ bool last;
     __shared__ uint32_t role_s;
-    if (threadIdx.x == 0) role_s = atomicAdd(&ctl->col_role, 1u);
+    StepHandoff* ho = a.ho;
+    if (threadIdx.x == 0) {
+        role_s = atomicAdd(&ho->col_role, 1u);
+        extern __shared__ __align__(16) unsigned char step_smem[];
+        reinterpret_cast<BlockDecision<V>*>(step_smem)->state = 0;
+    }
     __syncthreads();
     const int role = (int)role_s;
     if (role == 0) {
@@ -283,17 +325,20 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
         gather_all_partials<2>(t, reinterpret_cast<const V*>(a.part_row), a.rows.total_blocks, a.csr, sm);
         if (threadIdx.x == 0) {
             const bool ok = decide_step(*ctl, double(t[0]), double(t[1]));
-            ctl->step_ok = ok;
-            ctl->tau_next = ctl->eta / ctl->omega;
-            ctl->wgt_next = ctl->eta_used;
+            ho->step_ok = ok;
+            ho->accepted = ctl->accepted;
+            ho->tau_next = ctl->eta / ctl->omega;
+            ho->wgt_next = ctl->eta_used;
+            const int64_t seq = ho->pend_seq;
             __threadfence();
-            st_release_gpu(&ctl->decided_seq, ctl->pend_seq);
+#pragma unroll
+            for (int k = 0; k < kSeqCopies; ++k) st_release_gpu(&ho->decided[k].v, seq);
         }
         return;
     }
     const int vb = role - 1;
-    const int pc = ctl->pend_cur;
-    AdColStepEpi<V> e{&a, a.X[1 - pc], a.X[pc], a.ATY[1 - pc]};
+    const int pc = ho->pend_cur;
+    AdColStepEpi<V> e{&a, a.X[1 - pc], a.X[pc], a.ATY[1 - pc], role};
     const int colblocks = a.cols.total_blocks;
     if (vb < colblocks) {
         visit_bins<1, V>(a.cols, vb, a.csc, GatherOne<V>{a.Y[1 - pc]}, e);
@@ -332,7 +377,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     gather_all_partials<1>(t, part, gridDim.x - 1, a.csc, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_STEP] = 0;
-    ctl->col_role = 0;
+    ho->col_role = 0;
     ctl->dx2 = double(t[0]);
     ctl->apply = 0;
 }
