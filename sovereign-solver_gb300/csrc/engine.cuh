@@ -256,8 +256,8 @@ __device__ __forceinline__ int64_t opaque_diff(int64_t v, int64_t w) {
     return z;
 }
 
-__device__ __forceinline__ void st_release_gpu(int64_t* p, int64_t v) {
-    asm volatile("st.release.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+__device__ __forceinline__ void st_relaxed_gpu(int64_t* p, int64_t v) {
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 __device__ __forceinline__ uint64_t global_ns() {

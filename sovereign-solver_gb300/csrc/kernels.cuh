@@ -330,9 +330,9 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
             ho->tau_next = ctl->eta / ctl->omega;
             ho->wgt_next = ctl->eta_used;
             const int64_t seq = ho->pend_seq;
-            __threadfence();
+            __threadfence();             // one fence orders the decision before every copy
 #pragma unroll
-            for (int k = 0; k < kSeqCopies; ++k) st_release_gpu(&ho->decided[k].v, seq);
+            for (int k = 0; k < kSeqCopies; ++k) st_relaxed_gpu(&ho->decided[k].v, seq);
         }
         return;
     }
