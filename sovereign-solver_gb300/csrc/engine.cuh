@@ -131,26 +131,6 @@ struct Ctl {
     int32_t warm_used;       // batched solver: the instance started from its warm start
     double rel_kkt_lagr;     // the returned point's error in the Lagrangian form (= rel_kkt unless
                              // the single-LP engine measures the PDLP form)
-    int32_t wait_fail;       // a block of the adaptive column pass gave up waiting for the step decision
-};
-
-// Step hand-off between the adaptive single-LP row and column passes.  The row
-// pass opens an attempt (pend_seq, and the state index it read); the column
-// pass's first block decides it and publishes the decision, then the sequence
-// number in kSeqCopies copies, one per 128-byte line: each block of the column
-// pass polls the copy of its role, so the polls spread over L2 slices instead
-// of queueing on one line.  The role counter's atomics have a line of their own.
-constexpr int kSeqCopies = 16;
-struct StepHandoff {
-    struct alignas(128) Seq { int64_t v; };
-    Seq decided[kSeqCopies];         // sequence number of the last decided attempt (copies)
-    alignas(128) int64_t pend_seq;   // sequence number of the attempt the last row pass opened
-    double tau_next;                 // eta / omega after the decision (the column pass's primal step)
-    double wgt_next;                 // eta_used after the decision (the averaging weight)
-    int32_t pend_cur;                // cur when the attempt was opened
-    int32_t accepted;                // the decided attempt was accepted
-    int32_t step_ok;                 // the decided attempt is applied (0 after a non-finite step)
-    alignas(128) uint32_t col_role;  // arrival counter of the column pass's blocks (block roles)
 };
 
 enum TicketSlot { T_ROW_STEP = 0, T_COL_STEP, T_ROW_CHECK, T_COL_CHECK, T_APPLY, T_AUX0, T_AUX1, T_AUX2 };
@@ -242,24 +222,6 @@ __device__ __forceinline__ T block_scalar(F f) {
     return s;
 }
 
-__device__ __forceinline__ int64_t ld_relaxed_gpu(const int64_t* p) {
-    int64_t v;
-    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-// A zero the compiler cannot see through: offsets a load's address by (v - w) so
-// that the load is issued only after v is known.
-__device__ __forceinline__ int64_t opaque_diff(int64_t v, int64_t w) {
-    int64_t z;
-    asm volatile("sub.s64 %0, %1, %2;" : "=l"(z) : "l"(v), "l"(w));
-    return z;
-}
-
-__device__ __forceinline__ void st_relaxed_gpu(int64_t* p, int64_t v) {
-    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
-}
-
 __device__ __forceinline__ uint64_t global_ns() {
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
@@ -272,16 +234,8 @@ __device__ __forceinline__ uint64_t global_ns() {
 //   e.pre(r)                  loads the row's own operands (issued before the
 //                             row's dot product, so they overlap its gathers)
 //   e(r, kind, acc[NV], pre)  consumes them; called once per row by one thread
-//   e.ready()                 (optional) called by the whole warp before its
-//                             epilogues of a unit: where a functor waits for
-//                             data another block publishes during the pass
 // and the gather functor g(q, j) returns vector q at column j (as Acc).
 // All control flow below is warp-uniform, so full-mask shuffles are safe.
-
-template <class E>
-__device__ __forceinline__ auto epi_ready(E& e, int) -> decltype(e.ready(), void()) { e.ready(); }
-template <class E>
-__device__ __forceinline__ void epi_ready(E&, long) {}
 
 #ifndef SPS_UNROLL
 #define SPS_UNROLL 8
@@ -357,7 +311,6 @@ __device__ __forceinline__ void visit_slice_pair(const Bin& b, int s0, int s1, c
                         for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
         }
     }
-    epi_ready(e, 0);
     if (r[0] < b.end) e(r[0], b.kind, acc[0], pre[0]);
     if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
 }
@@ -403,7 +356,6 @@ __device__ __forceinline__ void visit_slice_pair_fixed(const Bin& b, int s0, int
             for (int u = 0; u < LEN; ++u)
 #pragma unroll
                 for (int q = 0; q < NV; ++q) acc[h][q] += a[h][u] * g(q, j[h][u]);
-    epi_ready(e, 0);
     if (r[0] < b.end) e(r[0], b.kind, acc[0], pre[0]);
     if (has1 && r[1] < b.end) e(r[1], b.kind, acc[1], pre[1]);
 }
@@ -500,7 +452,6 @@ __device__ __forceinline__ void visit_warp_row_pair(const Bin& b, int u0, int u1
     const int s1 = __ldg(L.ptr + r1), t1 = has1 ? __ldg(L.ptr + r1 + 1) : s1;
     Acc acc[2][NV];
     warp_dot2<NV, Acc>(s0, t0, s1, t1, L, g, acc);
-    epi_ready(e, 0);
     if (lead) {
         e(r0, b.kind, acc[0], pre0);
         if (has1) e(r1, b.kind, acc[1], pre1);
@@ -522,7 +473,6 @@ __device__ __forceinline__ void visit_segment_pair(const Bin& b, int u0, int u1,
     const int k0 = __ldg(&L.unit[2 * gs0 + 1].x), k1 = __ldg(&L.unit[2 * gs1 + 1].x);
     Acc acc[2][NV];
     warp_dot2<NV, Acc>(a0.x, a0.y, a1.x, has1 ? a1.y : a1.x, L, g, acc);
-    epi_ready(e, 0);
     if ((threadIdx.x & 31) != 0) return;
     finish_segment<NV, Acc>(b, gs0, a0.z, k0, a0.w, acc[0], L, e);
     if (has1) finish_segment<NV, Acc>(b, gs1, a1.z, k1, a1.w, acc[1], L, e);

@@ -95,7 +95,6 @@ struct Engine : EngineBase {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evq = nullptr;
     char* arena = nullptr;
     Ctl* d_ctl = nullptr;
-    StepHandoff* d_handoff = nullptr;   // adaptive step hand-off (sequence numbers only grow: set once)
     Ctl* h_ctl = nullptr;               // pinned read-back
     int32_t* h_abort = nullptr;         // mapped host flag
     int32_t* d_abort = nullptr;
@@ -705,7 +704,6 @@ struct Engine : EngineBase {
             add(&d_sigma, sizeof(V) * m);
         }
         add(&d_ctl, sizeof(Ctl));
-        if (adaptive) add(&d_handoff, sizeof(StepHandoff));
         add(&d_xout, sizeof(double) * n);
         add(&d_yout, sizeof(double) * m);
         if (adaptive) {
@@ -924,7 +922,6 @@ struct Engine : EngineBase {
         a.py[0] = d_py; a.py[1] = d_py ? d_py + m : nullptr;
         a.part_row = d_pr; a.part_col = d_pc; a.part_aux = d_pa;
         a.ctl = d_ctl;
-        a.ho = d_handoff;
         a.abort_flag = d_abort;
         a.has_cond = 0;
         a.check_interval = opt.check_interval > 0 ? opt.check_interval : (adaptive ? 64 : 50);
@@ -933,7 +930,6 @@ struct Engine : EngineBase {
         padded_nnz_rows = rp.total;
         padded_nnz_cols = cp.total;
         SPS_CK(cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st));
-        if (d_handoff) SPS_CK(cudaMemsetAsync(d_handoff, 0, sizeof(StepHandoff), st));
         SPS_CK(cudaEventRecord(ev1, st));
         SPS_CK(cudaStreamSynchronize(st));
         float ms = 0;
@@ -959,7 +955,7 @@ struct Engine : EngineBase {
         if (mode == SPS_MODE_ADAPTIVE) {
             for (int w = 0; w < W; ++w) {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                ad_col_step<V><<<1 + gc + a.col_tail_blocks, kBlock, sizeof(BlockDecision<V>), st>>>(a);   // + the decision block
+                ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
             }
             ad_check_prep<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
             ad_row_check<V><<<a.rows_chk.total_blocks, kBlock, 0, st>>>(a);
@@ -1148,8 +1144,6 @@ struct Engine : EngineBase {
         if (rc) return rc;
         SPS_CK(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
         SPS_CK(cudaStreamSynchronize(st));
-        if (h_ctl->wait_fail)
-            return fail(SPS_ERR_CUDA, "internal error: a column-pass block stopped waiting for the step decision");
         int status = h_ctl->status;
         if (!h_ctl->done) status = SPS_STATUS_ITERATION_LIMIT;
         if (!adaptive && status != SPS_STATUS_OPTIMAL) {
@@ -1304,7 +1298,7 @@ struct Engine : EngineBase {
                 for (int r = 0; r < reps; ++r) {
                     if (mode == SPS_MODE_ADAPTIVE) {
                         ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                        if (variant == 0) ad_col_step<V><<<1 + gc + a.col_tail_blocks, kBlock, sizeof(BlockDecision<V>), st>>>(a);   // + the decision block
+                        if (variant == 0) ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
                     } else {
                         rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
                         if (variant == 0) rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
@@ -1344,7 +1338,7 @@ struct Engine : EngineBase {
             if (mode == SPS_MODE_ADAPTIVE) {
                 ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
                 SPS_CK(cudaEventRecord(ev[2 * r + 1], st));
-                ad_col_step<V><<<1 + gc + a.col_tail_blocks, kBlock, sizeof(BlockDecision<V>), st>>>(a);   // + the decision block
+                ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
             } else {
                 rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
                 SPS_CK(cudaEventRecord(ev[2 * r + 1], st));

@@ -49,7 +49,6 @@ struct Args {
     double* px[2]; double* py[2];   // adaptive: the check's two points (average, current) in FP64
     double* part_row; double* part_col; double* part_aux;
     Ctl* ctl;
-    StepHandoff* ho;               // adaptive step hand-off (row pass -> column pass)
     const volatile int32_t* abort_flag;
     cudaGraphConditionalHandle cond;
     int32_t has_cond;
@@ -128,131 +127,35 @@ struct AdRowStepEpi {
     }
 };
 
-// The row pass ends without a serial tail: each block writes its partials of
-// ||dy||^2 and dy^T K dx, and the step decision they feed is taken by the first
-// block to reach the column pass, while the other blocks of that pass run
-// their K^T y' gathers (speculatively: y' is the new dual if the attempt is
-// accepted, as nearly all are) and wait for it only at their first update.
 template <class V>
 SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
     __shared__ V sm[kWarps * 2];
+    __shared__ bool last;
     const int cur = ctl->cur;
     const V sigma = block_scalar<V>([&] { return ctl->eta * ctl->omega; });
-    if (blockIdx.x == 0 && threadIdx.x == 0) {      // open the attempt (no block of this pass reads these)
-        a.ho->pend_seq = a.ho->decided[0].v + 1;
-        a.ho->pend_cur = cur;
-        ctl->apply = AP_STEP_PENDING;
-    }
     AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], sigma};
     visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e);
     // reductions in V: FP32 sums in the FP32 engine (the step rule's inputs)
     V v[2] = {e.dy2, e.inter};
-    block_sum<2>(v, sm);
-    if (threadIdx.x == 0) {
-        V* part = reinterpret_cast<V*>(a.part_row);
-        part[(size_t)blockIdx.x * 2] = v[0];
-        part[(size_t)blockIdx.x * 2 + 1] = v[1];
-    }
+    V* part = reinterpret_cast<V*>(a.part_row);
+    if (!publish_partials<2>(v, part, &ctl->ticket[T_ROW_STEP], sm, &last)) return;
+    V t[2];
+    gather_all_partials<2>(t, part, gridDim.x, a.csr, sm);
+    if (threadIdx.x != 0) return;
+    ctl->ticket[T_ROW_STEP] = 0;
+    decide_step(*ctl, double(t[0]), double(t[1]));
 }
 
-// Polls of the step decision before a block of the column pass gives up (each
-// poll an L2 round trip plus a short sleep: well over 10 ms in all).
-constexpr int kDecisionPolls = 1 << 16;
-
-template <class V>
-struct StepDecision {
-    int verdict;        // 1 accepted, 0 rejected, -1 not applied (non-finite step, or the wait gave up)
-    V tau, wgt;
-};
-
-// The column pass's dynamic shared memory: the block's copy of the decision.
-template <class V>
-struct BlockDecision {
-    int state;          // 0 nobody waiting yet, 1 one warp polling for the block, 2 ready
-    int verdict;
-    V tau, wgt;
-};
-
-// The decision of the open attempt, for the whole calling warp.  The first warp
-// of the block to get here polls for the block (lane 0, relaxed L2 loads of the
-// block's copy of the sequence number, backing off to 256 ns; an acquire load
-// would also drop the SM's L1, where the gathered vector lives), reads the
-// decision with loads whose addresses depend on the number it saw (so they are
-// issued after it: the decision block stores the values, fences, then the
-// numbers) and leaves it in shared memory; later warps read it there.  Every
-// wait is bounded.
-template <class V>
-__device__ __noinline__ StepDecision<V> wait_step_decision(const StepHandoff* ho, Ctl* ctl, int role) {
-    extern __shared__ __align__(16) unsigned char step_smem[];
-    BlockDecision<V>* bd = reinterpret_cast<BlockDecision<V>*>(step_smem);
-    volatile BlockDecision<V>* vbd = bd;
-    int v = -1;
-    V t = V(0), w = V(0);
-    if ((threadIdx.x & 31) == 0) {
-        if (atomicCAS(&bd->state, 0, 1) == 0) {
-            const int64_t pend = __ldcg(&ho->pend_seq);
-            const int64_t* seq = &ho->decided[role % kSeqCopies].v;
-            int64_t seen = ld_relaxed_gpu(seq);
-            int polls = 0;
-            unsigned ns = 32;
-            while (seen != pend && ++polls <= kDecisionPolls) {
-                __nanosleep(ns);
-                ns = ns < 256 ? 2 * ns : 256;
-                seen = ld_relaxed_gpu(seq);
-            }
-            if (seen == pend) {
-                const int64_t z = opaque_diff(seen, pend);      // 0
-                if (__ldcg(&ho->step_ok + z)) {
-                    t = V(__ldcg(&ho->tau_next + z));
-                    w = V(__ldcg(&ho->wgt_next + z));
-                    v = __ldcg(&ho->accepted + z) != 0 ? 1 : 0;
-                }
-            } else {
-                atomicExch(&ctl->wait_fail, 1);
-                ctl->status = SPS_STATUS_NUMERIC_ERROR;
-                ctl->done = 1;
-            }
-            vbd->verdict = v;
-            vbd->tau = t;
-            vbd->wgt = w;
-            __threadfence_block();
-            vbd->state = 2;
-        } else {
-            int spins = 0;
-            while (vbd->state != 2 && ++spins <= 4 * kDecisionPolls) __nanosleep(32);
-            __threadfence_block();
-            if (vbd->state == 2) {
-                v = vbd->verdict;
-                t = vbd->tau;
-                w = vbd->wgt;
-            } else {
-                atomicExch(&ctl->wait_fail, 1);
-                ctl->done = 1;
-            }
-        }
-    }
-    StepDecision<V> d;
-    d.verdict = __shfl_sync(0xffffffffu, v, 0);
-    d.tau = __shfl_sync(0xffffffffu, t, 0);
-    d.wgt = __shfl_sync(0xffffffffu, w, 0);
-    return d;
-}
-
-// Column-pass epilogue.  The speculative operands (the state the attempt makes
-// current if accepted) are loaded with the gathers; the warp reads the decision
-// in ready(), before the epilogues of its first unit.  With pc = cur when the
-// attempt was opened, an accepted attempt makes X[1 - pc] current, writes K^T y'
-// to ATY[1 - pc] and the next candidate to X[pc].
 template <class V>
 struct AdColStepEpi {
     const Args<V>* a;
-    const V* xspec;             // X[1 - pc]
-    V *xnext, *aty;             // X[pc], ATY[1 - pc]
-    int role;
-    int verdict = 2;            // warp-uniform: 2 not read yet, 1 accepted, 0 rejected, -1 not applied
-    V tau = V(0), wgt = V(0);
+    const V *xc, *cc, *atyo;
+    const V* xl;
+    V *aty, *xn, *xs;
+    V tau, wgt;
+    bool accepted;
     V dx2 = V(0);
     struct Pre { V xj, cj, lo, hi, s, l; };
     static constexpr int NP = 1;
@@ -261,123 +164,55 @@ struct AdColStepEpi {
     __device__ __forceinline__ void export_to(R* d) const { d[0] = dx2; }
     __device__ __forceinline__ Pre pre(int j) const {
         Pre p;
-        p.xj = xspec[j];
-        p.cj = a->c[j];
+        p.xj = xc[j];
+        p.cj = cc[j];
         p.lo = lo_at(*a, j);
         p.hi = hi_at(*a, j);
-        if constexpr (sizeof(V) == 4) {   // (the FP64 engine loads them at the update: registers)
-            p.s = a->xs[j];
-            p.l = a->xl[j];
-        }
+        p.s = accepted ? xs[j] : V(0);
+        p.l = accepted ? xl[j] : V(0);
         return p;
     }
-    // Called by the whole warp (the wait itself is out of line: it runs once per warp,
-    // and inlined at every traversal's epilogue it cost the pass registers).
-    __device__ __forceinline__ void ready() {
-        if (verdict != 2) return;
-        const StepDecision<V> d = wait_step_decision<V>(a->ho, a->ctl, role);
-        verdict = d.verdict;
-        tau = d.tau;
-        wgt = d.wgt;
-    }
-    __device__ __forceinline__ void finish(int j, V atyj, const Pre& p, bool acc, V* xn) {
-        if (acc) {
-            aty[j] = atyj;
-            if constexpr (sizeof(V) == 4) a->xs[j] = p.s + wgt * (p.xj - p.l);
-            else a->xs[j] = a->xs[j] + wgt * (p.xj - a->xl[j]);
-        }
+    __device__ __forceinline__ void finish(int j, V atyj, const Pre& p) {
+        if (accepted) { aty[j] = atyj; xs[j] = p.s + wgt * (p.xj - p.l); }
         const V x2 = clampv(p.xj - tau * (p.cj - atyj), p.lo, p.hi);
         xn[j] = x2;
         const V d = x2 - p.xj;
         dx2 += d * d;
     }
-    // accepted: the gathered K^T y' and the speculative point; otherwise nothing here (a
-    // rejected attempt's columns are redone from the kept state after the block's sweep)
-    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) {
-        if (verdict == 1) finish(j, acc[0], p, true, xnext);
-        else if (verdict == 2) atomicExch(&a->ctl->wait_fail, 1);   // a traversal without ready(): a bug
-    }
+    __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) { finish(j, acc[0], p); }
 };
 
-// Blocks take roles in arrival order: role 0 takes the step decision (the row
-// pass's partials, then decide_step) and publishes it; roles 1 .. colblocks
-// sweep the column bins (virtual block role - 1); the rest update the dual
-// average.  The first block to arrive is running by definition, so the waits of
-// the others on its decision always end.  Partials and the last-block ticket use
-// role - 1, the grouping of a launch without the decision block.
 template <class V>
 SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     Ctl* ctl = a.ctl;
     if (ctl->apply != AP_STEP_PENDING) return;
-    __shared__ V sm[kWarps * 2];
+    __shared__ V sm[kWarps];
     __shared__ bool last;
-    __shared__ uint32_t role_s;
-    StepHandoff* ho = a.ho;
-    if (threadIdx.x == 0) {
-        role_s = atomicAdd(&ho->col_role, 1u);
-        extern __shared__ __align__(16) unsigned char step_smem[];
-        reinterpret_cast<BlockDecision<V>*>(step_smem)->state = 0;
-    }
-    __syncthreads();
-    const int role = (int)role_s;
-    if (role == 0) {
-        V t[2];
-        gather_all_partials<2>(t, reinterpret_cast<const V*>(a.part_row), a.rows.total_blocks, a.csr, sm);
-        if (threadIdx.x == 0) {
-            const bool ok = decide_step(*ctl, double(t[0]), double(t[1]));
-            ho->step_ok = ok;
-            ho->accepted = ctl->accepted;
-            ho->tau_next = ctl->eta / ctl->omega;
-            ho->wgt_next = ctl->eta_used;
-            const int64_t seq = ho->pend_seq;
-            __threadfence();             // one fence orders the decision before every copy
-#pragma unroll
-            for (int k = 0; k < kSeqCopies; ++k) st_relaxed_gpu(&ho->decided[k].v, seq);
-        }
-        return;
-    }
-    const int vb = role - 1;
-    const int pc = ho->pend_cur;
-    AdColStepEpi<V> e{&a, a.X[1 - pc], a.X[pc], a.ATY[1 - pc], role};
+    const int cur = ctl->cur;
+    const bool acc = ctl->accepted;
+    const V tau = block_scalar<V>([&] { return ctl->eta / ctl->omega; });
+    const V wgt = block_scalar<V>([&] { return ctl->eta_used; });
+    AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.xl, a.ATY[cur], a.X[1 - cur], a.xs, tau, wgt, acc};
     const int colblocks = a.cols.total_blocks;
-    if (vb < colblocks) {
-        visit_bins<1, V>(a.cols, vb, a.csc, GatherOne<V>{a.Y[1 - pc]}, e);
-        // a warp that updated no column reads the decision here; rejected: the new
-        // candidate from the kept state X[pc] and its K^T y, ATY[pc]
-        e.ready();
-        if (e.verdict == 0) {
-            const V* xk = a.X[pc];
-            const V* atyk = a.ATY[pc];
-            V* xn = a.X[1 - pc];
-            for (int j = vb * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock) {
-                typename AdColStepEpi<V>::Pre p;
-                p.xj = xk[j];
-                p.cj = a.c[j];
-                p.lo = lo_at(a, j);
-                p.hi = hi_at(a, j);
-                e.finish(j, atyk[j], p, false, xn);
-            }
+    if ((int)blockIdx.x < colblocks) {
+        if (acc) {
+            visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[cur]}, e);
+        } else {
+            for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock)
+                e.finish(j, e.atyo[j], e.pre(j));
         }
-    } else if (e.ready(), e.verdict == 1) {
-        const V* yc = a.Y[1 - pc];
-        for (int i = (vb - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
-            a.ys[i] += e.wgt * (yc[i] - a.yl[i]);
+    } else if (acc) {
+        const V* yc = a.Y[cur];
+        for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
+            a.ys[i] += wgt * (yc[i] - a.yl[i]);
     }
     V v[1] = {e.dx2};
-    block_sum<1>(v, sm);
     V* part = reinterpret_cast<V*>(a.part_col);
-    if (threadIdx.x == 0) {
-        part[vb] = v[0];
-        __threadfence();
-        last = atomicAdd(&ctl->ticket[T_COL_STEP], 1u) == gridDim.x - 2;
-    }
-    __syncthreads();
-    if (!last) return;
+    if (!publish_partials<1>(v, part, &ctl->ticket[T_COL_STEP], sm, &last)) return;
     V t[1];
-    gather_all_partials<1>(t, part, gridDim.x - 1, a.csc, sm);
+    gather_all_partials<1>(t, part, gridDim.x, a.csc, sm);
     if (threadIdx.x != 0) return;
     ctl->ticket[T_COL_STEP] = 0;
-    ho->col_role = 0;
     ctl->dx2 = double(t[0]);
     ctl->apply = 0;
 }
