@@ -759,4 +759,80 @@ __device__ __forceinline__ void visit_bins(const BinTable& bt, int block, const 
 // Epilogue helper with nothing to prefetch.
 struct NoPre {};
 
+// ---- programmatic dependent launch of the iteration kernels ------------------
+// A pass kernel is launched as the programmatic dependent of the one before it:
+// its blocks may start while the previous pass's last blocks (and its serial
+// tail) still run.  Before griddepcontrol.wait they only touch what the
+// previous pass does not write (the matrix entries and the vectors of the
+// warp's first unit, both state buffers where the pass picks one by the
+// decision), so the first unit's loads hit L1 after the wait; every read that
+// depends on the previous pass comes after it.
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// The entries of the warp's first unit in the bins of `block` (the units
+// visit_bins gives it first), and touch(r) for the rows they finish.
+template <class V, class Touch>
+__device__ __forceinline__ void prefetch_first_unit(const BinTable& bt, int block, const Layout<V>& L,
+                                                    const Touch& touch) {
+    int bi = -1;
+#pragma unroll
+    for (int i = 0; i < kMaxBins; ++i)
+        if (i < bt.nbins && block >= bt.bin[i].block_begin && block < bt.bin[i].block_begin + bt.bin[i].nblocks)
+            bi = i;
+    if (bi < 0) return;
+    const Bin& b = bt.bin[bi];
+    const int stride = b.nblocks * kWarps;
+    const int w0 = (block - b.block_begin) * kWarps + (threadIdx.x >> 5);
+    if (w0 >= b.units) return;
+    const int lane = threadIdx.x & 31;
+    if (b.mode == BM_SLICED) {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int s = w0 + h * stride;
+            if (s >= b.units) break;
+            int off, len;
+            if (b.part0 > 0) {
+                off = b.slice0 + s * 32 * b.part0;
+                len = b.part0;
+            } else {
+                off = __ldg(L.soff + b.aux + s);
+                len = (__ldg(L.soff + b.aux + s + 1) - off) >> 5;
+            }
+            for (int u = 0; u < len && u < 4; ++u) {
+                prefetch_l1(L.idx + off + 32 * u + lane);
+                prefetch_l1(L.val + off + 32 * u + lane);
+            }
+            const int r = b.begin + s * 32 + lane;
+            if (r < b.end) touch(r);
+        }
+    } else if (b.mode == BM_SLAB) {
+        const int4 d = __ldg(L.unit + 2 * (b.aux + w0));
+        const int k0 = d.w * kSlabSteps, k1 = min(d.y, k0 + kSlabSteps);
+        for (int k = k0; k < k1 && k < k0 + kUnroll; ++k) {
+            prefetch_l1(L.idx + d.x + 32 * k + lane);
+            prefetch_l1(L.val + d.x + 32 * k + lane);
+        }
+        const int r = b.begin + 32 * d.z + lane;
+        if (r < b.end) touch(r);
+    } else {
+        int s0, t0, r = -1;
+        if (b.mode == BM_WARP) {
+            r = b.begin + w0;
+            s0 = __ldg(L.ptr + r);
+            t0 = __ldg(L.ptr + r + 1);
+        } else {                                   // SEGMENT
+            const int4 a0 = __ldg(L.unit + 2 * (b.aux + w0));
+            s0 = a0.x;
+            t0 = a0.y;
+        }
+        for (int k = s0 + lane; k < t0 && k < s0 + 32 * kUnroll; k += 32) {
+            prefetch_l1(L.idx + k);
+            prefetch_l1(L.val + k);
+        }
+        if (r >= 0 && lane == 0) touch(r);
+    }
+}
+
 }  // namespace sps

@@ -949,13 +949,33 @@ struct Engine : EngineBase {
         else ad_col_check<V, false><<<a.cols_chk.total_blocks, kBlock, 0, st>>>(a);
     }
 
+    // An adaptive pass kernel as the programmatic dependent of the kernel before it
+    // on the stream (its blocks may start during that kernel's last blocks; the
+    // kernel waits for it with griddepcontrol.wait before reading what it wrote).
+    cudaError_t launch_err = cudaSuccess;
+    template <class K>
+    void launch_pass(K kernel, int grid, const Args<V>& a) {
+        cudaLaunchConfig_t cfg{};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3(kBlock);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        const cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, a);
+        if (e != cudaSuccess && launch_err == cudaSuccess) launch_err = e;
+    }
+
     void launch_window(const Args<V>& a) {
         const int W = a.check_interval;
         const int gr = a.rows.total_blocks, gc = a.cols.total_blocks;
         if (mode == SPS_MODE_ADAPTIVE) {
             for (int w = 0; w < W; ++w) {
-                ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+                launch_pass(ad_row_step<V>, gr, a);
+                launch_pass(ad_col_step<V>, gc + a.col_tail_blocks, a);
             }
             ad_check_prep<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
             ad_row_check<V><<<a.rows_chk.total_blocks, kBlock, 0, st>>>(a);
@@ -977,8 +997,11 @@ struct Engine : EngineBase {
         SPS_CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         Args<V> a = args;
         a.has_cond = 0;
+        launch_err = cudaSuccess;
         launch_window(a);
+        cudaError_t le = launch_err;
         SPS_CK(cudaStreamEndCapture(st, &g));
+        SPS_CK(le);
         cudaError_t e = cudaGraphInstantiate(&win_exec, g, 0);
         cudaGraphDestroy(g);
         SPS_CK(e);
@@ -1005,8 +1028,10 @@ struct Engine : EngineBase {
         Args<V> a = args;
         a.cond = h;
         a.has_cond = 1;
+        launch_err = cudaSuccess;
         launch_window(a);
         e = cudaStreamEndCapture(st, &body);
+        if (e == cudaSuccess) e = launch_err;
         if (e != cudaSuccess) { cudaGraphDestroy(g); SPS_CK(e); }
         e = cudaGraphInstantiate(&loop_exec, g, 0);
         cudaGraphDestroy(g);
@@ -1052,7 +1077,11 @@ struct Engine : EngineBase {
         for (;;) {
             for (int64_t b = 0; b < batch; ++b) {
                 if (gm == 1) SPS_CK(cudaGraphLaunch(win_exec, st));
-                else launch_window(args);
+                else {
+                    launch_err = cudaSuccess;
+                    launch_window(args);
+                    SPS_CK(launch_err);
+                }
             }
             run += batch;
             launches += batch * nodes_per_window();
@@ -1295,16 +1324,18 @@ struct Engine : EngineBase {
                 cudaGraphExec_t ge = nullptr;
                 rec = cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal);
                 if (rec != cudaSuccess) break;
+                launch_err = cudaSuccess;
                 for (int r = 0; r < reps; ++r) {
                     if (mode == SPS_MODE_ADAPTIVE) {
-                        ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
-                        if (variant == 0) ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+                        launch_pass(ad_row_step<V>, gr, a);
+                        if (variant == 0) launch_pass(ad_col_step<V>, gc + a.col_tail_blocks, a);
                     } else {
                         rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
                         if (variant == 0) rf_col_step<V><<<gc, kBlock, 0, st>>>(a);
                     }
                 }
                 rec = cudaGetLastError();
+                if (rec == cudaSuccess) rec = launch_err;
                 const cudaError_t end = cudaStreamEndCapture(st, &g);     // always ends the capture
                 if (rec == cudaSuccess) rec = end;
                 if (rec == cudaSuccess) rec = cudaGraphInstantiate(&ge, g, 0);

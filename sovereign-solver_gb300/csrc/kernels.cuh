@@ -127,8 +127,23 @@ struct AdRowStepEpi {
     }
 };
 
+// Operands of row r in both state buffers (the pass reads one of them).
+template <class V>
+struct RowTouch {
+    const Args<V>* a;
+    __device__ __forceinline__ void operator()(int r) const {
+        prefetch_l1(a->b + r);
+        prefetch_l1(a->AX[0] + r);
+        prefetch_l1(a->AX[1] + r);
+        prefetch_l1(a->Y[0] + r);
+        prefetch_l1(a->Y[1] + r);
+    }
+};
+
 template <class V>
 SPS_PASS_KERNEL ad_row_step(Args<V> a) {
+    prefetch_first_unit(a.rows, blockIdx.x, a.csr, RowTouch<V>{&a});
+    grid_dep_wait();
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
     __shared__ V sm[kWarps * 2];
@@ -137,6 +152,7 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     const V sigma = block_scalar<V>([&] { return ctl->eta * ctl->omega; });
     AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], sigma};
     visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e);
+    grid_dep_launch_dependents();
     // reductions in V: FP32 sums in the FP32 engine (the step rule's inputs)
     V v[2] = {e.dy2, e.inter};
     V* part = reinterpret_cast<V*>(a.part_row);
@@ -182,8 +198,23 @@ struct AdColStepEpi {
     __device__ __forceinline__ void operator()(int j, int, const V (&acc)[1], const Pre& p) { finish(j, acc[0], p); }
 };
 
+// Operands of column j in both state buffers (the pass reads one of them).
+template <class V>
+struct ColTouch {
+    const Args<V>* a;
+    __device__ __forceinline__ void operator()(int j) const {
+        prefetch_l1(a->X[0] + j);
+        prefetch_l1(a->X[1] + j);
+        prefetch_l1(a->c + j);
+        prefetch_l1(a->xs + j);
+        prefetch_l1(a->xl + j);
+    }
+};
+
 template <class V>
 SPS_PASS_KERNEL ad_col_step(Args<V> a) {
+    if ((int)blockIdx.x < a.cols.total_blocks) prefetch_first_unit(a.cols, blockIdx.x, a.csc, ColTouch<V>{&a});
+    grid_dep_wait();
     Ctl* ctl = a.ctl;
     if (ctl->apply != AP_STEP_PENDING) return;
     __shared__ V sm[kWarps];
@@ -206,6 +237,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
         for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
             a.ys[i] += wgt * (yc[i] - a.yl[i]);
     }
+    grid_dep_launch_dependents();
     V v[1] = {e.dx2};
     V* part = reinterpret_cast<V*>(a.part_col);
     if (!publish_partials<1>(v, part, &ctl->ticket[T_COL_STEP], sm, &last)) return;
