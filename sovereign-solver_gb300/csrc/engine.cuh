@@ -783,34 +783,31 @@ __device__ __forceinline__ void prefetch_first_unit(const BinTable& bt, int bloc
             bi = i;
     if (bi < 0) return;
     const Bin& b = bt.bin[bi];
-    const int stride = b.nblocks * kWarps;
     const int w0 = (block - b.block_begin) * kWarps + (threadIdx.x >> 5);
     if (w0 >= b.units) return;
     const int lane = threadIdx.x & 31;
+    // (the first slice or unit and its first two steps only: with more, the touched
+    // lines of five resident blocks outgrew L1 on LPs with longer columns)
     if (b.mode == BM_SLICED) {
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const int s = w0 + h * stride;
-            if (s >= b.units) break;
-            int off, len;
-            if (b.part0 > 0) {
-                off = b.slice0 + s * 32 * b.part0;
-                len = b.part0;
-            } else {
-                off = __ldg(L.soff + b.aux + s);
-                len = (__ldg(L.soff + b.aux + s + 1) - off) >> 5;
-            }
-            for (int u = 0; u < len && u < 4; ++u) {
-                prefetch_l1(L.idx + off + 32 * u + lane);
-                prefetch_l1(L.val + off + 32 * u + lane);
-            }
-            const int r = b.begin + s * 32 + lane;
-            if (r < b.end) touch(r);
+        const int s = w0;
+        int off, len;
+        if (b.part0 > 0) {
+            off = b.slice0 + s * 32 * b.part0;
+            len = b.part0;
+        } else {
+            off = __ldg(L.soff + b.aux + s);
+            len = (__ldg(L.soff + b.aux + s + 1) - off) >> 5;
         }
+        for (int u = 0; u < len && u < 2; ++u) {
+            prefetch_l1(L.idx + off + 32 * u + lane);
+            prefetch_l1(L.val + off + 32 * u + lane);
+        }
+        const int r = b.begin + s * 32 + lane;
+        if (r < b.end) touch(r);
     } else if (b.mode == BM_SLAB) {
         const int4 d = __ldg(L.unit + 2 * (b.aux + w0));
         const int k0 = d.w * kSlabSteps, k1 = min(d.y, k0 + kSlabSteps);
-        for (int k = k0; k < k1 && k < k0 + kUnroll; ++k) {
+        for (int k = k0; k < k1 && k < k0 + 2; ++k) {
             prefetch_l1(L.idx + d.x + 32 * k + lane);
             prefetch_l1(L.val + d.x + 32 * k + lane);
         }
@@ -827,7 +824,7 @@ __device__ __forceinline__ void prefetch_first_unit(const BinTable& bt, int bloc
             s0 = a0.x;
             t0 = a0.y;
         }
-        for (int k = s0 + lane; k < t0 && k < s0 + 32 * kUnroll; k += 32) {
+        for (int k = s0 + lane; k < t0 && k < s0 + 64; k += 32) {
             prefetch_l1(L.idx + k);
             prefetch_l1(L.val + k);
         }

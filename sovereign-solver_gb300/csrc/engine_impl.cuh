@@ -899,6 +899,12 @@ struct Engine : EngineBase {
         }
         a.col_tail_blocks = tail;
         a.apply_blocks = apply_blocks;
+        // Programmatic dependent launch of the step kernels where a pass is short enough
+        // for the launch and the first unit's load latency to matter: on GB300 it cut the
+        // attempt by 6 % on a 200 x 500 LP and 2 % on a 4M-nonzero transportation LP,
+        // and slowed a 21M-nonzero power-law LP's row pass by 4 % (which keeps the plain
+        // instantiations).
+        a.pdl = adaptive && rp.total + cp.total < (int64_t(1) << 25);
         a.c = d_c; a.b = d_b; a.lo = d_lo; a.hi = d_hi;
         a.uniform_bounds = uniform;
         a.far_residual = adaptive && opt.kkt_form == SPS_KKT_PDLP;
@@ -974,8 +980,13 @@ struct Engine : EngineBase {
         const int gr = a.rows.total_blocks, gc = a.cols.total_blocks;
         if (mode == SPS_MODE_ADAPTIVE) {
             for (int w = 0; w < W; ++w) {
-                launch_pass(ad_row_step<V>, gr, a);
-                launch_pass(ad_col_step<V>, gc + a.col_tail_blocks, a);
+                if (a.pdl) {
+                    launch_pass(ad_row_step<V, true>, gr, a);
+                    launch_pass(ad_col_step<V, true>, gc + a.col_tail_blocks, a);
+                } else {
+                    ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
+                    ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
+                }
             }
             ad_check_prep<V><<<a.apply_blocks, kBlock, 0, st>>>(a);
             ad_row_check<V><<<a.rows_chk.total_blocks, kBlock, 0, st>>>(a);
@@ -1326,9 +1337,12 @@ struct Engine : EngineBase {
                 if (rec != cudaSuccess) break;
                 launch_err = cudaSuccess;
                 for (int r = 0; r < reps; ++r) {
-                    if (mode == SPS_MODE_ADAPTIVE) {
-                        launch_pass(ad_row_step<V>, gr, a);
-                        if (variant == 0) launch_pass(ad_col_step<V>, gc + a.col_tail_blocks, a);
+                    if (mode == SPS_MODE_ADAPTIVE && a.pdl) {
+                        launch_pass(ad_row_step<V, true>, gr, a);
+                        if (variant == 0) launch_pass(ad_col_step<V, true>, gc + a.col_tail_blocks, a);
+                    } else if (mode == SPS_MODE_ADAPTIVE) {
+                        ad_row_step<V><<<gr, kBlock, 0, st>>>(a);
+                        if (variant == 0) ad_col_step<V><<<gc + a.col_tail_blocks, kBlock, 0, st>>>(a);
                     } else {
                         rf_row_step<V><<<gr, kBlock, 0, st>>>(a);
                         if (variant == 0) rf_col_step<V><<<gc, kBlock, 0, st>>>(a);

@@ -52,6 +52,7 @@ struct Args {
     const volatile int32_t* abort_flag;
     cudaGraphConditionalHandle cond;
     int32_t has_cond;
+    int32_t pdl;               // launch the step kernels' programmatic-dependent instantiations
     int32_t check_interval;
     int64_t max_windows;
 };
@@ -140,10 +141,14 @@ struct RowTouch {
     }
 };
 
-template <class V>
+// Pdl: launched as a programmatic dependent (a separate instantiation, so the
+// plain kernel's code is not touched by the prologue).
+template <class V, bool Pdl = false>
 SPS_PASS_KERNEL ad_row_step(Args<V> a) {
-    prefetch_first_unit(a.rows, blockIdx.x, a.csr, RowTouch<V>{&a});
-    grid_dep_wait();
+    if constexpr (Pdl) {
+        prefetch_first_unit(a.rows, blockIdx.x, a.csr, RowTouch<V>{&a});
+        grid_dep_wait();
+    }
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
     __shared__ V sm[kWarps * 2];
@@ -152,7 +157,7 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     const V sigma = block_scalar<V>([&] { return ctl->eta * ctl->omega; });
     AdRowStepEpi<V> e{a.b, a.AX[cur], a.Y[cur], a.AX[1 - cur], a.Y[1 - cur], sigma};
     visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.X[1 - cur]}, e);
-    grid_dep_launch_dependents();
+    if constexpr (Pdl) grid_dep_launch_dependents();
     // reductions in V: FP32 sums in the FP32 engine (the step rule's inputs)
     V v[2] = {e.dy2, e.inter};
     V* part = reinterpret_cast<V*>(a.part_row);
@@ -211,10 +216,12 @@ struct ColTouch {
     }
 };
 
-template <class V>
+template <class V, bool Pdl = false>
 SPS_PASS_KERNEL ad_col_step(Args<V> a) {
-    if ((int)blockIdx.x < a.cols.total_blocks) prefetch_first_unit(a.cols, blockIdx.x, a.csc, ColTouch<V>{&a});
-    grid_dep_wait();
+    if constexpr (Pdl) {
+        if ((int)blockIdx.x < a.cols.total_blocks) prefetch_first_unit(a.cols, blockIdx.x, a.csc, ColTouch<V>{&a});
+        grid_dep_wait();
+    }
     Ctl* ctl = a.ctl;
     if (ctl->apply != AP_STEP_PENDING) return;
     __shared__ V sm[kWarps];
@@ -237,7 +244,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
         for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
             a.ys[i] += wgt * (yc[i] - a.yl[i]);
     }
-    grid_dep_launch_dependents();
+    if constexpr (Pdl) grid_dep_launch_dependents();
     V v[1] = {e.dx2};
     V* part = reinterpret_cast<V*>(a.part_col);
     if (!publish_partials<1>(v, part, &ctl->ticket[T_COL_STEP], sm, &last)) return;
