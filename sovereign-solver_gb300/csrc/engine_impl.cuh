@@ -355,7 +355,8 @@ struct Engine : EngineBase {
     // SEGMENT rows, then SLAB rows (stable counting sort); one bin per (kind,
     // schedule).
     static void make_plan(const std::vector<int64_t>& lens, const std::vector<int8_t>* kinds,
-                          const std::vector<uint8_t>* slab, Plan& P, int block_cap) {
+                          const std::vector<uint8_t>* slab, Plan& P, int block_cap,
+                          const CreateTrace* tr = nullptr) {
         const int R = (int)lens.size();
         constexpr int NB = kSliceMax + 4;
         auto kind_of = [&](int i) { return kinds ? (int)(*kinds)[i] : 0; };
@@ -395,6 +396,7 @@ struct Engine : EngineBase {
             for (; i < hi; ++i) ++h[kb[i]];
             for (int b = 0; b < 2 * NB; ++b) hist[t][b] = h[b] + h[2 * NB + b] + h[4 * NB + b] + h[6 * NB + b];
         });
+        if (tr) tr->mark("    buckets + histograms");
         std::vector<int64_t> cnt(2 * NB + 1, 0);
         for (int t = 0; t < nt; ++t)
             for (int b = 0; b < 2 * NB; ++b) cnt[b + 1] += hist[t][b];
@@ -426,6 +428,7 @@ struct Engine : EngineBase {
             return kd * 4 + (sub <= kSliceMax ? (int)BM_SLICED : sub == kSliceMax + 1 ? (int)BM_WARP
                                               : sub == kSliceMax + 2 ? (int)BM_SEGMENT : (int)BM_SLAB);
         };
+        if (tr) tr->mark("    stable placement");
         P.fptr.assign(R + 1, 0);
         P.bt = BinTable{};
         int64_t off = 0;
@@ -508,6 +511,7 @@ struct Engine : EngineBase {
             P.bt.bin[P.bt.nbins++] = b;
             r = e;
         }
+        if (tr) tr->mark("    bins + offsets");
         P.fptr[R] = (int32_t)std::min<int64_t>(off, INT32_MAX);
         P.total = off;
         P.bin_store = bin_store;
@@ -608,18 +612,23 @@ struct Engine : EngineBase {
         std::vector<int64_t> clen(n);
         for (int j = 0; j < n; ++j) clen[j] = colcount[j];
         Plan cp;
-        make_plan(clen, nullptr, nullptr, cp, block_cap);
+        if (trace) trace->mark("  column lengths");
+        make_plan(clen, nullptr, nullptr, cp, block_cap, trace);
+        if (trace) trace->mark("  column plan");
         const std::vector<int32_t>& perm_col = cp.perm;
         std::vector<int32_t> inv_col(n);
         for_chunks(n, host_threads(n), [&](int, int lo, int hi) {
             for (int j = lo; j < hi; ++j) inv_col[perm_col[j]] = j;
         });
+        if (trace) trace->mark("  inverse column order");
 
         // ---- row plan: bins by row kind, length and gather locality (SLAB groups)
         Plan rp;
         {
             const std::vector<uint8_t> slab = choose_slab(hp, inv_col, (int)sizeof(V));
+            if (trace) trace->mark("  SLAB choice");
             make_plan(rlen, &hp.kind, &slab, rp, block_cap);
+            if (trace) trace->mark("  row plan");
         }
         const std::vector<int32_t>& perm_row = rp.perm;
         if (rp.total > INT32_MAX || cp.total > INT32_MAX) {
@@ -627,6 +636,7 @@ struct Engine : EngineBase {
             return fail(SPS_ERR_INVALID, "padded matrix layout exceeds 2^31-1 entries");
         }
         std::vector<int32_t> nptr(m + 1, 0), cptr(n + 1, 0);
+        if (trace) trace->mark("  layout size checks");
         prefix_lengths(m, [&](int r) { return (int32_t)rlen[perm_row[r]]; }, nptr);
         prefix_lengths(n, [&](int j) { return colcount[perm_col[j]]; }, cptr);
 
