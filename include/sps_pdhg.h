@@ -98,7 +98,9 @@ typedef struct {
     int32_t batch_group;      /* batched solver: lanes per column (1, 2, 4, 8, 16, 32), 0 = autotune */
     int32_t escalate;         /* adaptive FP32 stall handling.  A solve stalls when its best
                                  relative KKT error has not halved for max(2048, k/2) attempts
-                                 (k = attempt of the last halving).  1 (default): continue in
+                                 (k = attempt of the last halving); a single LP only once that
+                                 error is at most 1e-3 (counting from when it got there), a
+                                 batch instance at any error.  1 (default): continue in
                                  FP64 from the best point seen, with the primal weight it had;
                                  2: stop with SPS_STATUS_STALLED; 0: no stall test (FP32 only) */
     int32_t warm_fallback;    /* 1 (default): a warm start whose relative KKT error is larger than

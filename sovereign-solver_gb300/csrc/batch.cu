@@ -386,6 +386,7 @@ __device__ bool start_point(const Args& A, int k, const Inst& I, const View& v, 
         c.omega = warm && A.wom[k] > 0.0 ? A.wom[k] : A.a.omega0[k];
         c.kkt_last = INFINITY;
         c.stall_on = A.stall_on;
+        c.stall_ceiling = INFINITY;   // a stalled instance leaves the launch for the FP64 continuation
     }
     TEAM_OWNED(j, v.n, chc) {
         const float x0 = warm ? float(A.wx[I.vc + j] / v.dc[j]) : 0.f;

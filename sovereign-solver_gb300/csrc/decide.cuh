@@ -14,7 +14,15 @@ enum ApplyBits { AP_LOAD_AVG = 1, AP_RESTART = 2, AP_CANDIDATE = 4, AP_STEP_PEND
 
 // Stall test: the best relative KKT error has not halved for
 // max(kStallMin, anchor / 2) attempts, anchor = attempt of the last halving.
+// With a ceiling (Ctl::stall_ceiling) only an error at or below it can stall,
+// and the count starts again when the error first reaches it: above it a
+// plateau is the method's slow progress, not the FP32 precision floor.
 constexpr int64_t kStallMin = 2048;
+// The single-LP engine's ceiling.  FP32 iterates' error floor is far below it
+// on any LP they can solve; above it FP64 only makes each attempt dearer (a
+// 21M-nonzero power-law LP stalled at 1.3e-2 after 3 968 attempts: 13.7 s to
+// 1e-4 with the FP64 continuation, 10.9 s in FP32 alone).
+constexpr double kStallCeiling = 1e-3;
 // Infeasibility tests on the change since the last restart (scaled space): a
 // certificate's residual must be at most kRayTol of its objective.
 constexpr double kRayTol = 1e-6;
@@ -125,10 +133,11 @@ __device__ __forceinline__ void decide_check(Ctl& c, const double (&tc)[kColPart
             c.best_saved = 1;
             save = AP_SAVE_BEST | (best == 0 ? AP_SAVE_AVG : 0);
         }
-        if (r <= 0.5 * c.anchor_rel) {
+        if (r <= 0.5 * c.anchor_rel || (c.anchor_rel > c.stall_ceiling && r <= c.stall_ceiling)) {
             c.anchor_rel = r;
             c.anchor_iter = c.iters;
-        } else if (c.iters - c.anchor_iter >= (c.anchor_iter / 2 > kStallMin ? c.anchor_iter / 2 : kStallMin)) {
+        } else if (c.best_rel <= c.stall_ceiling &&
+                   c.iters - c.anchor_iter >= (c.anchor_iter / 2 > kStallMin ? c.anchor_iter / 2 : kStallMin)) {
             stalled = true;
         }
     }

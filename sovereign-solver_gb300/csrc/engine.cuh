@@ -127,6 +127,7 @@ struct Ctl {
     double anchor_rel;       // best error at that attempt
     double best_rel;         // best relative KKT error seen at a check
     double omega_best;       // primal weight when the best point was taken
+    double stall_ceiling;    // a stall is declared only at or below this error (INFINITY: always)
     uint64_t t_begin, t_end; // batched solver: device clock (ns) at the instance's start and end
     int32_t warm_used;       // batched solver: the instance started from its warm start
     double rel_kkt_lagr;     // the returned point's error in the Lagrangian form (= rel_kkt unless

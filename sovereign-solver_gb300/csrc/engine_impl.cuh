@@ -1131,6 +1131,7 @@ struct Engine : EngineBase {
         c0.omega = omega0;
         c0.kkt_last = INFINITY;
         c0.stall_on = stall_test() ? 1 : 0;
+        c0.stall_ceiling = kStallCeiling;
         *h_ctl = c0;
         *(volatile int32_t*)h_abort = 0;
         launches = 0;
