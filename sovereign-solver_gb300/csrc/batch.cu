@@ -1544,6 +1544,8 @@ extern "C" int sps_batch_set_warm_starts_gnn(sps_batch* b, sps_gnn* g, const dou
         SPB_CK(cudaGetLastError());
     }
     SPB_CK(cudaStreamSynchronize(io.stream));
+    if (sps::gnn::check_device_error(g) != 0)
+        return b->fail(SPS_ERR_CUDA, std::string("network: ") + sps_gnn_last_error(g));
     b->warm = 1;
     return SPS_OK;
 }

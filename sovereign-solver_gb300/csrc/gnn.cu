@@ -186,6 +186,204 @@ __global__ void __launch_bounds__(kT, 2) k_update(const float* __restrict__ h, c
     }
 }
 
+// ---- dense node update on the tensor cores (H = 64) -------------------------------
+// The same update as k_update, out = relu([h | a] W^T + b) with W = [U | M]
+// (64 x 128), as tcgen05 MMAs: M = 128 nodes per tile (one TMEM lane each), N =
+// 64 outputs (64 TMEM columns of FP32 accumulators), K = 128 in four 32-float
+// chunks of 128-byte rows (K-major, 128-byte swizzle: 16-byte piece q of row r
+// sits at piece q ^ (r & 7) of the row; 8-row groups 1024 bytes apart), eight
+// K = 8 steps per chunk.  The activations are split as x = big + small, both
+// TF32 (round to nearest), and both parts are multiplied (the BF16 weights are
+// exact in TF32): the products are exact and the sum is accumulated in FP32,
+// so the result agrees with the FP32 update to FP32 rounding, not TF32's.
+// All 256 threads stage a chunk (global -> split -> swizzled shared memory,
+// two buffers); thread 0 issues the chunk's MMAs and commits them to the
+// buffer's mbarrier, which the stagers wait on before they overwrite it; the
+// eight warps read the accumulators back (tcgen05.ld, warp w: lanes of quarter
+// w % 4, columns 32 (w / 4) ..) for the bias and ReLU.  Every wait is bounded;
+// a block that gives up sets *err, stops, and still frees its TMEM.
+namespace tc {
+constexpr int kRows = 128;                    // nodes per tile: the MMA's M and the TMEM lanes
+constexpr int kABytes = kRows * 128;          // one 32-float chunk of the activations (16 KB)
+constexpr int kBBytes = 64 * 128;             // one 32-float chunk of the weights (8 KB)
+constexpr uint32_t kTmemCols = 64;
+constexpr int kSmemBytes = 4 * kBBytes + 4 * kABytes + 64 + 1024;   // + barriers, TMEM slot, alignment
+constexpr int kWaitPolls = 1 << 20;
+// instruction descriptor: D F32, A and B TF32, both K-major, N = 64, M = 128
+constexpr uint32_t kIdesc = (1u << 4) | (2u << 7) | (2u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t u;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(u) : "f"(x));
+    return __uint_as_float(u);
+}
+
+// K-major operand, 128-byte swizzle, 8-row groups 1024 bytes apart
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t addr) {
+    return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (int i = 0; i < kWaitPolls; ++i) {
+        uint32_t done;
+        asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                     "selp.u32 %0, 1, 0, p;\n\t}"
+                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}"
+                 ::"r"(d), "l"(a), "l"(b), "r"(kIdesc), "r"(accumulate) : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+                 "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+                 "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                   "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]),
+                   "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]),
+                   "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+}  // namespace tc
+
+__global__ void __launch_bounds__(kT, 2) k_update_tc(const float* __restrict__ h, const float* __restrict__ a,
+                                                     const __nv_bfloat16* __restrict__ U,
+                                                     const __nv_bfloat16* __restrict__ M,
+                                                     const float* __restrict__ bias, float* __restrict__ out,
+                                                     int64_t nodes, int32_t* __restrict__ err) {
+    constexpr int H = 64;
+    extern __shared__ __align__(16) unsigned char tc_smem[];
+    unsigned char* base = tc_smem + ((1024 - (tc::smem_u32(tc_smem) & 1023)) & 1023);
+    unsigned char* Bs = base;                              // 4 chunks of W, 64 rows of 128 bytes
+    unsigned char* As = base + 4 * tc::kBBytes;            // buffer b: big at As + 2 b kABytes, small after it
+    uint64_t* bars = reinterpret_cast<uint64_t*>(As + 4 * tc::kABytes);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // the weights, K-major: row o of chunk c holds W[o][32 c .. 32 c + 31]
+    for (int t = threadIdx.x; t < 4 * H * 8; t += kT) {
+        const int c = t / (H * 8), o = (t / 8) % H, q = t % 8;
+        float w[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int k = 32 * c + 4 * q + e;
+            w[e] = __bfloat162float(k < H ? U[o * H + k] : M[o * H + (k - H)]);
+        }
+        *reinterpret_cast<float4*>(Bs + c * tc::kBBytes + o * 128 + ((q ^ (o & 7)) << 4)) =
+            make_float4(w[0], w[1], w[2], w[3]);
+    }
+    if (threadIdx.x == 0) {
+        tc::mbar_init(tc::smem_u32(&bars[0]), 1);
+        tc::mbar_init(tc::smem_u32(&bars[1]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                     ::"r"(tc::smem_u32(tmem_slot)), "r"(tc::kTmemCols) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");   // W, written by threads, read by the MMA
+    tc::fence_before();
+    __syncthreads();
+    tc::fence_after();
+    const uint32_t tmem = *tmem_slot;
+    const int col0 = 32 * (warp >> 2);                     // this warp's accumulator columns
+    const uint32_t tq = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)col0;
+    uint32_t parity[2] = {0u, 0u};
+    bool ok = true;
+    const int64_t tiles = (nodes + tc::kRows - 1) / tc::kRows;
+    for (int64_t tile = blockIdx.x; tile < tiles && ok; tile += gridDim.x) {
+        const int64_t base_node = tile * tc::kRows;
+        for (int c = 0; c < 4; ++c) {
+            const int buf = c & 1;
+            if (c >= 2) {                                  // the MMAs that read this buffer (chunk c - 2)
+                if (!tc::mbar_wait(tc::smem_u32(&bars[buf]), parity[buf])) ok = false;
+                parity[buf] ^= 1u;
+            }
+            unsigned char* big = As + 2 * buf * tc::kABytes;
+            unsigned char* small = big + tc::kABytes;
+            const float* src = c < 2 ? h + 32 * c : a + 32 * (c - 2);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int pc = threadIdx.x + kT * i, row = pc >> 3, q = pc & 7;
+                const int64_t v = base_node + row;
+                float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (v < nodes) x = __ldg(reinterpret_cast<const float4*>(src + v * H + 4 * q));
+                const float4 hi = make_float4(tc::tf32_rna(x.x), tc::tf32_rna(x.y), tc::tf32_rna(x.z), tc::tf32_rna(x.w));
+                const float4 lo = make_float4(tc::tf32_rna(x.x - hi.x), tc::tf32_rna(x.y - hi.y),
+                                              tc::tf32_rna(x.z - hi.z), tc::tf32_rna(x.w - hi.w));
+                const int off = row * 128 + ((q ^ (row & 7)) << 4);
+                *reinterpret_cast<float4*>(big + off) = hi;
+                *reinterpret_cast<float4*>(small + off) = lo;
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            tc::fence_before();
+            __syncthreads();
+            tc::fence_after();
+            if (threadIdx.x == 0) {
+                const uint32_t ab = tc::smem_u32(big), as = tc::smem_u32(small);
+                const uint32_t bb = tc::smem_u32(Bs + c * tc::kBBytes);
+#pragma unroll
+                for (int kk = 0; kk < 4; ++kk) {
+                    const uint64_t bd = tc::desc_sw128(bb + 32 * kk);
+                    tc::mma_tf32(tmem, tc::desc_sw128(ab + 32 * kk), bd, (c | kk) != 0 ? 1u : 0u);
+                    tc::mma_tf32(tmem, tc::desc_sw128(as + 32 * kk), bd, 1u);
+                }
+                tc::mma_commit(tc::smem_u32(&bars[buf]));
+            }
+        }
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {                      // chunks 2 and 3: the tile's last MMAs
+            if (!tc::mbar_wait(tc::smem_u32(&bars[b]), parity[b])) ok = false;
+            parity[b] ^= 1u;
+        }
+        tc::fence_after();
+        uint32_t r[32];
+        tc::tmem_ld32(tq, r);
+        const int64_t v = base_node + 32 * (warp & 3) + lane;
+        if (v < nodes && ok) {
+            float* o = out + v * H + col0;
+#pragma unroll
+            for (int j = 0; j < 32; j += 4) {
+                const float4 y = make_float4(relu(__uint_as_float(r[j]) + bias[col0 + j]),
+                                             relu(__uint_as_float(r[j + 1]) + bias[col0 + j + 1]),
+                                             relu(__uint_as_float(r[j + 2]) + bias[col0 + j + 2]),
+                                             relu(__uint_as_float(r[j + 3]) + bias[col0 + j + 3]));
+                *reinterpret_cast<float4*>(o + j) = y;
+            }
+        }
+        tc::fence_before();
+        ok = __syncthreads_and(ok) != 0;                    // TMEM read before the next tile's MMAs
+        tc::fence_after();
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(tc::kTmemCols) : "memory");
+}
+
 // ---- heads: out[v] = w . h[v] + b (warp per node) ----------------------------------
 template <int H>
 __global__ void __launch_bounds__(kT) k_head(const float* __restrict__ h, const __nv_bfloat16* __restrict__ w,
@@ -558,6 +756,7 @@ struct sps_gnn {
     std::vector<float*> HV, HC, AV, AC;
     float *dHV, *dHC, *dHV2, *dHC2, *dA;
     float *x0, *y0, *lw, *pool, *dx0, *dy0, *dlw;
+    int32_t* d_err = nullptr;    // set by a tensor-core update that gave up waiting (internal error)
     float *part;              // weight-gradient block partials
     double* lpart;            // loss partials
     float *pcp, *pvp;         // pooling partials
@@ -605,6 +804,9 @@ int set_smem_attrs() {
     if (cudaFuncSetAttribute(k_update<H>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)update_smem<H>()) !=
         cudaSuccess)
         return -2;
+    if (H == 64 &&
+        cudaFuncSetAttribute(k_update_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kSmemBytes) != cudaSuccess)
+        return -2;
     if (cudaFuncSetAttribute(k_update_back<H>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)update_back_smem<H>()) != cudaSuccess)
         return -2;
@@ -614,6 +816,28 @@ int set_smem_attrs() {
 int grid_for(int64_t work, int per_block) {
     const int64_t b = (work + per_block - 1) / per_block;
     return (int)std::max<int64_t>(1, std::min<int64_t>(b, 152 * 8));
+}
+
+// The dense node update: on the tensor cores for H = 64, the register-tiled
+// FP32 kernel for H = 32.
+template <int H>
+void dense_update(sps_gnn* g, const float* h, const float* a, const __nv_bfloat16* U, const __nv_bfloat16* M,
+                  const float* b, float* out, int64_t nodes) {
+    if constexpr (H == 64)
+        k_update_tc<<<g->nb_dense, kT, tc::kSmemBytes, g->st>>>(h, a, U, M, b, out, nodes, g->d_err);
+    else
+        k_update<H><<<g->nb_dense, kT, update_smem<H>(), g->st>>>(h, a, U, M, b, out, nodes);
+}
+
+// After the stream is synchronised: a tensor-core update that gave up waiting
+// for its MMAs left its flag (the outputs of that forward are not valid).
+int device_error(sps_gnn* g) {
+    int32_t e = 0;
+    if (!g->d_err) return 0;
+    if (cudaMemcpyAsync(&e, g->d_err, sizeof(e), cudaMemcpyDeviceToHost, g->st) != cudaSuccess ||
+        cudaStreamSynchronize(g->st) != cudaSuccess)
+        return g->fail(-2, "reading the network's error flag failed");
+    return e ? g->fail(-2, "internal error: a tensor-core node update stopped waiting for its MMAs") : 0;
 }
 
 // Forward pass over `batch` instances whose features are already on the device.
@@ -631,12 +855,10 @@ int forward(sps_gnn* g, int batch) {
         const int64_t oUc = o, oMc = o + H * H, obc = o + 2 * H * H;
         const int64_t oUv = obc + H, oMv = oUv + H * H, obv = oMv + H * H;
         k_agg<H><<<grid_for(NC * 32, kT), kT, 0, st>>>(g->cptr, g->cidx, g->ac_c, g->HV[l], g->AC[l], m, n, batch, 0);
-        k_update<H><<<g->nb_dense, kT, update_smem<H>(), st>>>(g->HC[l], g->AC[l], W + oUc, W + oMc, P + obc,
-                                                               g->HC[l + 1], NC);
+        dense_update<H>(g, g->HC[l], g->AC[l], W + oUc, W + oMc, P + obc, g->HC[l + 1], NC);
         k_agg<H><<<grid_for(NV * 32, kT), kT, 0, st>>>(g->vptr, g->vidx, g->av_v, g->HC[l + 1], g->AV[l], n, m, batch,
                                                        0);
-        k_update<H><<<g->nb_dense, kT, update_smem<H>(), st>>>(g->HV[l], g->AV[l], W + oUv, W + oMv, P + obv,
-                                                               g->HV[l + 1], NV);
+        dense_update<H>(g, g->HV[l], g->AV[l], W + oUv, W + oMv, P + obv, g->HV[l + 1], NV);
     }
     k_head<H><<<grid_for(NV * 32, kT), kT, 0, st>>>(g->HV[L], W + g->oWx, P + g->obx, g->x0, NV);
     k_head<H><<<grid_for(NC * 32, kT), kT, 0, st>>>(g->HC[L], W + g->oWy, P + g->oby, g->y0, NC);
@@ -790,6 +1012,8 @@ int device_io(sps_gnn* g, DeviceIO* io) {
     return 0;
 }
 
+int check_device_error(sps_gnn* g) { return g ? device_error(g) : -1; }
+
 int forward_in_place(sps_gnn* g, int batch) {
     if (!g || !g->lpf || batch < 1 || batch > g->B) return g ? g->fail(-1, "forward_in_place needs lp_features") : -1;
     k_lp_con_features<<<grid_for((int64_t)g->m * batch * 32, kT), kT, 0, g->st>>>(
@@ -930,6 +1154,8 @@ int sps_gnn_create(const sps_gnn_graph* gr, const sps_gnn_options* opt_in, sps_g
             GNN_CK(g->alloc(&g->x0, NV)); GNN_CK(g->alloc(&g->y0, NC)); GNN_CK(g->alloc(&g->lw, B));
             GNN_CK(g->alloc(&g->dx0, NV)); GNN_CK(g->alloc(&g->dy0, NC)); GNN_CK(g->alloc(&g->dlw, B));
             GNN_CK(g->alloc(&g->pool, 2 * H * B));
+            GNN_CK(g->alloc(&g->d_err, 1));
+            GNN_CK(cudaMemsetAsync(g->d_err, 0, sizeof(int32_t), g->st));
             g->nb_dense = 152 * 2;
             g->nb_loss = 152 * 2;
             g->nb_pool_c = std::max(1, std::min(64, (m + 31) / 32));
@@ -973,7 +1199,7 @@ int sps_gnn_predict(sps_gnn* g, int32_t batch, const float* vf, const float* cf,
     if (y0) GNN_CK(cudaMemcpyAsync(y0, g->y0, sizeof(float) * nc, cudaMemcpyDeviceToHost, g->st));
     if (lw) GNN_CK(cudaMemcpyAsync(lw, g->lw, sizeof(float) * batch, cudaMemcpyDeviceToHost, g->st));
     GNN_CK(cudaStreamSynchronize(g->st));
-    return 0;
+    return device_error(g);
 }
 
 int sps_gnn_loss_grad(sps_gnn* g, int32_t batch, const float* vf, const float* cf, const float* xt, const float* yt,
@@ -989,7 +1215,7 @@ int sps_gnn_loss_grad(sps_gnn* g, int32_t batch, const float* vf, const float* c
         GNN_CK(cudaMemcpyAsync(grad, g->G, sizeof(float) * g->np, cudaMemcpyDeviceToHost, g->st));
         GNN_CK(cudaStreamSynchronize(g->st));
     }
-    return 0;
+    return device_error(g);
 }
 
 int sps_gnn_train_step(sps_gnn* g, int32_t batch, const float* vf, const float* cf, const float* xt, const float* yt,
@@ -1007,8 +1233,7 @@ int sps_gnn_train_step(sps_gnn* g, int32_t batch, const float* vf, const float* 
     k_adam<<<grid_for(g->np, 256), 256, 0, g->st>>>(g->P, g->G, g->M1, g->M2, g->PB, g->np, g->opt.lr,
                                                     g->opt.beta1, g->opt.beta2, g->opt.eps, c1, c2);
     GNN_CK(cudaGetLastError());
-    if (!loss) GNN_CK(cudaStreamSynchronize(g->st));
-    return 0;
+    return device_error(g);     // (synchronises the stream)
 }
 
 int64_t sps_gnn_num_params(const sps_gnn* g) { return g ? g->np : -1; }

@@ -22,6 +22,9 @@ int device_io(sps_gnn* g, DeviceIO* io);
 // Forward pass of `batch` instances whose inputs are already in c_in / b_in
 // (queued on io.stream; no synchronisation).
 int forward_in_place(sps_gnn* g, int batch);
+// After the network's stream is synchronised: 0, or the internal error of a
+// tensor-core node update that gave up waiting (that forward's outputs are invalid).
+int check_device_error(sps_gnn* g);
 
 }  // namespace gnn
 }  // namespace sps
