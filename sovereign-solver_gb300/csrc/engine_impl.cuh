@@ -642,7 +642,7 @@ struct Engine : EngineBase {
 
         if (trace) trace->mark("host plans");
         // ---- persistent arena
-        const int tail = std::min(grid_for(m), kSms * 4);
+        const int tail = 0;     // the column pass's blocks also update the dual average
         const int apply_blocks = grid_for(std::max(n, m), kBlock, kSms * 8);
         const size_t part_row_n = (size_t)std::max(rp.bt.total_blocks, 1) * kRowPartials;
         const size_t part_col_n = (size_t)(cp.bt.total_blocks + tail) * (kColPartials + kLagPartials);

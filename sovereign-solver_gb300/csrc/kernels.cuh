@@ -32,7 +32,7 @@ struct Args {
     BinTable rows, cols;
     BinTable rows_chk, cols_chk;   // the same bins with the check kernels' block shares (one wave
                                    // at their own occupancy: they hold more registers)
-    int32_t col_tail_blocks;   // extra blocks of ad_col_step that sweep the rows
+    int32_t col_tail_blocks;   // extra blocks of ad_col_step (0: its column blocks also sweep the rows)
     int32_t apply_blocks;
     const V* c; const V* b; const V* lo; const V* hi;
     V lo_u, hi_u;
@@ -219,7 +219,7 @@ struct ColTouch {
 template <class V, bool Pdl = false>
 SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     if constexpr (Pdl) {
-        if ((int)blockIdx.x < a.cols.total_blocks) prefetch_first_unit(a.cols, blockIdx.x, a.csc, ColTouch<V>{&a});
+        prefetch_first_unit(a.cols, blockIdx.x, a.csc, ColTouch<V>{&a});
         grid_dep_wait();
     }
     Ctl* ctl = a.ctl;
@@ -232,17 +232,16 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     const V wgt = block_scalar<V>([&] { return ctl->eta_used; });
     AdColStepEpi<V> e{&a, a.X[cur], a.c, a.ATY[cur], a.xl, a.ATY[cur], a.X[1 - cur], a.xs, tau, wgt, acc};
     const int colblocks = a.cols.total_blocks;
-    if ((int)blockIdx.x < colblocks) {
-        if (acc) {
-            visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[cur]}, e);
-        } else {
-            for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock)
-                e.finish(j, e.atyo[j], e.pre(j));
-        }
-    } else if (acc) {
+    if (acc) {
+        visit_bins<1, V>(a.cols, blockIdx.x, a.csc, GatherOne<V>{a.Y[cur]}, e);
+        // the dual average's running sum, in the same blocks (extra blocks for it ran
+        // as a second wave after the columns; it adds nothing to the step partials)
         const V* yc = a.Y[cur];
-        for (int i = (blockIdx.x - colblocks) * kBlock + threadIdx.x; i < a.m; i += a.col_tail_blocks * kBlock)
+        for (int i = blockIdx.x * kBlock + threadIdx.x; i < a.m; i += colblocks * kBlock)
             a.ys[i] += wgt * (yc[i] - a.yl[i]);
+    } else {
+        for (int j = blockIdx.x * kBlock + threadIdx.x; j < a.n; j += colblocks * kBlock)
+            e.finish(j, e.atyo[j], e.pre(j));
     }
     if constexpr (Pdl) grid_dep_launch_dependents();
     V v[1] = {e.dx2};
