@@ -93,7 +93,9 @@ def make_options(mode="adaptive", precision="fp32", max_iters=MAX_PDHG_ITERS, to
                  max_blocks=0, escalate="fp64", warm_fallback=True, kkt_form="lagrangian") -> N.Options:
     """Options for ``sps_create``.  ``escalate`` (adaptive FP32): "fp64" continues a
     stalled solve in FP64 from its best point, "stop" ends it with status
-    "stalled", "off" keeps iterating in FP32.  ``warm_fallback``: start cold when
+    "stalled", "off" keeps iterating in FP32 (a single LP counts as stalled only
+    once its best relative KKT error is at most 1e-3 and has not halved for
+    max(2048, k/2) attempts since, k the attempt of the last halving).  ``warm_fallback``: start cold when
     a warm start's relative KKT error is above the cold start's.  ``kkt_form``
     (adaptive mode): "lagrangian" puts every finite bound into the dual
     objective; "pdlp" leaves out bounds farther from x_j than |x_j| and counts
