@@ -466,6 +466,7 @@ struct Engine : EngineBase {
                 b.aux = P.units();
                 b.aux2 = P.ntickets;
                 b.slot0 = P.nslots;
+                b.part0 = e - r <= kSegLoadAcquireRows ? 1 : 0;
                 for (int q = r; q < e; ++q) {
                     P.fptr[q] = (int32_t)off;
                     const int64_t len = lens[P.perm[q]];

@@ -617,8 +617,7 @@ SPS_PASS_KERNEL rf_row_step(Args<V> a) {
     visit_bins<1, V>(a.rows, blockIdx.x, a.csr, GatherOne<V>{a.xbar}, e);
     __syncthreads();
     if (threadIdx.x == 0) {
-        __threadfence();
-        last = atomicAdd(&ctl->ticket[T_ROW_STEP], 1u) == gridDim.x - 1;
+        last = ticket_release(&ctl->ticket[T_ROW_STEP]) == gridDim.x - 1;
         if (last) {
             ctl->ticket[T_ROW_STEP] = 0;
             ctl->iters += 1;
@@ -770,8 +769,7 @@ __global__ void __launch_bounds__(kBlock) rf_apply(Args<V> a) {
         }
         __syncthreads();
         if (threadIdx.x == 0) {
-            __threadfence();
-            last = atomicAdd(&ctl->ticket[T_APPLY], 1u) == gridDim.x - 1;
+            last = ticket_release(&ctl->ticket[T_APPLY]) == gridDim.x - 1;
             if (last) {
                 ctl->ticket[T_APPLY] = 0;
                 if (rst) ctl->window = 0;
