@@ -107,13 +107,15 @@ struct Team {
 };
 
 // All threads: barrier over the team with global-memory ordering.  Returns false
-// (for every thread of the block) when the wait timed out.
+// (for every thread of the block) when the wait timed out.  The block's barrier
+// orders its threads' writes before thread 0's release-add, which publishes them
+// to the cluster (a release is cumulative); thread 0's acquire-poll and the
+// closing block barrier make the other blocks' writes visible to every thread.
 __device__ __forceinline__ bool team_barrier(const Team& T) {
     if (T.size <= 1) {
         __syncthreads();
         return true;
     }
-    __threadfence();          // every thread's writes are ordered before the block's arrival
     __syncthreads();
     if (threadIdx.x == 0 && !*T.err) {
         const uint32_t target = (*T.gen + 1) * (uint32_t)T.size;
