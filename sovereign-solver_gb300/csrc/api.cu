@@ -55,24 +55,17 @@ bool check_csr(const int32_t* ptr, const int32_t* idx, const double* val, int32_
 }
 
 // Index of the first item in [0, len) that bad() flags, or len: on host threads
-// over contiguous chunks when len is large.
+// (the set-up's pool) over contiguous chunks when len is large.
 template <class F>
 int64_t first_bad(int64_t len, F bad) {
-    const int64_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(sps::HostPool::kMaxThreads, std::thread::hardware_concurrency()));
     const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(hw, len >> 17));
     std::vector<int64_t> first(nt, len);
-    auto scan = [&](int t) {
+    sps::HostPool::run(nt, [&](int t) {
         const int64_t lo = len * t / nt, hi = len * (t + 1) / nt;
         for (int64_t i = lo; i < hi; ++i)
             if (bad(i)) { first[t] = i; return; }
-    };
-    if (nt == 1) {
-        scan(0);
-    } else {
-        std::vector<std::thread> pool;
-        for (int t = 0; t < nt; ++t) pool.emplace_back(scan, t);
-        for (auto& th : pool) th.join();
-    }
+    });
     return *std::min_element(first.begin(), first.end());
 }
 

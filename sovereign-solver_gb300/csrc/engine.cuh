@@ -200,9 +200,7 @@ __device__ __forceinline__ uint32_t ticket_release(uint32_t* t) {
     return old;
 }
 __device__ __forceinline__ void ticket_acquire(const uint32_t* t) {
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(t) : "memory");
-    (void)v;
+    asm volatile("{\n\t.reg .u32 v;\n\tld.acquire.gpu.global.u32 v, [%0];\n\t}" ::"l"(t) : "memory");
 }
 __device__ __forceinline__ void ticket_acquire_fence() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 

@@ -15,6 +15,7 @@
 #include <thread>
 #include <vector>
 
+#include "host_pool.cuh"
 #include "setup.cuh"
 
 namespace sps {
@@ -250,11 +251,7 @@ struct Engine : EngineBase {
         const int64_t cols = (int64_t)j1 - j0;
         const int nt = (int)std::min<int64_t>(std::max(1u, std::min(16u, std::thread::hardware_concurrency())),
                                               std::max<int64_t>(1, cols / 4096));
-        if (nt <= 1) { work(j0, j1); return; }
-        std::vector<std::thread> pool;
-        for (int t = 0; t < nt; ++t)
-            pool.emplace_back(work, (int32_t)(j0 + cols * t / nt), (int32_t)(j0 + cols * (t + 1) / nt));
-        for (auto& th : pool) th.join();
+        HostPool::run(nt, [&](int t) { work((int32_t)(j0 + cols * t / nt), (int32_t)(j0 + cols * (t + 1) / nt)); });
     }
 
     // Blocks of one launch over the bins: one resident wave (block_cap) shared by
@@ -319,17 +316,15 @@ struct Engine : EngineBase {
     }
 
     // Host threads for a loop over R items (one below 2^17 items), and the loop over
-    // nt contiguous chunks, chunk t on thread t.
+    // nt contiguous chunks, chunk t on one of the pool's threads.
     static int host_threads(int64_t R) {
-        const int64_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+        const int64_t hw = std::max<int64_t>(1, std::min<int64_t>(HostPool::kMaxThreads, std::thread::hardware_concurrency()));
         return (int)std::max<int64_t>(1, std::min<int64_t>(hw, R >> 17));
     }
     template <class F>
     static void for_chunks(int64_t R, int nt, F f) {
         if (nt <= 1) { f(0, 0, (int)R); return; }
-        std::vector<std::thread> pool;
-        for (int t = 0; t < nt; ++t) pool.emplace_back(f, t, (int)(R * t / nt), (int)(R * (t + 1) / nt));
-        for (auto& th : pool) th.join();
+        HostPool::run(nt, [&](int t) { f(t, (int)(R * t / nt), (int)(R * (t + 1) / nt)); });
     }
 
     // out[0] = 0, out[i + 1] = out[i] + len(i): chunk sums on host threads, then
