@@ -208,6 +208,11 @@ int sps_time_gather_floor(int64_t nnz, int32_t vec_len, int32_t reps, int32_t de
 /* Message of the last error on this handle (or of the last failed sps_create when h is NULL). */
 const char *sps_last_error(const sps_handle *h);
 
+/* Release the handle (the reference's DeviceEngine, solver/lp/pdhg_gpu.py:72,
+ * is released by garbage collection).  Its device memory returns to the library's
+ * memory pool of the CUDA context, which keeps up to 8 GiB of freed memory
+ * mapped for later sps_create calls; memory beyond that goes back to the
+ * system at the next synchronisation. */
 void sps_destroy(sps_handle *h);
 
 /* Page-lock / release caller host memory so uploads run at full link speed. */

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "host_pool.cuh"
+#include "mem_pool.cuh"
 #include "setup.cuh"
 
 namespace sps {
@@ -112,6 +113,7 @@ struct Engine : EngineBase {
     double cold_rel = -1.0;      // relative KKT error of the cold start point (cached)
     double eta0 = 1.0, omega0 = 1.0;
     Args<V> args{};
+    cudaMemPool_t pool = nullptr;       // device memory (engine_pool; null: the default pool)
     cudaGraphExec_t win_exec = nullptr, loop_exec = nullptr;
     int64_t launches = 0;
     double setup_ms = 0.0;
@@ -131,6 +133,13 @@ struct Engine : EngineBase {
         if (ev1) cudaEventDestroy(ev1);
         if (evq) cudaEventDestroy(evq);
         if (st) cudaStreamDestroy(st);
+    }
+
+    // stream-ordered allocation on the engine's stream, from the engine's pool
+    template <class T>
+    cudaError_t dalloc(T** p, size_t bytes) {
+        return pool ? cudaMallocFromPoolAsync(reinterpret_cast<void**>(p), bytes, pool, st)
+                    : cudaMallocAsync(reinterpret_cast<void**>(p), bytes, st);
     }
 
     static int grid_for(int64_t work, int per_block = kBlock, int cap = kSms * 16) {
@@ -556,6 +565,7 @@ struct Engine : EngineBase {
         SPS_CK(cudaSetDevice(opt.device));
         cudaGetLastError();   // a stale non-sticky error from an unrelated call must not fail this setup
         SPS_CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        pool = engine_pool(opt.device);
         SPS_CK(cudaEventCreate(&ev0));
         SPS_CK(cudaEventCreate(&ev1));
         SPS_CK(cudaEventCreateWithFlags(&evq, cudaEventDisableTiming));
@@ -573,11 +583,11 @@ struct Engine : EngineBase {
         // ---- staging upload and validation
         int32_t *s_ptr, *s_idx, *s_colcount, *s_err;
         double* s_val;
-        SPS_CK(cudaMallocAsync(&s_ptr, sizeof(int32_t) * (m + 1), st));
-        SPS_CK(cudaMallocAsync(&s_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1), st));
-        SPS_CK(cudaMallocAsync(&s_val, sizeof(double) * std::max<int64_t>(nnz, 1), st));
-        SPS_CK(cudaMallocAsync(&s_colcount, sizeof(int32_t) * (n + 1), st));
-        SPS_CK(cudaMallocAsync(&s_err, sizeof(int32_t), st));
+        SPS_CK(dalloc(&s_ptr, sizeof(int32_t) * (m + 1)));
+        SPS_CK(dalloc(&s_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(dalloc(&s_val, sizeof(double) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(dalloc(&s_colcount, sizeof(int32_t) * (n + 1)));
+        SPS_CK(dalloc(&s_err, sizeof(int32_t)));
         SPS_CK(cudaMemcpyAsync(s_ptr, hp.ptr.data(), sizeof(int32_t) * (m + 1), cudaMemcpyHostToDevice, st));
         {
             int64_t off = 0;
@@ -721,7 +731,7 @@ struct Engine : EngineBase {
         add(&d_wy, sizeof(double) * m);
         size_t total = 0;
         for (auto& p : plan) total += p.second;
-        SPS_CK(cudaMallocAsync(&arena, total, st));
+        SPS_CK(dalloc(&arena, total));
         {
             size_t off = 0;
             for (auto& p : plan) { *p.first = arena + off; off += p.second; }
@@ -732,15 +742,15 @@ struct Engine : EngineBase {
         // ---- internal CSR and CSC temporaries (FP64 values)
         int32_t *t_inv_col, *t_fill, *t_ptr, *t_idx, *t_cptr, *t_cidx;
         double *t_rval, *t_cval, *t_stat;
-        SPS_CK(cudaMallocAsync(&t_inv_col, sizeof(int32_t) * n, st));
-        SPS_CK(cudaMallocAsync(&t_fill, sizeof(int32_t) * n, st));
-        SPS_CK(cudaMallocAsync(&t_ptr, sizeof(int32_t) * (m + 1), st));
-        SPS_CK(cudaMallocAsync(&t_cptr, sizeof(int32_t) * (n + 1), st));
-        SPS_CK(cudaMallocAsync(&t_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1), st));
-        SPS_CK(cudaMallocAsync(&t_cidx, sizeof(int32_t) * std::max<int64_t>(nnz, 1), st));
-        SPS_CK(cudaMallocAsync(&t_rval, sizeof(double) * std::max<int64_t>(nnz, 1), st));
-        SPS_CK(cudaMallocAsync(&t_cval, sizeof(double) * std::max<int64_t>(nnz, 1), st));
-        SPS_CK(cudaMallocAsync(&t_stat, sizeof(double) * 2 * (size_t)(n + m), st));
+        SPS_CK(dalloc(&t_inv_col, sizeof(int32_t) * n));
+        SPS_CK(dalloc(&t_fill, sizeof(int32_t) * n));
+        SPS_CK(dalloc(&t_ptr, sizeof(int32_t) * (m + 1)));
+        SPS_CK(dalloc(&t_cptr, sizeof(int32_t) * (n + 1)));
+        SPS_CK(dalloc(&t_idx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(dalloc(&t_cidx, sizeof(int32_t) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(dalloc(&t_rval, sizeof(double) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(dalloc(&t_cval, sizeof(double) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(dalloc(&t_stat, sizeof(double) * 2 * (size_t)(n + m)));
         SPS_CK(cudaMemcpyAsync(d_perm_row, perm_row.data(), sizeof(int32_t) * m, cudaMemcpyHostToDevice, st));
         SPS_CK(cudaMemcpyAsync(d_perm_col, perm_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
         SPS_CK(cudaMemcpyAsync(t_inv_col, inv_col.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st));
@@ -818,8 +828,8 @@ struct Engine : EngineBase {
         SPS_CK(cudaStreamSynchronize(st));
         cudaFreeAsync(t_stat, st);
         V *t_rvV, *t_cvV;
-        SPS_CK(cudaMallocAsync(&t_rvV, sizeof(V) * std::max<int64_t>(nnz, 1), st));
-        SPS_CK(cudaMallocAsync(&t_cvV, sizeof(V) * std::max<int64_t>(nnz, 1), st));
+        SPS_CK(dalloc(&t_rvV, sizeof(V) * std::max<int64_t>(nnz, 1)));
+        SPS_CK(dalloc(&t_cvV, sizeof(V) * std::max<int64_t>(nnz, 1)));
         k_finish_values<V><<<warp_grid_m, kBlock, 0, st>>>(t_ptr, t_idx, t_rval, d_dr, d_dc, t_rvV, m);
         k_finish_values<V><<<warp_grid_n, kBlock, 0, st>>>(t_cptr, t_cidx, t_cval, d_dc, d_dr, t_cvV, n);
         SPS_CK(cudaGetLastError());
@@ -841,7 +851,7 @@ struct Engine : EngineBase {
         // ---- vectors in internal order (uploaded in the caller's order, permuted on the device)
         {
             double *t_c, *t_l, *t_u, *t_b;
-            SPS_CK(cudaMallocAsync(&t_c, sizeof(double) * (3 * (size_t)n + m), st));
+            SPS_CK(dalloc(&t_c, sizeof(double) * (3 * (size_t)n + m)));
             t_l = t_c + n; t_u = t_l + n; t_b = t_u + n;
             SPS_CK(cudaMemcpyAsync(t_c, hp.c, sizeof(double) * n, cudaMemcpyHostToDevice, st));
             SPS_CK(cudaMemcpyAsync(t_l, hp.lb, sizeof(double) * n, cudaMemcpyHostToDevice, st));
@@ -865,7 +875,7 @@ struct Engine : EngineBase {
         {
             const int g = kSms * 2;
             double* t_n;
-            SPS_CK(cudaMallocAsync(&t_n, sizeof(double) * 3 * g, st));
+            SPS_CK(dalloc(&t_n, sizeof(double) * 3 * g));
             k_norms<V><<<g, kBlock, 0, st>>>(d_rval, rp.total, d_c, n, d_b, m, t_n);
             std::vector<double> hn(3 * g);
             SPS_CK(cudaMemcpyAsync(hn.data(), t_n, sizeof(double) * 3 * g, cudaMemcpyDeviceToHost, st));
