@@ -81,6 +81,10 @@ def check_plan(tool, tmp, ptr, idx, kind, n, inv_col, cap=760, seed=0, cols=Fals
     fidx = np.full(max(total, 1), -1, np.int64)
     fval = np.full(max(total, 1), np.nan)
     for (beg, end, mode, _k, _bb, _nb, units, aux, _a2, slice0, part0, _s0) in B:
+        if mode == SEGMENT:
+            # a row's last segment acquires by a load of its ticket in bins of at most
+            # 4096 rows, by a fence in larger ones (engine.cuh kSegLoadAcquireRows)
+            assert part0 == (1 if end - beg <= 4096 else 0)
         if mode in (SLICED, SLAB):
             first, nsl = (aux, units) if mode == SLICED else (slice0, (end - beg + 31) // 32)
             for s in range(nsl):
@@ -285,3 +289,19 @@ def test_column_plans(plan_tool, tmp_path, cap):
     M = sp.csr_matrix((np.ones(ptr[-1]), np.concatenate(rows), ptr), shape=(m, n)).T.tocsr()
     bins = check_plan(plan_tool, str(tmp_path), M.indptr, M.indices, [0] * n, m, np.arange(m), cap=cap, cols=True)
     assert {b[0] for b in bins} <= {SLICED, WARP, SEGMENT} and {b[1] for b in bins} == {0}
+
+
+def test_segment_bin_acquire_choice(plan_tool, tmp_path):
+    """SEGMENT rows: a bin of at most 4096 rows has its rows' last segments acquire
+    by a load of the row ticket (part0 = 1), a larger bin by a fence (part0 = 0);
+    the plan only, without the traversal replay (2.2M entries)."""
+    rng = np.random.default_rng(11)
+    n = 20000
+    for m, want in ((4096, 1), (4200, 0)):
+        lens = np.full(m, 520)                       # two segments per row, random columns
+        idx = np.concatenate([rng.choice(n, 520, replace=False) for _ in range(m)])
+        ptr = np.concatenate([[0], np.cumsum(lens)])
+        P = run_plan(plan_tool, str(tmp_path), ptr, idx, [0] * m, n, np.arange(n), 760)
+        seg = [b for b in P["bins"] if b[2] == SEGMENT]
+        assert len(seg) == 1 and seg[0][1] - seg[0][0] == m
+        assert seg[0][10] == want
