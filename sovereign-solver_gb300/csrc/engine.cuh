@@ -562,6 +562,12 @@ __device__ __forceinline__ void finish_segment(const Bin& b, int gseg, int r, in
 // slot order.
 template <int NP, class T, class V>
 __device__ __forceinline__ void add_segment_rows(T (&tot)[NP], const Layout<V>& L, T* smem) {
+    if (L.nsegrows == 0) {     // (block-uniform) the block sum of no slots is +0: add that alone
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) tot[p] += T(0);
+        return;
+    }
     // B rows' loads are issued before their adds: B round trips overlap instead
     // of one L2 round trip per row (fixed order, so the sum stays deterministic)
     constexpr int B = NP <= 2 ? 8 : 2;
@@ -630,6 +636,12 @@ __device__ __forceinline__ void gather_all_partials(T (&tot)[NP], const T* parti
             for (int p = 0; p < NP; ++p) tot[p] += v[u][p];
     }
     block_sum<NP>(tot, smem);
+    if (L.nsegrows == 0) {     // (block-uniform) as add_segment_rows: the slots' block sum is +0
+        if (threadIdx.x == 0)
+#pragma unroll
+            for (int p = 0; p < NP; ++p) tot[p] += T(0);
+        return;
+    }
     T sacc[NP];
 #pragma unroll
     for (int p = 0; p < NP; ++p) sacc[p] = T(0);
