@@ -596,7 +596,8 @@ __device__ __forceinline__ void add_segment_rows(T (&tot)[NP], const Layout<V>& 
 
 // In a kernel's last block: gather_partials followed by add_segment_rows, with
 // the first round of both's loads issued together (one L2 round trip fewer on
-// the serial tail of the pass); the same additions in the same order.
+// the serial tail of the pass); the same additions in the same order.  smem
+// holds kWarps * 2 * NP values.
 template <int NP, class T, class V>
 __device__ __forceinline__ void gather_all_partials(T (&tot)[NP], const T* partials, int nblk,
                                                     const Layout<V>& L, T* smem) {
@@ -635,8 +636,8 @@ __device__ __forceinline__ void gather_all_partials(T (&tot)[NP], const T* parti
 #pragma unroll
             for (int p = 0; p < NP; ++p) tot[p] += v[u][p];
     }
-    block_sum<NP>(tot, smem);
     if (L.nsegrows == 0) {     // (block-uniform) as add_segment_rows: the slots' block sum is +0
+        block_sum<NP>(tot, smem);
         if (threadIdx.x == 0)
 #pragma unroll
             for (int p = 0; p < NP; ++p) tot[p] += T(0);
@@ -662,10 +663,18 @@ __device__ __forceinline__ void gather_all_partials(T (&tot)[NP], const T* parti
 #pragma unroll
             for (int p = 0; p < NP; ++p) sacc[p] += v[u][p];
     }
-    block_sum<NP>(sacc, smem);
+    // both block sums in one reduction (every value has its own fixed tree, so
+    // these are the same sums as two reductions; one round of barriers fewer)
+    T both[2 * NP];
+#pragma unroll
+    for (int p = 0; p < NP; ++p) {
+        both[p] = tot[p];
+        both[NP + p] = sacc[p];
+    }
+    block_sum<2 * NP>(both, smem);
     if (threadIdx.x == 0)
 #pragma unroll
-        for (int p = 0; p < NP; ++p) tot[p] += sacc[p];
+        for (int p = 0; p < NP; ++p) tot[p] = both[p] + both[NP + p];
 }
 
 // SLAB: unit u of the bin = steps [c S, min(L, (c+1) S)) of slice s (S =

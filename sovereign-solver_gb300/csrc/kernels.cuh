@@ -151,7 +151,7 @@ SPS_PASS_KERNEL ad_row_step(Args<V> a) {
     }
     Ctl* ctl = a.ctl;
     if (ctl->done || ctl->iters >= ctl->max_iters) return;
-    __shared__ V sm[kWarps * 2];
+    __shared__ V sm[kWarps * 4];
     __shared__ bool last;
     const int cur = ctl->cur;
     const V sigma = block_scalar<V>([&] { return ctl->eta * ctl->omega; });
@@ -224,7 +224,7 @@ SPS_PASS_KERNEL ad_col_step(Args<V> a) {
     }
     Ctl* ctl = a.ctl;
     if (ctl->apply != AP_STEP_PENDING) return;
-    __shared__ V sm[kWarps];
+    __shared__ V sm[kWarps * 2];
     __shared__ bool last;
     const int cur = ctl->cur;
     const bool acc = ctl->accepted;
