@@ -156,3 +156,25 @@ def test_gather_floor_rejects_bad_arguments():
     for args in ((0, 10, 1), (100, 0, 1), (100, 10, 0)):
         assert lib.sps_time_gather_floor(args[0], args[1], args[2], 0, N.f64p(out)) == -1
     assert lib.sps_time_gather_floor(100, 10, 1, 0, None) == -1
+
+
+def test_create_validation_names_the_first_bad_variable():
+    """sps_create's validation scans (on the set-up's host worker pool for large
+    inputs) report the first invalid variable whichever thread's chunk finds it;
+    the call returns before any device work, so it runs without a GPU."""
+    import ctypes as C
+    from sovereign_solver_gb300 import _native as N
+    n = 300_000
+    lb, ub = np.zeros(n), np.full(n, np.inf)
+    lb[[250_000, 200_123, 299_999]] = [5.0, 3.0, np.inf]      # lb > ub, lb > ub, lb = +inf
+    ub[[250_000, 200_123]] = 1.0
+    p = sps.Problem(c=np.ones(n), A_ub=sp.csr_matrix((np.ones(n), (np.zeros(n, int), np.arange(n))), shape=(1, n)),
+                    b_ub=np.array([1.0]), A_eq=sp.csr_matrix((0, n)), b_eq=np.zeros(0), lb=lb, ub=ub,
+                    integer_mask=np.zeros(n, bool))
+    lib = N.load()
+    d = pdhg._Desc(p)
+    h = C.c_void_p()
+    for _ in range(3):                                        # the pool is reused between calls
+        rc = lib.sps_create(C.byref(d.desc), C.byref(pdhg.make_options()), C.byref(h))
+        assert rc == -1 and not h.value
+        assert lib.sps_last_error(None).decode() == "invalid bounds at variable 200123"
