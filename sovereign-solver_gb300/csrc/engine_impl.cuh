@@ -199,7 +199,12 @@ struct Engine : EngineBase {
             std::vector<int32_t> rows;
             for (int i = 0; i < m; ++i)
                 if (hp.kind[i] == kd && hp.ptr[i + 1] - hp.ptr[i] > kSliceMax) rows.push_back(i);
-            for (size_t g = 0; g < rows.size(); g += 32) {
+            // groups of 32 rows are scored independently: on the host pool, a range
+            // of groups per thread (each group's rows are marked by its own thread)
+            const int64_t ngroups = ((int64_t)rows.size() + 31) / 32;
+            const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(HostPool::kMaxThreads, ngroups / 8));
+            HostPool::run(nt, [&](int th) {
+            for (size_t g = 32 * (size_t)(ngroups * th / nt); g < 32 * (size_t)(ngroups * (th + 1) / nt) && g < rows.size(); g += 32) {
                 const int cnt = (int)std::min<size_t>(32, rows.size() - g);
                 int64_t lmin = INT64_MAX, lmax = 0, stored = 0;
                 for (int t = 0; t < cnt; ++t) {
@@ -228,6 +233,7 @@ struct Engine : EngineBase {
                 if (slab_cost <= 0.5 * csr_cost)
                     for (int t = 0; t < cnt; ++t) slab[rows[g + t]] = 1;
             }
+            });
         }
         return slab;
     }
@@ -616,7 +622,9 @@ struct Engine : EngineBase {
         if (trace) trace->mark("upload + validate");
         // ---- column plan
         std::vector<int64_t> clen(n);
-        for (int j = 0; j < n; ++j) clen[j] = colcount[j];
+        for_chunks(n, host_threads(n), [&](int, int lo, int hi) {
+            for (int j = lo; j < hi; ++j) clen[j] = colcount[j];
+        });
         Plan cp;
         if (trace) trace->mark("  column lengths");
         make_plan(clen, nullptr, nullptr, cp, block_cap, trace);
