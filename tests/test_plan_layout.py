@@ -305,3 +305,13 @@ def test_segment_bin_acquire_choice(plan_tool, tmp_path):
         seg = [b for b in P["bins"] if b[2] == SEGMENT]
         assert len(seg) == 1 and seg[0][1] - seg[0][0] == m
         assert seg[0][10] == want
+
+
+def test_many_slab_groups(plan_tool, tmp_path):
+    """600 demand rows of 40 entries (stride-40 columns): 19 groups of up to 32
+    rows, scored on two host-pool threads (the SLAB choice runs its groups in
+    parallel from 16 groups on); every group takes SLAB and the traversal replay
+    checks the layout."""
+    ptr, idx, kind, n = transport(40, 600)
+    bins = check_plan(plan_tool, str(tmp_path), ptr, idx, kind, n, np.arange(n))
+    assert (SLAB, 0, 600) in bins and (SEGMENT, 1, 40) in bins
