@@ -154,8 +154,8 @@ def problem_bytes(p) -> int:
 # from one ncu capture per workload (seed 0, FP32 adaptive; --graph-mode 0 so the
 # kernels are separate launches): the transportation LP 1000 x 2000 and the
 # power-law LP rescaled to ~20M nonzeros.
-MEASURED_TRAFFIC = {1: {"row": 40.44e6 + 0.00e6, "col": 64.88e6 + 1.65e6},
-                    2: {"row": 189.5e6 + 6.9e6, "col": 228.3e6 + 15.5e6}}
+MEASURED_TRAFFIC = {1: {"row": 40.44e6 + 0.00e6, "col": 64.88e6 + 1.20e6},
+                    2: {"row": 189.54e6 + 7.03e6, "col": 228.30e6 + 16.03e6}}
 
 
 def iteration_bytes(p) -> dict:
